@@ -1,0 +1,377 @@
+"""Benchmark: energy-point solves/s of the per-energy NEGF solve at M = 400.
+
+Workload ("ti_wire_M400_Npx100"): the 4-band TI nanowire with Npy = Npz = 10 (M = 400),
+Npx = 100, axial flux 0.5 Phi_0 (Peierls phases on the y hops), Zeeman 0.01 eV, Anderson
+disorder W = 0.1 eV with 4 seeds (4 Hamiltonian slots, 1 GB of complex128 on the device),
+eta = 1e-5, Sancho-Rubio tolerance 1e-10, kT = 0.025 eV, mu_L - mu_R = 0.01 eV, energies
+from the 512-point grid in [-0.3, 0.3] eV.  Synthetic, seeded inputs of the stated
+shapes (no dataset exists for this workload).
+
+One step = one batch of --batch requests (consecutive grid energies, seeds round-robin),
+solved through negf_solve_batch with the Hamiltonians resident in HBM.  `value` is
+solves/s over K steps timed with CUDA events on the stream the library launches on.
+`e2e` repeats the steps through the public API with host buffers: every step uploads the
+4 Hamiltonians from pinned host memory and reads the results back.
+
+--impl reference times the CPU restatement of the reference algorithm (oracle/) on this
+host's cores on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+import numpy as np  # noqa: E402
+
+WORKLOAD = "ti_wire_M400_Npx100"
+NPX, NPY, NPZ = 100, 10, 10
+SEEDS = 4
+N_E = 512
+ETA, SR_TOL, KT = 1e-5, 1e-10, 0.025
+MU = (0.005, -0.005)
+FLUX, ZEEMAN, W = 0.5, 0.01, 0.1
+METRIC = "energy-point solves/s at M=400 (mixed vs FP64, T err<=1e-6)"
+
+
+def energy_grid():
+    return np.linspace(-0.3, 0.3, N_E)
+
+
+def fermi(e, mu, kt):
+    x = (e - mu) / kt
+    return 0.0 if x > 700 else 1.0 / (1.0 + math.exp(x))
+
+
+def step_requests(step, batch, rank, world):
+    """Requests of one step: consecutive grid energies, seeds round-robin; ranks take
+    disjoint energies (the units are independent, no exchange between ranks)."""
+    grid = energy_grid()
+    idx = [((step * world + rank) * batch + i) % N_E for i in range(batch)]
+    e = grid[idx]
+    slots = np.array([(step * batch + i) % SEEDS for i in range(batch)], dtype=np.int32)
+    f1 = np.array([fermi(x, MU[0], KT) for x in e])
+    f2 = np.array([fermi(x, MU[1], KT) for x in e])
+    return e, f1, f2, slots
+
+
+def algorithmic_flops_per_solve(m, npx, n_sr, n_seeds_sharing=SEEDS):
+    """Work model of the solve (real flops), per energy point:
+    RGF: per slice 2 inverses + 4 complex GEMMs (column 1, column N, G Gamma_L, G Gamma_R),
+    each 8 M^3 -> 48 M^3 per slice (HopX products are site-local, O(M^2));
+    Sancho-Rubio: per iteration 10 GEMMs + 1 inverse (both leads share t, t~) = 88 M^3,
+    plus 3 inverses at set-up/final = 24 M^3, shared by the seeds at one energy;
+    traces: 4 GEMMs = 32 M^3."""
+    m3 = float(m) ** 3
+    rgf = 48.0 * m3 * npx
+    sr = (88.0 * n_sr + 24.0) * m3 / n_seeds_sharing
+    return rgf + sr + 32.0 * m3
+
+
+class ClockSampler:
+    def __init__(self, path):
+        self.path = path
+        self.proc = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + q, "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self, device_index):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": []}
+        try:
+            rows = [ln.split(",") for ln in open(self.path).read().strip().splitlines()]
+        except Exception:
+            return out
+        rows = [[c.strip() for c in r] for r in rows if len(r) >= 9 and r[0].strip() == str(device_index)]
+        if not rows:
+            return out
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in rows:
+            for name, v in zip(names, r[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        out["sm_mhz"] = statistics.median(sm) if sm else None
+        out["sm_max_mhz"] = max(mx) if mx else None
+        out["reasons"] = sorted(reasons)
+        out["samples"] = len(rows)
+        return out
+
+
+def measured_peaks():
+    try:
+        return json.load(open(os.path.join(REPO, "MEASURED_PEAKS.json")))
+    except Exception:
+        return {}
+
+
+def fp64_zgemm_peak_tflops(torch, device):
+    """FP64 denominator for the FP64 form: cuBLAS ZGEMM (complex128, 4096^3) measured live."""
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.complex128, device=device)
+    b = torch.randn(n, n, dtype=torch.complex128, device=device)
+    for _ in range(2):
+        torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 0.0
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = max(best, 8.0 * n ** 3 / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+    del a, b
+    torch.cuda.empty_cache()
+    return best
+
+
+def build_hamiltonians():
+    from nonequilibriumgreensfunction_gb300 import hamiltonian as HB
+    hams = []
+    for seed in range(SEEDS):
+        h, x = HB.ti_wire(NPX, NPY, NPZ, zeeman=ZEEMAN, flux=FLUX, W=W, seed=seed)
+        hams.append((h, x))
+    return hams
+
+
+def cpu_sample(n_energies=1):
+    """The oracle (CPU restatement of the reference algorithm) on a bounded sample: the
+    first n_energies requests of step 0 at full size.  Returns (solves/s, threads, text)."""
+    from oracle import negf_oracle as O
+    from nonequilibriumgreensfunction_gb300 import hamiltonian as HB
+    e, f1, f2, slots = step_requests(0, n_energies, 0, 1)
+    opt = O.SolveOptions(eta=ETA, sr_tol=SR_TOL, kT=KT, calc_spin=True)
+    hams = {s: HB.ti_wire(NPX, NPY, NPZ, zeeman=ZEEMAN, flux=FLUX, W=W, seed=s) for s in set(int(v) for v in slots)}
+    t0 = time.perf_counter()
+    for i in range(n_energies):
+        h, x = hams[int(slots[i])]
+        O.energy_sweep(h, x, float(e[i]), MU, 0.6 / (N_E - 1), NPY, NPZ, opt)
+    dt = time.perf_counter() - t0
+    threads = os.cpu_count() or 1
+    return n_energies / dt, threads, ("%d energy point(s) of the workload at full size (M=400, Npx=100), "
+                                      "NumPy/OpenBLAS on all host threads" % n_energies)
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    from oracle import negf_oracle as O
+    from nonequilibriumgreensfunction_gb300 import hamiltonian as HB
+    opt = O.SolveOptions(eta=ETA, sr_tol=SR_TOL, kT=KT, calc_spin=True)
+    hams = {}
+    times = []
+    per_step = 1
+    # warm-up steps exercise the same code on a 4-slice wire (a CPU path has nothing to
+    # warm but its caches); timed steps solve full-size energy points
+    hw, xw = HB.ti_wire(4, NPY, NPZ, zeeman=ZEEMAN, flux=FLUX, W=W, seed=0)
+    for step in range(args.warmup):
+        O.energy_sweep(hw, xw, float(energy_grid()[step % N_E]), MU, 0.6 / (N_E - 1), NPY, NPZ, opt)
+    for step in range(args.steps):
+        e, f1, f2, slots = step_requests(step, per_step, 0, 1)
+        for s in set(int(v) for v in slots):
+            if s not in hams:
+                hams[s] = HB.ti_wire(NPX, NPY, NPZ, zeeman=ZEEMAN, flux=FLUX, W=W, seed=s)
+        t0 = time.perf_counter()
+        for i in range(per_step):
+            h, x = hams[int(slots[i])]
+            O.energy_sweep(h, x, float(e[i]), MU, 0.6 / (N_E - 1), NPY, NPZ, opt)
+        times.append(time.perf_counter() - t0)
+    total = sum(times)
+    value = per_step * len(times) / total
+    threads = os.cpu_count() or 1
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * total / len(times), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "batch": per_step, "form": "cpu-oracle"},
+        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": threads, "kind": "port",
+                         "sample": "%d energy point per step at full size (M=400, Npx=100), NumPy/OpenBLAS "
+                                   "restatement of the reference algorithm on all host threads" % per_step},
+        "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--form", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--batch", type=int, default=16)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+
+    import torch
+    import torch.distributed as dist
+    from nonequilibriumgreensfunction_gb300 import Solver
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=dev)
+
+    hams = build_hamiltonians()
+    m = 4 * NPY * NPZ
+    solver = Solver(NPX, NPY, NPZ, n_hamiltonians=SEEDS, max_batch=args.batch, eta=ETA, sr_tol=SR_TOL,
+                    calc_spin=True, precision=args.form, device=local_rank)
+    stream = torch.cuda.Stream(dev)          # a real stream handle, so events bracket the work
+    torch.cuda.set_stream(stream)
+    solver.set_stream(stream.cuda_stream)
+    # pinned host copies of the inputs in the reference's memory layout (for e2e)
+    pinned = []
+    for h, x in hams:
+        hf = torch.empty((NPX, m, m), dtype=torch.complex128, pin_memory=True).numpy()
+        hf[...] = h.transpose(0, 2, 1)
+        xf = np.asfortranarray(x)
+        pinned.append((hf, xf))
+    for k, (hf, xf) in enumerate(pinned):
+        solver.set_hamiltonian_fortran(hf, xf, slot=k)
+
+    nsites = NPX * NPY * NPZ
+    rho_n = np.zeros((NPX, NPY, NPZ, SEEDS), order="F")
+    rho_p = np.zeros_like(rho_n)
+    spin = [np.zeros_like(rho_n) for _ in range(3)]
+
+    def one_step(step):
+        e, f1, f2, slots = step_requests(step, args.batch, rank, world)
+        return solver.solve_batch(e, f1, f2, 0.6 / (N_E - 1), slots=slots, rho_n=rho_n, rho_p=rho_p, spin=spin)
+
+    for s in range(args.warmup):
+        r = one_step(s)
+        assert (r["status"] == 0).all(), r["status"]
+    sr_iters = int(np.max(r["sr_iters"]))
+
+    clocks_path = os.path.join(REPO, "gpurun_out", "bench_clocks_rank%d.csv" % rank)
+    os.makedirs(os.path.dirname(clocks_path), exist_ok=True)
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    solver.profile(True)
+    with ClockSampler(clocks_path) as clk:
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for s in range(args.steps):
+            r = one_step(args.warmup + s)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    st = solver.stats()
+    solver.profile(False)
+    elapsed = ev0.elapsed_time(ev1) * 1e-3
+    if world > 1:
+        t = torch.tensor([elapsed], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed = float(t.item())
+        dist.barrier()
+    solves = args.batch * args.steps * world
+    value = solves / elapsed
+
+    # e2e: through the public API with host buffers, upload + solve + readback each step
+    e2e = None
+    if not args.no_e2e:
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        ev2, ev3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev2.record(stream)
+        for s in range(args.steps):
+            for k, (hf, xf) in enumerate(pinned):
+                solver.set_hamiltonian_fortran(hf, xf, slot=k)
+            one_step(args.warmup + s)
+        ev3.record(stream)
+        torch.cuda.synchronize()
+        el2 = ev2.elapsed_time(ev3) * 1e-3
+        if world > 1:
+            t = torch.tensor([el2], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            el2 = float(t.item())
+        h2d = sum(hf.nbytes + xf.nbytes for hf, xf in pinned) + args.batch * 40
+        d2h = args.batch * 64 + 5 * nsites * SEEDS * 8
+        e2e = {"value": args.batch * args.steps * world / el2, "unit": "solves/s",
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)}
+
+    if rank != 0:
+        if world > 1:
+            dist.destroy_process_group()
+        return
+
+    peaks = measured_peaks()
+    fp64_peak = fp64_zgemm_peak_tflops(torch, dev)
+    gemm_tf = st["gemm_flops"] / (st["gemm_ms"] * 1e-3) / 1e12 if st["gemm_ms"] > 0 else None
+    roofline = {
+        "bound": "tensor", "kernel": "zgemm_kernel (FP64 complex GEMM, DFMA)",
+        "achieved": gemm_tf, "peak": fp64_peak, "unit": "TFLOP/s",
+        "frac": (gemm_tf / fp64_peak) if gemm_tf else None, "traffic": None,
+        "peak_source": "cuBLAS ZGEMM 4096^3 complex128 measured live (of measured)",
+        "gemm_launches": st["gemm_launches"], "gemm_share_of_step": st["gemm_ms"] * 1e-3 / elapsed,
+    }
+    flops_solve = algorithmic_flops_per_solve(m, NPX, sr_iters)
+    cpu = None
+    if not args.no_cpu_baseline and world == 1:
+        v, cores, sample = cpu_sample(1)
+        cpu = {"value": v, "unit": "solves/s", "cores": cores, "kind": "port", "sample": sample}
+    line = {
+        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c128" if args.form == "fp64" else "bf16-sliced/c128",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "M": m, "npx": NPX, "seeds": SEEDS, "batch_per_gpu": args.batch,
+                   "form": args.form, "eta": ETA, "sr_tol": SR_TOL, "l2": "inputs larger than L2 (1 GB H, "
+                   "%.1f GB block store)" % (args.batch * NPX * m * m * 16 / 1e9), "parallelism": "energy-sharded x%d" % world},
+        "roofline": roofline,
+        "solve_tflops": flops_solve * value / 1e12 / world,
+        "algorithmic_flops_per_solve": flops_solve,
+        "sr_iters": sr_iters,
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": st["launches"],
+        "clocks": clk.summary(local_rank),
+        "peaks_file": {k: peaks.get(k) for k in ("hbm_gbs", "bf16_tflops", "bf16_tflops_sustained")},
+    }
+    print(json.dumps(line), flush=True)
+    solver.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

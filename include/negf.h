@@ -1,0 +1,184 @@
+/*
+ * negf.h - C ABI of libnegf_gb300.so, the GB300 (sm_103a) implementation of the
+ * per-energy NEGF solve of brian-dellabetta/nonEquilibriumGreensFunction.
+ *
+ * The reference's hot path is four argument-less Fortran subroutines that read and
+ * write NEGF_Module globals, called once per energy point by Energy_Sweep
+ * (Source/Energy_Sweep.F90:28,40,42,45).  This header replaces them with calls that
+ * take the same data explicitly: plain pointers to the caller's column-major arrays,
+ * sizes, and an opaque handle that owns every device buffer.
+ *
+ * Conventions
+ *  - Complex arrays are interleaved (re, im) doubles, i.e. the memory layout of Fortran
+ *    COMPLEX(8) / C double _Complex.  A "block" is an M x M column-major complex
+ *    matrix, M = norb*npy*npz (NNz in Source/Read_In_Allocate.F90:96-97).
+ *  - Htotd is M x M x npx (Source/NEGF_Module.F90:56), HopX is M x M (:57) and is the
+ *    coupling H(x, x+1); H(x+1, x) = HopX^H (Source/Recursive_Greens.F90:6).
+ *  - Site arrays (RhoN, RhoP, SigXExp, ...) are npx x npy x npz, column-major
+ *    (x fastest), as Source/NEGF_Module.F90:51-52.  In-slice orbital index is
+ *    orb + y*norb + z*norb*npy (Source/Calculate_Gnp.F90:122).
+ *  - Every entry point returns int: 0 = success; > 0 = LAPACK-style INFO (1-based
+ *    index of the first exactly-zero pivot of an inverse, as ZGETRF/ZGETRI report it
+ *    through Invert_Matrix, Source/MKL_Routines_Cluster.F90:17-28); < 0 = NEGF_E*.
+ *    No entry point aborts, exits or traps.
+ *  - A handle is used by one host thread at a time; separate handles are independent.
+ *  - There is no CPU fallback: if no CUDA device is present, negf_create returns
+ *    NEGF_ENODEV.
+ */
+#ifndef NEGF_GB300_H
+#define NEGF_GB300_H
+
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define NEGF_API __attribute__((visibility("default")))
+#else
+#define NEGF_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------------------- */
+#define NEGF_OK            0
+#define NEGF_EINVAL       (-1)   /* bad argument or size                                 */
+#define NEGF_ENOMEM       (-2)   /* device allocation failed                             */
+#define NEGF_ECUDA        (-3)   /* a CUDA runtime call failed                           */
+#define NEGF_ESR_NOCONV   (-4)   /* Sancho-Rubio hit sr_max_iter (Contact_Self_Energy.F90:248-251) */
+#define NEGF_ENAN         (-5)   /* NaN in the Sancho-Rubio update (Contact_Self_Energy.F90:228-237) */
+#define NEGF_ESTATE       (-6)   /* call order violated (e.g. Greens before self-energy) */
+#define NEGF_EADMIT       (-7)   /* request larger than the handle's admission budget    */
+#define NEGF_ETIMEDOUT    (-8)   /* bounded device wait ran out                          */
+#define NEGF_EREFINE      (-9)   /* mixed form: refinement residual above bound          */
+#define NEGF_ENODEV      (-10)   /* no CUDA device                                       */
+#define NEGF_ENOHAM      (-11)   /* Hamiltonian slot never set                           */
+
+/* ---- arithmetic form ------------------------------------------------------------- */
+#define NEGF_PREC_FP64     0     /* plain FP64 complex throughout                        */
+#define NEGF_PREC_MIXED    1     /* tcgen05 BF16 sliced products, FP64 refinement        */
+
+typedef struct negf_params {
+    int32_t npx, npy, npz;   /* lattice (Source/NEGF_Module.F90:26)                      */
+    int32_t norb;            /* orbitals per site; 4 for the TI models                   */
+    int32_t n_hamiltonians;  /* Htotd slots held on the device (e.g. disorder seeds)     */
+    int32_t max_batch;       /* energy points solved together by negf_solve_batch        */
+    double  eta;             /* eta_sigma, Source/Constants.F90:7 (reference 1e-4)       */
+    double  sr_tol;          /* Sancho-Rubio stop: max|change| <= sr_tol (ref. 1e-8)      */
+    int32_t sr_max_iter;     /* Sancho-Rubio iteration cap (reference 20000)             */
+    int32_t calc_spin;       /* calcSigExp, Source/Read_In_Allocate.F90:93               */
+    int32_t precision;       /* NEGF_PREC_*                                              */
+    int32_t device;          /* CUDA device ordinal                                      */
+    int32_t mixed_slices;    /* NEGF_PREC_MIXED: BF16 slices per operand (0 = default)   */
+    int32_t keep_g_columns;  /* 1: keep G(:,1), G(:,N) of the per-energy call for
+                                negf_copy_g_columns (2*Npx*M^2*16 extra device bytes)    */
+    int32_t reserved[6];     /* must be zero                                             */
+    double  spin_ops[3][4][4][2]; /* gMx, gMy, gMz (row-major [row][col][re,im]) used by
+                                     the spin reduction, Source/Read_In_Allocate.F90:183-196;
+                                     all zero = the reference's tau0 (x) sigma_j          */
+} negf_params;
+
+typedef struct negf_handle negf_handle;
+
+/* ---- lifetime -------------------------------------------------------------------- */
+NEGF_API int  negf_create(const negf_params* p, negf_handle** out);
+NEGF_API int  negf_destroy(negf_handle* h);
+NEGF_API const char* negf_strerror(int code);
+/* bytes of device memory the handle holds (for admission / reporting) */
+NEGF_API int  negf_device_bytes(const negf_handle* h, int64_t* bytes);
+
+/* Run the handle's work on a caller-owned CUDA stream (cudaStream_t passed as void*);
+ * NULL restores the handle's own stream.  Calls still return only after their results
+ * are on the host.                                                                     */
+NEGF_API int negf_set_stream(negf_handle* h, void* stream);
+
+/* Instrumentation: launch counts and CUDA-event timings of the dense kernels.  Enabling
+ * resets the counters; timing adds one event pair per timed launch.                    */
+typedef struct negf_stats {
+    int64_t launches;        /* kernels launched by the library since the last reset       */
+    int64_t gemm_launches;   /* complex GEMM launches (also those inside the inverses)     */
+    double  gemm_ms;         /* summed device time of those launches (profiling on)        */
+    double  gemm_flops;      /* their real flops, 8*m*n*k per complex GEMM                 */
+    int64_t panel_launches;  /* Gauss-Jordan panel factorisations                          */
+    double  panel_ms;
+} negf_stats;
+NEGF_API int negf_profile(negf_handle* h, int enable);
+NEGF_API int negf_get_stats(negf_handle* h, negf_stats* out);
+
+/* ---- Hamiltonian upload ------------------------------------------------------------
+ * Replaces the broadcast of Build_Hamiltonian's output to the solvers
+ * (Source/MPI_Routines.F90:19-30).  Htotd: M x M x npx complex, HopX: M x M complex.
+ * HopX is shared by all slots: the call with slot 0 sets it, other slots must pass the
+ * same HopX (or NULL).  Detects whether HopX is block diagonal in norb x norb site
+ * blocks (true for every channel of Source/Build_Hamiltonian.F90:59-64) and then
+ * applies it as a site-local operator instead of a dense product.                     */
+NEGF_API int negf_set_hamiltonian(negf_handle* h, int32_t slot, const double* Htotd, const double* HopX);
+
+/* ---- per-energy interface (one energy point, Hamiltonian slot 0) ---------------------
+ * The four calls below are the drop-in for the reference's subroutines, in the order
+ * Energy_Sweep makes them.  All device results stay in the handle between calls.       */
+
+/* Contact_Self_Energy (Source/Contact_Self_Energy.F90:1-152, contactType 0):
+ * Sancho-Rubio decimation of both semi-infinite leads at `energy`.  Writes SigmaL,
+ * SigmaR, GammaL, GammaR (M x M complex, any may be NULL) and dosc[2] = (DOSc1, DOSc2)
+ * increments (:140-143).  Returns NEGF_ESR_NOCONV / NEGF_ENAN as errorFlag would be set. */
+NEGF_API int negf_contact_self_energy(negf_handle* h, double energy,
+                             double* SigmaL, double* SigmaR, double* GammaL, double* GammaR,
+                             double* dosc);
+
+/* Get_Retarded_Greens (Source/Recursive_Greens.F90:2-107) for the InvGRd that
+ * Energy_Sweep.F90:31-38 assembles from Htotd, energy, eta and the self-energies of the
+ * last negf_contact_self_energy call.  Results (the first and last block columns of G)
+ * stay on the device.  Returns the INFO of the first singular inverse, if any.          */
+NEGF_API int negf_get_retarded_greens(negf_handle* h);
+
+/* Optional copy-out of GRLef = G(:,1) and GRRgt = G(:,N) (Ntot x M complex each,
+ * Source/NEGF_Module.F90:70); either may be NULL.  Debug/parity use only.              */
+NEGF_API int negf_copy_g_columns(negf_handle* h, double* GRLef, double* GRRgt);
+
+/* Calculate_Gnp (Source/Calculate_Gnp.F90:1-136): Gn = f1 G1 GammaL G1^H + f2 GN GammaR GN^H,
+ * Gp with (1-f), and the site densities RhoN/RhoP += Re diag * dE/(2 pi) (:117-124),
+ * accumulated into the caller's npx x npy x npz arrays.                                 */
+NEGF_API int negf_calculate_gnp(negf_handle* h, double f1, double f2, double dE,
+                       double* RhoN, double* RhoP);
+
+/* Calculate_Observables (Source/Calculate_Observables.F90:2-108, non-BdG branch):
+ * writes T12, EDensity, HDensity, modes[2] = (Modec1, Modec2) for this energy, adds the
+ * ContactCurrent increments to contact_current[2], and, if the handle has calc_spin and
+ * the pointers are non-NULL, accumulates SigXExp/SigYExp/SigZExp (npx x npy x npz).      */
+NEGF_API int negf_calculate_observables(negf_handle* h, double dE, double f1, double f2,
+                               double* T12, double* EDensity, double* HDensity,
+                               double* modes, double* contact_current,
+                               double* SigX, double* SigY, double* SigZ);
+
+/* ---- batched interface -------------------------------------------------------------
+ * Many energy points (and Hamiltonian slots, e.g. disorder seeds) in one device pass:
+ * the GB300 replacement for the round-robin energy loop of Source/NEGF_Main.F90:21-27
+ * plus the MPI sums of Source/MPI_Routines.F90:33-90.  n may exceed max_batch; requests
+ * are processed in chunks of max_batch in order.                                       */
+typedef struct negf_request {
+    double  energy;
+    double  f1, f2;          /* lead occupations at this energy (Energy_Sweep.F90:11-23) */
+    double  dE;              /* quadrature weight (Energy_Sweep.F90:7-9)                 */
+    int32_t slot;            /* Hamiltonian slot                                         */
+    int32_t flags;           /* reserved, 0                                              */
+} negf_request;
+
+typedef struct negf_result {
+    double  T12;             /* Calculate_Observables.F90:85-100                         */
+    double  EDensity, HDensity;
+    double  modes[2];
+    double  dosc[2];
+    int32_t status;          /* per-request status (NEGF_OK, INFO > 0, NEGF_E*)          */
+    int32_t sr_iters;        /* Sancho-Rubio iterations taken                           */
+} negf_result;
+
+/* RhoN, RhoP, SigX/Y/Z (may be NULL) are npx x npy x npz x n_hamiltonians arrays
+ * (slot slowest) that the requests' dE-weighted densities are ADDED to.                 */
+NEGF_API int negf_solve_batch(negf_handle* h, const negf_request* req, int32_t n, negf_result* res,
+                     double* RhoN, double* RhoP, double* SigX, double* SigY, double* SigZ);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NEGF_GB300_H */

@@ -1,0 +1,134 @@
+"""ctypes binding of include/negf.h (libnegf_gb300.so).
+
+This is the same binding a Python caller of the reference-side C ABI would write; the
+Fortran ISO_C_BINDING interface in fortran/negf_gpu_shim.F90 binds the same symbols.
+Loading never falls back to a CPU path: a missing or unbuildable library raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from ctypes import POINTER, c_char_p, c_double, c_int, c_int32, c_int64, c_void_p
+
+from . import _build
+
+NEGF_OK = 0
+NEGF_EINVAL = -1
+NEGF_ENOMEM = -2
+NEGF_ECUDA = -3
+NEGF_ESR_NOCONV = -4
+NEGF_ENAN = -5
+NEGF_ESTATE = -6
+NEGF_EADMIT = -7
+NEGF_ETIMEDOUT = -8
+NEGF_EREFINE = -9
+NEGF_ENODEV = -10
+NEGF_ENOHAM = -11
+
+NEGF_PREC_FP64 = 0
+NEGF_PREC_MIXED = 1
+
+# every symbol include/negf.h declares
+EXPORTED_SYMBOLS = (
+    "negf_create", "negf_destroy", "negf_strerror", "negf_device_bytes",
+    "negf_set_stream", "negf_profile", "negf_get_stats",
+    "negf_set_hamiltonian", "negf_contact_self_energy", "negf_get_retarded_greens",
+    "negf_copy_g_columns", "negf_calculate_gnp", "negf_calculate_observables",
+    "negf_solve_batch",
+)
+
+
+class NegfParams(ctypes.Structure):
+    _fields_ = [
+        ("npx", c_int32), ("npy", c_int32), ("npz", c_int32), ("norb", c_int32),
+        ("n_hamiltonians", c_int32), ("max_batch", c_int32),
+        ("eta", c_double), ("sr_tol", c_double),
+        ("sr_max_iter", c_int32), ("calc_spin", c_int32), ("precision", c_int32),
+        ("device", c_int32), ("mixed_slices", c_int32), ("keep_g_columns", c_int32),
+        ("reserved", c_int32 * 6),
+        ("spin_ops", c_double * (3 * 4 * 4 * 2)),
+    ]
+
+
+class NegfRequest(ctypes.Structure):
+    _fields_ = [("energy", c_double), ("f1", c_double), ("f2", c_double), ("dE", c_double),
+                ("slot", c_int32), ("flags", c_int32)]
+
+
+class NegfResult(ctypes.Structure):
+    _fields_ = [("T12", c_double), ("EDensity", c_double), ("HDensity", c_double),
+                ("modes", c_double * 2), ("dosc", c_double * 2),
+                ("status", c_int32), ("sr_iters", c_int32)]
+
+
+class NegfStats(ctypes.Structure):
+    _fields_ = [("launches", c_int64), ("gemm_launches", c_int64), ("gemm_ms", c_double),
+                ("gemm_flops", c_double), ("panel_launches", c_int64), ("panel_ms", c_double)]
+
+
+class NegfError(RuntimeError):
+    def __init__(self, code: int, where: str):
+        self.code = code
+        super().__init__("%s failed: %s (%d)" % (where, strerror(code), code))
+
+
+_lib = None
+_dp = POINTER(c_double)
+
+
+def _declare(lib):
+    h = c_void_p
+    sig = {
+        "negf_create": (c_int, [POINTER(NegfParams), POINTER(c_void_p)]),
+        "negf_destroy": (c_int, [h]),
+        "negf_strerror": (c_char_p, [c_int]),
+        "negf_device_bytes": (c_int, [h, POINTER(c_int64)]),
+        "negf_set_stream": (c_int, [h, c_void_p]),
+        "negf_profile": (c_int, [h, c_int]),
+        "negf_get_stats": (c_int, [h, POINTER(NegfStats)]),
+        "negf_set_hamiltonian": (c_int, [h, c_int32, _dp, _dp]),
+        "negf_contact_self_energy": (c_int, [h, c_double, _dp, _dp, _dp, _dp, _dp]),
+        "negf_get_retarded_greens": (c_int, [h]),
+        "negf_copy_g_columns": (c_int, [h, _dp, _dp]),
+        "negf_calculate_gnp": (c_int, [h, c_double, c_double, c_double, _dp, _dp]),
+        "negf_calculate_observables": (c_int, [h, c_double, c_double, c_double, _dp, _dp, _dp, _dp,
+                                               _dp, _dp, _dp, _dp]),
+        "negf_solve_batch": (c_int, [h, POINTER(NegfRequest), c_int32, POINTER(NegfResult),
+                                     _dp, _dp, _dp, _dp, _dp]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+
+
+def library_path() -> str:
+    return _build.LIB_PATH
+
+
+def load(build_if_missing: bool = True):
+    """Load libnegf_gb300.so (building it with nvcc when absent or stale)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB_PATH
+    if build_if_missing and (not os.path.exists(path) or _build.needs_build()):
+        _build.build()
+    if not os.path.exists(path):
+        raise RuntimeError("libnegf_gb300.so is missing and could not be built")
+    lib = ctypes.CDLL(path)
+    _declare(lib)
+    _lib = lib
+    return lib
+
+
+def strerror(code: int) -> str:
+    if _lib is None:
+        return "error %d" % code
+    return _lib.negf_strerror(code).decode()
+
+
+def check(code: int, where: str) -> int:
+    if code < 0:
+        raise NegfError(code, where)
+    return code

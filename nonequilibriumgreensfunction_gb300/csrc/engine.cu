@@ -1,0 +1,597 @@
+// Host orchestration of the per-energy NEGF solve (FP64 form).
+//
+// Mapping to the reference (all paths relative to the reference project):
+//   solve_sr   - Contact_Self_Energy / Sancho_Rubio, Source/Contact_Self_Energy.F90:114-147,156-269
+//   solve_rgf  - Energy_Sweep InvGRd assembly (Source/Energy_Sweep.F90:31-38) and
+//                Get_Retarded_Greens (Source/Recursive_Greens.F90:2-107), fused with the
+//                G Gamma G^H products of Calculate_Gnp (Source/Calculate_Gnp.F90:10-114)
+//                and the trace of Calculate_Observables (Source/Calculate_Observables.F90:46-100)
+//   densities  - Calculate_Gnp.F90:117-124 and Calculate_Observables.F90:10-43
+//   batch_solve- the energy loop of Source/NEGF_Main.F90:21-27 and the MPI sums of
+//                Source/MPI_Routines.F90:33-90, as one device pass per chunk of requests
+//
+// Algorithmic differences from the reference, all exact in exact arithmetic:
+//  * Only the two block columns G(:,1), G(:,N) are formed; the backward GRd/GRu/GRl
+//    recursion (Recursive_Greens.F90:37-51) is not needed because G(1,1) = gR_1 and
+//    G(x+1,1) = gR_{x+1} H^H G(x,1) (the reference obtains G(2,1) from GRl(1) and then
+//    overwrites it with the same recursion, :88-96).
+//  * The right-connected sweep runs first and its blocks are overwritten in place by
+//    the left-connected ones, so one Npx*M^2 block store per energy suffices.
+//  * Gn/Gp are formed as P_c = G(:,c) Gamma_c G(:,c)^H restricted to the site blocks the
+//    reductions read (diagonal norb x norb site blocks), Gn = f1 P_1 + f2 P_2 and
+//    Gp = (1-f1) P_1 + (1-f2) P_2 (Calculate_Gnp.F90:10-114 with the scalars pulled out).
+//  * When H_1 == H_N the two leads share one decimation: the right-lead recursion is the
+//    left one with t and t~ exchanged (Contact_Self_Energy.F90:121,133), so the products
+//    that involve only t, t~ are shared and each lead keeps its own T and stop test.
+//  * HopX that is block diagonal in norb x norb site blocks (every channel built by
+//    Source/Build_Hamiltonian.F90:59-64) is applied as a site-local operator.
+#include "engine.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstddef>
+#include <cstring>
+#include <map>
+#include <utility>
+
+namespace negf {
+
+namespace {
+
+constexpr int kSrBlocks = 13;
+enum SrRole { SR_ALPHA = 0, SR_T, SR_TT, SR_TOLDL, SR_TOLDR, SR_TL, SR_TR, SR_TMP, SR_W1, SR_TN, SR_TTN, SR_CHG, SR_W2 };
+
+__global__ void merge_info_k(int batch, const int* info, int* status) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b < batch && status[b] == 0 && info[b] != 0) status[b] = info[b];
+}
+
+template <typename T>
+int dalloc(T** p, size_t count, long long& bytes) {
+  if (count == 0) { *p = nullptr; return NEGF_OK; }
+  if (cudaMalloc((void**)p, sizeof(T) * count) != cudaSuccess) { *p = nullptr; return NEGF_ENOMEM; }
+  bytes += (long long)(sizeof(T) * count);
+  return NEGF_OK;
+}
+template <typename T>
+void dfree(T*& p) {
+  if (p) cudaFree((void*)p);
+  p = nullptr;
+}
+
+bool blocks_equal(const double2* a, const double2* b, size_t n) { return std::memcmp(a, b, n * sizeof(double2)) == 0; }
+
+}  // namespace
+
+int merge_info_kernel_launch(int batch, const int* info, int* status, cudaStream_t st) {
+  merge_info_k<<<(batch + 127) / 128, 128, 0, st>>>(batch, info, status);
+  NEGF_CUDA_TRY(cudaGetLastError());
+  count_launch();
+  return NEGF_OK;
+}
+
+Engine::~Engine() {
+  if (p_.npx > 0) cudaSetDevice(p_.device);
+  dfree(dH_); dfree(dHop_); dfree(dHopBD_); dfree(dSpin_);
+  dfree(dG_); dfree(dC1_); dfree(dCN_); dfree(dZ_); dfree(dY_); dfree(dQ_);
+  dfree(dSigL_); dfree(dSigR_); dfree(dGamL_); dfree(dGamR_);
+  dfree(dP1_); dfree(dP2_); dfree(dCol1_); dfree(dColN_);
+  dfree(dSite_); dfree(dSums_); dfree(dTr_); dfree(dAcc_); dfree(dStatus_); dfree(dItems_);
+  dfree(dSr_); dfree(dSrSigL_); dfree(dSrSigR_); dfree(dSrGamL_); dfree(dSrGamR_);
+  dfree(dSrCmax_); dfree(dSrDos_); dfree(dSrActive_); dfree(dSrE_); dfree(dSrHend_); dfree(dSrStatus_);
+  inv_work_free(inv_);
+  if (hPin_) cudaFreeHost(hPin_);
+  if (own_st_) cudaStreamDestroy(own_st_);
+}
+
+int Engine::init(const negf_params& p) {
+  if (p.npx < 2 || p.npy < 1 || p.npz < 1 || p.norb < 1 || p.norb > 4) return NEGF_EINVAL;
+  if (p.n_hamiltonians < 1 || p.max_batch < 1 || p.max_batch > 4096) return NEGF_EINVAL;
+  if (!(p.eta >= 0.0) || !(p.sr_tol > 0.0) || p.sr_max_iter < 1) return NEGF_EINVAL;
+  if (p.precision != NEGF_PREC_FP64) return NEGF_EINVAL;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return NEGF_ENODEV;
+  if (p.device < 0 || p.device >= ndev) return NEGF_EINVAL;
+  p_ = p;
+  M_ = p.norb * p.npy * p.npz;
+  MM_ = (long long)M_ * M_;
+  nsite_ = p.npy * p.npz;
+  B_ = p.max_batch;
+  S_ = 2 * p.max_batch;
+  keep_columns_ = p.keep_g_columns != 0;
+  NEGF_CUDA_TRY(cudaSetDevice(p.device));
+  NEGF_CUDA_TRY(cudaStreamCreateWithFlags(&own_st_, cudaStreamNonBlocking));
+  st_ = own_st_;
+  slot_set_.assign(p.n_hamiltonians, 0);
+  slot_rep_.assign(p.n_hamiltonians, 0);
+  slot_joint_.assign(p.n_hamiltonians, 0);
+  end_h1_.assign(p.n_hamiltonians, {});
+  end_hn_.assign(p.n_hamiltonians, {});
+  return alloc();
+}
+
+int Engine::alloc() {
+  const long long N = p_.npx;
+  const long long total = nsite_total();
+  NEGF_TRY(dalloc(&dH_, (size_t)(p_.n_hamiltonians * N * MM_), bytes_));
+  NEGF_TRY(dalloc(&dHop_, (size_t)MM_, bytes_));
+  NEGF_TRY(dalloc(&dHopBD_, (size_t)nsite_ * p_.norb * p_.norb, bytes_));
+  NEGF_TRY(dalloc(&dSpin_, (size_t)3 * p_.norb * p_.norb, bytes_));
+  NEGF_TRY(dalloc(&dG_, (size_t)(B_ * N * MM_), bytes_));
+  double2** bufs[] = {&dC1_, &dCN_, &dZ_, &dY_, &dQ_, &dSigL_, &dSigR_, &dGamL_, &dGamR_};
+  for (double2** b : bufs) NEGF_TRY(dalloc(b, (size_t)(B_ * MM_), bytes_));
+  NEGF_TRY(dalloc(&dP1_, (size_t)(B_ * N * M_ * p_.norb), bytes_));
+  NEGF_TRY(dalloc(&dP2_, (size_t)(B_ * N * M_ * p_.norb), bytes_));
+  if (keep_columns_) {
+    NEGF_TRY(dalloc(&dCol1_, (size_t)(N * MM_), bytes_));
+    NEGF_TRY(dalloc(&dColN_, (size_t)(N * MM_), bytes_));
+  }
+  sums_blocks_ = (int)((total + 255) / 256);
+  NEGF_TRY(dalloc(&dSite_, (size_t)(B_ * 5 * total), bytes_));
+  NEGF_TRY(dalloc(&dSums_, (size_t)B_ * sums_blocks_ * 2, bytes_));
+  NEGF_TRY(dalloc(&dTr_, (size_t)B_ * 4, bytes_));
+  NEGF_TRY(dalloc(&dAcc_, (size_t)(p_.n_hamiltonians * 5 * total), bytes_));
+  NEGF_TRY(dalloc(&dStatus_, (size_t)B_, bytes_));
+  NEGF_TRY(dalloc(&dItems_, (size_t)B_, bytes_));
+  NEGF_TRY(dalloc(&dSr_, (size_t)(kSrBlocks * S_ * MM_), bytes_));
+  double2** srb[] = {&dSrSigL_, &dSrSigR_, &dSrGamL_, &dSrGamR_};
+  for (double2** b : srb) NEGF_TRY(dalloc(b, (size_t)(S_ * MM_), bytes_));
+  NEGF_TRY(dalloc(&dSrCmax_, (size_t)2 * S_, bytes_));
+  NEGF_TRY(dalloc(&dSrDos_, (size_t)2 * S_, bytes_));
+  NEGF_TRY(dalloc(&dSrActive_, (size_t)2 * S_, bytes_));
+  NEGF_TRY(dalloc(&dSrE_, (size_t)S_, bytes_));
+  NEGF_TRY(dalloc(&dSrHend_, (size_t)S_, bytes_));
+  NEGF_TRY(dalloc(&dSrStatus_, (size_t)S_, bytes_));
+  NEGF_TRY(inv_work_alloc(inv_, M_, std::max(B_, S_)));
+  hPinBytes_ = sizeof(double) * (size_t)std::max<long long>(
+                   {(long long)B_ * sums_blocks_ * 2, (long long)B_ * 4, 4LL * S_,
+                    (long long)p_.n_hamiltonians * 5 * total, 5LL * total, 64});
+  NEGF_CUDA_TRY(cudaMallocHost((void**)&hPin_, hPinBytes_));
+  // spin operators (default: tau0 (x) sigma_j of Source/Read_In_Allocate.F90:183-196)
+  std::vector<double2> spin(3 * p_.norb * p_.norb, make_double2(0.0, 0.0));
+  bool any = false;
+  for (int j = 0; j < 3; ++j)
+    for (int r = 0; r < 4; ++r)
+      for (int c = 0; c < 4; ++c)
+        if (p_.spin_ops[j][r][c][0] != 0.0 || p_.spin_ops[j][r][c][1] != 0.0) any = true;
+  const int no = p_.norb;
+  if (any) {
+    for (int j = 0; j < 3; ++j)
+      for (int r = 0; r < no; ++r)
+        for (int c = 0; c < no; ++c)
+          spin[(j * no + r) * no + c] = make_double2(p_.spin_ops[j][r][c][0], p_.spin_ops[j][r][c][1]);
+  } else if (no == 4) {
+    // sigma_x, sigma_y, sigma_z on the spin index (orbital = 2*tau + sigma)
+    const double2 one = make_double2(1, 0), mi = make_double2(0, -1), pi_ = make_double2(0, 1), m1 = make_double2(-1, 0);
+    for (int blk = 0; blk < 2; ++blk) {
+      const int o = 2 * blk;
+      spin[(0 * 4 + o) * 4 + o + 1] = one; spin[(0 * 4 + o + 1) * 4 + o] = one;
+      spin[(1 * 4 + o) * 4 + o + 1] = mi;  spin[(1 * 4 + o + 1) * 4 + o] = pi_;
+      spin[(2 * 4 + o) * 4 + o] = one;     spin[(2 * 4 + o + 1) * 4 + o + 1] = m1;
+    }
+  }
+  NEGF_CUDA_TRY(cudaMemcpy(dSpin_, spin.data(), sizeof(double2) * spin.size(), cudaMemcpyHostToDevice));
+  return NEGF_OK;
+}
+
+int Engine::set_hamiltonian(int slot, const double* Htotd, const double* HopX) {
+  if (slot < 0 || slot >= p_.n_hamiltonians || !Htotd) return NEGF_EINVAL;
+  if (!hop_set_ && !HopX) return NEGF_EINVAL;
+  NEGF_CUDA_TRY(cudaSetDevice(p_.device));
+  const double2* h = reinterpret_cast<const double2*>(Htotd);
+  const long long N = p_.npx;
+  if (HopX) {
+    const double2* hx = reinterpret_cast<const double2*>(HopX);
+    if (hop_set_) {
+      std::vector<double2> cur(MM_);
+      NEGF_CUDA_TRY(cudaMemcpy(cur.data(), dHop_, sizeof(double2) * MM_, cudaMemcpyDeviceToHost));
+      // a different HopX invalidates every slot uploaded with the old one
+      if (!blocks_equal(cur.data(), hx, MM_)) std::fill(slot_set_.begin(), slot_set_.end(), 0);
+    }
+    NEGF_CUDA_TRY(cudaMemcpy(dHop_, hx, sizeof(double2) * MM_, cudaMemcpyHostToDevice));
+    // block-diagonal detection (site blocks of norb x norb)
+    const int no = p_.norb;
+    bool bd = true;
+    for (int j = 0; j < M_ && bd; ++j)
+      for (int i = 0; i < M_; ++i) {
+        if (i / no == j / no) continue;
+        const double2 v = hx[(long long)j * M_ + i];
+        if (v.x != 0.0 || v.y != 0.0) { bd = false; break; }
+      }
+    hop_bd_ = bd;
+    if (bd) {
+      std::vector<double2> hb((size_t)nsite_ * no * no);
+      for (int s = 0; s < nsite_; ++s)
+        for (int a = 0; a < no; ++a)
+          for (int c = 0; c < no; ++c) hb[((size_t)s * no + a) * no + c] = hx[(long long)(s * no + c) * M_ + s * no + a];
+      NEGF_CUDA_TRY(cudaMemcpy(dHopBD_, hb.data(), sizeof(double2) * hb.size(), cudaMemcpyHostToDevice));
+    }
+    hop_set_ = true;
+  }
+  NEGF_CUDA_TRY(cudaMemcpy(dH_ + (long long)slot * N * MM_, h, sizeof(double2) * N * MM_, cudaMemcpyHostToDevice));
+  end_h1_[slot].assign(h, h + MM_);
+  end_hn_[slot].assign(h + (N - 1) * MM_, h + N * MM_);
+  slot_set_[slot] = 1;
+  recompute_lead_classes();
+  sr_valid_ = rgf_valid_ = dens_valid_ = false;
+  return NEGF_OK;
+}
+
+void Engine::recompute_lead_classes() {
+  const int ns = p_.n_hamiltonians;
+  for (int s = 0; s < ns; ++s) {
+    slot_rep_[s] = s;
+    slot_joint_[s] = 0;
+    if (!slot_set_[s]) continue;
+    slot_joint_[s] = blocks_equal(end_h1_[s].data(), end_hn_[s].data(), MM_) ? 1 : 0;
+    for (int r = 0; r < s; ++r) {
+      if (!slot_set_[r] || slot_rep_[r] != r) continue;
+      if (blocks_equal(end_h1_[r].data(), end_h1_[s].data(), MM_) &&
+          blocks_equal(end_hn_[r].data(), end_hn_[s].data(), MM_)) {
+        slot_rep_[s] = r;
+        break;
+      }
+    }
+  }
+}
+
+int Engine::gemm(int batch, Op opA, const double2* A, long long sA, Op opB, const double2* B, long long sB, double2* C,
+                 long long sC, double2 alpha, double2 beta) {
+  GemmBatch g{};
+  g.m = M_; g.n = M_; g.k = M_;
+  g.alpha = alpha; g.beta = beta;
+  g.A = A; g.lda = M_; g.sA = sA; g.opA = opA;
+  g.B = B; g.ldb = M_; g.sB = sB; g.opB = opB;
+  g.C = C; g.ldc = M_; g.sC = sC;
+  g.batch = batch;
+  return zgemm_f64(g, st_);
+}
+
+int Engine::hop_mul(int left, Op op, const double2* X, long long sX, double2* Y, long long sY, int batch) {
+  if (hop_bd_) return hop_apply(hop(), M_, batch, left, op, X, sX, Y, sY, st_);
+  const double2 one = make_double2(1, 0), zero = make_double2(0, 0);
+  if (left) return gemm(batch, op, dHop_, 0, OP_N, X, sX, Y, sY, one, zero);
+  return gemm(batch, OP_N, X, sX, op, dHop_, 0, Y, sY, one, zero);
+}
+
+int Engine::merge_info(int batch) { return merge_info_kernel_launch(batch, inv_.info, dStatus_, st_); }
+
+// -------------------------------------------------------------------------------------
+// Sancho-Rubio (Source/Contact_Self_Energy.F90:156-269), batched over problems
+// -------------------------------------------------------------------------------------
+int Engine::solve_sr(const std::vector<SrJob>& jobs, std::vector<int>& status, std::vector<int>& iters) {
+  const int S = (int)jobs.size();
+  if (S == 0) return NEGF_OK;
+  if (S > S_) return NEGF_EINVAL;
+  const long long N = p_.npx;
+  const double2 one = make_double2(1, 0), zero = make_double2(0, 0), mone = make_double2(-1, 0);
+  std::vector<double> e(S);
+  std::vector<const double2*> hend(S);
+  for (int s = 0; s < S; ++s) {
+    e[s] = jobs[s].energy;
+    const int slot = jobs[s].slot;
+    if (slot < 0 || !slot_set_[slot]) return NEGF_ENOHAM;
+    hend[s] = dH_ + ((long long)slot * N + (jobs[s].use_last ? N - 1 : 0)) * MM_;
+  }
+  NEGF_CUDA_TRY(cudaMemcpyAsync(dSrE_, e.data(), sizeof(double) * S, cudaMemcpyHostToDevice, st_));
+  NEGF_CUDA_TRY(cudaMemcpyAsync(dSrHend_, hend.data(), sizeof(void*) * S, cudaMemcpyHostToDevice, st_));
+  NEGF_CUDA_TRY(cudaMemsetAsync(dSrStatus_, 0, sizeof(int) * S, st_));
+  int role[kSrBlocks];
+  for (int r = 0; r < kSrBlocks; ++r) role[r] = r;
+  auto buf = [&](int r) { return dSr_ + (long long)role[r] * S_ * MM_; };
+  const long long sM = MM_;
+  auto inv_merge = [&](double2* A) -> int {
+    NEGF_TRY(zinv_f64(A, sM, M_, S, inv_, st_));
+    return merge_info_kernel_launch(S, inv_.info, dSrStatus_, st_);
+  };
+
+  // alpha = (E + i eta) I - H_end (:117-120 / :129-132)
+  NEGF_TRY(form_alpha(M_, S, dSrE_, dSrHend_, p_.eta, 0.0, buf(SR_ALPHA), sM, st_));
+  // g0 = inv(alpha + i eta I) (:187)
+  NEGF_TRY(form_alpha(M_, S, dSrE_, dSrHend_, p_.eta, p_.eta, buf(SR_TMP), sM, st_));
+  NEGF_TRY(inv_merge(buf(SR_TMP)));
+  // left lead beta = -H^H:  t = -g0 beta^H = g0 H,  t~ = -g0 beta = g0 H^H (:193-195)
+  NEGF_TRY(hop_mul(0, OP_N, buf(SR_TMP), sM, buf(SR_T), sM, S));
+  NEGF_TRY(hop_mul(0, OP_C, buf(SR_TMP), sM, buf(SR_TT), sM, S));
+  // T_L = t; the right lead (beta = -H) starts from t_R = t~, so T_R = t~ (:197)
+  NEGF_TRY(copy_blocks(M_, S, buf(SR_T), sM, buf(SR_TL), sM, st_));
+  NEGF_TRY(copy_blocks(M_, S, buf(SR_TT), sM, buf(SR_TR), sM, st_));
+  NEGF_TRY(set_identity(M_, S, buf(SR_TOLDL), sM, st_));
+  NEGF_TRY(set_identity(M_, S, buf(SR_TOLDR), sM, st_));
+
+  std::vector<int> act(2 * S);
+  for (int s = 0; s < S; ++s) { act[s] = jobs[s].want_l; act[S + s] = jobs[s].want_r; }
+  iters.assign(2 * S, 0);
+  status.assign(S, 0);
+  NEGF_CUDA_TRY(cudaMemcpyAsync(dSrActive_, act.data(), sizeof(int) * 2 * S, cudaMemcpyHostToDevice, st_));
+  int it = 0;
+  auto any_active = [&]() { return std::any_of(act.begin(), act.end(), [](int a) { return a != 0; }); };
+  while (any_active() && it < p_.sr_max_iter) {
+    ++it;
+    // Told_L <- Told_L t~ ; Told_R <- Told_R t  (:203-204, with t <-> t~ for the right lead)
+    NEGF_TRY(gemm(S, OP_N, buf(SR_TOLDL), sM, OP_N, buf(SR_TT), sM, buf(SR_W1), sM, one, zero));
+    std::swap(role[SR_TOLDL], role[SR_W1]);
+    NEGF_TRY(gemm(S, OP_N, buf(SR_TOLDR), sM, OP_N, buf(SR_T), sM, buf(SR_W1), sM, one, zero));
+    std::swap(role[SR_TOLDR], role[SR_W1]);
+    // tmp = inv(I - t t~ - t~ t) (:206-209)
+    NEGF_TRY(set_identity(M_, S, buf(SR_TMP), sM, st_));
+    NEGF_TRY(gemm(S, OP_N, buf(SR_T), sM, OP_N, buf(SR_TT), sM, buf(SR_TMP), sM, mone, one));
+    NEGF_TRY(gemm(S, OP_N, buf(SR_TT), sM, OP_N, buf(SR_T), sM, buf(SR_TMP), sM, mone, one));
+    NEGF_TRY(inv_merge(buf(SR_TMP)));
+    // t <- tmp t t ; t~ <- tmp t~ t~ (:216-222)
+    NEGF_TRY(gemm(S, OP_N, buf(SR_TMP), sM, OP_N, buf(SR_T), sM, buf(SR_W1), sM, one, zero));
+    NEGF_TRY(gemm(S, OP_N, buf(SR_W1), sM, OP_N, buf(SR_T), sM, buf(SR_TN), sM, one, zero));
+    NEGF_TRY(gemm(S, OP_N, buf(SR_TMP), sM, OP_N, buf(SR_TT), sM, buf(SR_W1), sM, one, zero));
+    NEGF_TRY(gemm(S, OP_N, buf(SR_W1), sM, OP_N, buf(SR_TT), sM, buf(SR_TTN), sM, one, zero));
+    // change = Told t ; T += change (:224-226)
+    NEGF_TRY(gemm(S, OP_N, buf(SR_TOLDL), sM, OP_N, buf(SR_TN), sM, buf(SR_CHG), sM, one, zero));
+    NEGF_TRY(sr_accumulate(M_, S, dSrActive_, buf(SR_CHG), sM, buf(SR_TL), sM, dSrCmax_, st_));
+    NEGF_TRY(gemm(S, OP_N, buf(SR_TOLDR), sM, OP_N, buf(SR_TTN), sM, buf(SR_CHG), sM, one, zero));
+    NEGF_TRY(sr_accumulate(M_, S, dSrActive_ + S, buf(SR_CHG), sM, buf(SR_TR), sM, dSrCmax_ + S, st_));
+    std::swap(role[SR_T], role[SR_TN]);
+    std::swap(role[SR_TT], role[SR_TTN]);
+    NEGF_CUDA_TRY(cudaMemcpyAsync(hPin_, dSrCmax_, sizeof(double) * 2 * S, cudaMemcpyDeviceToHost, st_));
+    NEGF_CUDA_TRY(cudaStreamSynchronize(st_));
+    bool changed = false;
+    for (int q = 0; q < 2 * S; ++q) {
+      if (!act[q]) continue;
+      const double c = hPin_[q];
+      if (std::isnan(c)) {               // :228-237
+        status[q % S] = NEGF_ENAN;
+        act[q] = 0; iters[q] = it; changed = true;
+      } else if (!(c > p_.sr_tol)) {     // loop test of :200
+        act[q] = 0; iters[q] = it; changed = true;
+      }
+    }
+    if (changed)
+      NEGF_CUDA_TRY(cudaMemcpyAsync(dSrActive_, act.data(), sizeof(int) * 2 * S, cudaMemcpyHostToDevice, st_));
+  }
+  for (int q = 0; q < 2 * S; ++q)
+    if (act[q]) { iters[q] = it; if (status[q % S] == 0) status[q % S] = NEGF_ESR_NOCONV; }
+
+  // g = inv(alpha + beta T), Sigma = beta g beta^H (:241-255) for each lead
+  for (int lead = 0; lead < 2; ++lead) {
+    double2* T = buf(lead == 0 ? SR_TL : SR_TR);
+    double2* W = buf(SR_TMP);
+    if (hop_bd_) {
+      NEGF_TRY(sr_form_final(hop(), M_, S, lead, buf(SR_ALPHA), sM, T, sM, W, sM, st_));
+    } else {
+      NEGF_TRY(copy_blocks(M_, S, buf(SR_ALPHA), sM, W, sM, st_));
+      NEGF_TRY(gemm(S, lead == 0 ? OP_C : OP_N, dHop_, 0, OP_N, T, sM, W, sM, mone, one));
+    }
+    NEGF_TRY(inv_merge(W));
+    double2* sig = lead == 0 ? dSrSigL_ : dSrSigR_;
+    double2* gam = lead == 0 ? dSrGamL_ : dSrGamR_;
+    if (hop_bd_) {
+      NEGF_TRY(sr_sigma(hop(), M_, S, lead, W, sM, sig, sM, gam, sM, dSrDos_ + lead * S, st_));
+    } else {
+      // lead 0: H^H g H ; lead 1: H g H^H
+      NEGF_TRY(gemm(S, lead == 0 ? OP_C : OP_N, dHop_, 0, OP_N, W, sM, buf(SR_W1), sM, one, zero));
+      NEGF_TRY(gemm(S, OP_N, buf(SR_W1), sM, lead == 0 ? OP_N : OP_C, dHop_, 0, sig, sM, one, zero));
+      NEGF_TRY(sr_sigma(HopBD{}, M_, S, -1, nullptr, 0, sig, sM, gam, sM, dSrDos_ + lead * S, st_));
+    }
+  }
+  std::vector<int> st(S);
+  NEGF_CUDA_TRY(cudaMemcpyAsync(st.data(), dSrStatus_, sizeof(int) * S, cudaMemcpyDeviceToHost, st_));
+  NEGF_CUDA_TRY(cudaStreamSynchronize(st_));
+  for (int s = 0; s < S; ++s)
+    if (status[s] == 0 && st[s] != 0) status[s] = st[s];
+  return NEGF_OK;
+}
+
+// -------------------------------------------------------------------------------------
+// RGF sweep with the Gn site blocks and the end-block traces, batched over items
+// -------------------------------------------------------------------------------------
+int Engine::solve_rgf(const std::vector<Item>& items, bool keep_columns) {
+  const int B = (int)items.size();
+  if (B == 0) return NEGF_OK;
+  if (B > B_) return NEGF_EINVAL;
+  for (const Item& it : items)
+    if (it.slot < 0 || it.slot >= p_.n_hamiltonians || !slot_set_[it.slot]) return NEGF_ENOHAM;
+  const int N = p_.npx;
+  const long long sM = MM_, sG = (long long)N * MM_;
+  const long long sP = (long long)N * M_ * p_.norb;
+  const double2 one = make_double2(1, 0), zero = make_double2(0, 0);
+  NEGF_CUDA_TRY(cudaMemcpyAsync(dItems_, items.data(), sizeof(Item) * B, cudaMemcpyHostToDevice, st_));
+  NEGF_CUDA_TRY(cudaMemsetAsync(dStatus_, 0, sizeof(int) * B, st_));
+  const int istride = (int)(sizeof(Item) / sizeof(int));
+  const int* idx_l = reinterpret_cast<const int*>(reinterpret_cast<const char*>(dItems_) + offsetof(Item, sr_l));
+  const int* idx_r = reinterpret_cast<const int*>(reinterpret_cast<const char*>(dItems_) + offsetof(Item, sr_r));
+  NEGF_TRY(gather_blocks(M_, B, dSrSigL_, idx_l, istride, dSigL_, sM, st_));
+  NEGF_TRY(gather_blocks(M_, B, dSrSigR_, idx_r, istride, dSigR_, sM, st_));
+  NEGF_TRY(gather_blocks(M_, B, dSrGamL_, idx_l, istride, dGamL_, sM, st_));
+  NEGF_TRY(gather_blocks(M_, B, dSrGamR_, idx_r, istride, dGamR_, sM, st_));
+
+  auto form = [&](int x, int side, const double2* gprev) -> int {
+    FormW fw{};
+    fw.n = M_; fw.batch = B; fw.npx = N; fw.x = x; fw.eta = p_.eta;
+    fw.items = dItems_; fw.Hall = dH_;
+    fw.sigL = dSigL_; fw.sigR = dSigR_; fw.sSig = sM;
+    fw.side = side; fw.sG = sG; fw.sZ = sM;
+    fw.W = dG_ + (long long)x * MM_; fw.sW = sG;
+    if (gprev) {
+      if (hop_bd_) {
+        fw.gprev = gprev;
+        fw.hop = hop();
+      } else {
+        // side 0: H^H g H ; side 1: H g H^H  (dense HopX)
+        NEGF_TRY(hop_mul(1, side == 0 ? OP_C : OP_N, gprev, sG, dZ_, sM, B));
+        NEGF_TRY(hop_mul(0, side == 0 ? OP_N : OP_C, dZ_, sM, dQ_, sM, B));
+        fw.zsub = dQ_;
+      }
+    }
+    NEGF_TRY(form_w(fw, st_));
+    NEGF_TRY(zinv_f64(dG_ + (long long)x * MM_, sG, M_, B, inv_, st_));
+    return merge_info(B);
+  };
+
+  // right-connected sweep gR_x = inv(A_x - H gR_{x+1} H^H), x = N..1 (Recursive_Greens.F90:67-86)
+  for (int x = N - 1; x >= 0; --x) NEGF_TRY(form(x, 1, x < N - 1 ? dG_ + (long long)(x + 1) * MM_ : nullptr));
+
+  // forward: column 1 from gR, then the left-connected gL_x into the same slot
+  for (int x = 0; x < N; ++x) {
+    double2* Gx = dG_ + (long long)x * MM_;
+    if (x == 0) {
+      NEGF_TRY(copy_blocks(M_, B, Gx, sG, dC1_, sM, st_));                     // G(1,1) = gR_1
+    } else {
+      NEGF_TRY(hop_mul(1, OP_C, dC1_, sM, dZ_, sM, B));                          // H^H G(x-1,1)
+      NEGF_TRY(gemm(B, OP_N, Gx, sG, OP_N, dZ_, sM, dC1_, sM, one, zero));       // gR_x H^H G(x-1,1)
+    }
+    if (keep_columns && dCol1_) NEGF_TRY(copy_blocks(M_, 1, dC1_, sM, dCol1_ + (long long)x * MM_, sM, st_));
+    NEGF_TRY(gemm(B, OP_N, dC1_, sM, OP_N, dGamL_, sM, dY_, sM, one, zero));      // G(x,1) Gamma_L
+    NEGF_TRY(site_blocks(M_, p_.norb, B, dY_, sM, dC1_, sM, dP1_ + (long long)x * M_ * p_.norb, sP, st_));
+    if (x == 0) {
+      NEGF_TRY(gemm(B, OP_N, dGamL_, sM, OP_N, dY_, sM, dQ_, sM, one, zero));
+      NEGF_TRY(trace_dot(M_, B, dQ_, sM, dC1_, sM, dTr_ + 0, 4, st_));
+    }
+    if (x == N - 1) {
+      NEGF_TRY(gemm(B, OP_N, dGamR_, sM, OP_N, dY_, sM, dQ_, sM, one, zero));
+      NEGF_TRY(trace_dot(M_, B, dQ_, sM, dC1_, sM, dTr_ + 2, 4, st_));
+    }
+    // gL_x = inv(A_x - H^H gL_{x-1} H) (Recursive_Greens.F90:16-34)
+    NEGF_TRY(form(x, 0, x > 0 ? dG_ + (long long)(x - 1) * MM_ : nullptr));
+  }
+
+  // backward: column N, G(x,N) = gL_x H G(x+1,N) (Recursive_Greens.F90:53-63)
+  for (int x = N - 1; x >= 0; --x) {
+    double2* Gx = dG_ + (long long)x * MM_;
+    if (x == N - 1) {
+      NEGF_TRY(copy_blocks(M_, B, Gx, sG, dCN_, sM, st_));
+    } else {
+      NEGF_TRY(hop_mul(1, OP_N, dCN_, sM, dZ_, sM, B));
+      NEGF_TRY(gemm(B, OP_N, Gx, sG, OP_N, dZ_, sM, dCN_, sM, one, zero));
+    }
+    if (keep_columns && dColN_) NEGF_TRY(copy_blocks(M_, 1, dCN_, sM, dColN_ + (long long)x * MM_, sM, st_));
+    NEGF_TRY(gemm(B, OP_N, dCN_, sM, OP_N, dGamR_, sM, dY_, sM, one, zero));      // G(x,N) Gamma_R
+    NEGF_TRY(site_blocks(M_, p_.norb, B, dY_, sM, dCN_, sM, dP2_ + (long long)x * M_ * p_.norb, sP, st_));
+    if (x == 0) {   // T12 = Re Tr[Gamma_L G(1,N) Gamma_R G(1,N)^H] (Calculate_Observables.F90:85-100)
+      NEGF_TRY(gemm(B, OP_N, dGamL_, sM, OP_N, dY_, sM, dQ_, sM, one, zero));
+      NEGF_TRY(trace_dot(M_, B, dQ_, sM, dCN_, sM, dTr_ + 1, 4, st_));
+    }
+    if (x == N - 1) {
+      NEGF_TRY(gemm(B, OP_N, dGamR_, sM, OP_N, dY_, sM, dQ_, sM, one, zero));
+      NEGF_TRY(trace_dot(M_, B, dQ_, sM, dCN_, sM, dTr_ + 3, 4, st_));
+    }
+  }
+  return NEGF_OK;
+}
+
+int Engine::densities(const std::vector<Item>& items, std::vector<double>& edens, std::vector<double>& hdens) {
+  const int B = (int)items.size();
+  NEGF_CUDA_TRY(cudaMemcpyAsync(dItems_, items.data(), sizeof(Item) * B, cudaMemcpyHostToDevice, st_));
+  DensityArgs a{};
+  a.n = M_; a.norb = p_.norb; a.npx = p_.npx; a.npy = p_.npy; a.npz = p_.npz; a.batch = B;
+  a.calc_spin = p_.calc_spin; a.items = dItems_;
+  a.P1 = dP1_; a.P2 = dP2_; a.sP = (long long)p_.npx * M_ * p_.norb;
+  a.spin_ops = dSpin_; a.site_out = dSite_; a.sums = dSums_;
+  NEGF_TRY(density_spin(a, st_));
+  const size_t np = (size_t)B * sums_blocks_ * 2;
+  NEGF_CUDA_TRY(cudaMemcpyAsync(hPin_, dSums_, sizeof(double) * np, cudaMemcpyDeviceToHost, st_));
+  NEGF_CUDA_TRY(cudaStreamSynchronize(st_));
+  edens.assign(B, 0.0);
+  hdens.assign(B, 0.0);
+  const double inv2pi = 1.0 / (2.0 * 3.14159265358979323846);
+  for (int b = 0; b < B; ++b) {
+    double sn = 0.0, sp = 0.0;
+    for (int k = 0; k < sums_blocks_; ++k) {
+      sn += hPin_[((size_t)b * sums_blocks_ + k) * 2 + 0];
+      sp += hPin_[((size_t)b * sums_blocks_ + k) * 2 + 1];
+    }
+    edens[b] = sn * inv2pi;
+    hdens[b] = sp * inv2pi;
+  }
+  return NEGF_OK;
+}
+
+// -------------------------------------------------------------------------------------
+// Batched solve
+// -------------------------------------------------------------------------------------
+int Engine::batch_solve(const negf_request* req, int n, negf_result* res, double* RhoN, double* RhoP, double* SigX,
+                        double* SigY, double* SigZ) {
+  if (n < 0 || (n > 0 && (!req || !res))) return NEGF_EINVAL;
+  NEGF_CUDA_TRY(cudaSetDevice(p_.device));
+  const long long total = nsite_total();
+  const int nslots = p_.n_hamiltonians;
+  for (int i = 0; i < n; ++i) {
+    const int s = req[i].slot;
+    if (s < 0 || s >= nslots) return NEGF_EINVAL;
+    if (!slot_set_[s]) return NEGF_ENOHAM;
+  }
+  NEGF_CUDA_TRY(cudaMemsetAsync(dAcc_, 0, sizeof(double) * nslots * 5 * total, st_));
+  int first_err = NEGF_OK;
+  for (int c0 = 0; c0 < n; c0 += B_) {
+    const int nb = std::min(B_, n - c0);
+    // Sancho-Rubio problems: one per (energy, lead class), two if H_1 != H_N
+    std::vector<SrJob> jobs;
+    std::map<std::pair<double, int>, std::pair<int, int>> key2job;
+    std::vector<Item> items(nb);
+    for (int i = 0; i < nb; ++i) {
+      const negf_request& r = req[c0 + i];
+      const int rep = slot_rep_[r.slot];
+      auto key = std::make_pair(r.energy, rep);
+      auto itk = key2job.find(key);
+      std::pair<int, int> jl;
+      if (itk == key2job.end()) {
+        if (slot_joint_[rep]) {
+          jobs.push_back(SrJob{r.energy, rep, 0, 1, 1});
+          jl = {(int)jobs.size() - 1, (int)jobs.size() - 1};
+        } else {
+          jobs.push_back(SrJob{r.energy, rep, 0, 1, 0});
+          jobs.push_back(SrJob{r.energy, rep, 1, 0, 1});
+          jl = {(int)jobs.size() - 2, (int)jobs.size() - 1};
+        }
+        key2job[key] = jl;
+      } else {
+        jl = itk->second;
+      }
+      Item& it = items[i];
+      it.energy = r.energy; it.f1 = r.f1; it.f2 = r.f2; it.dE = r.dE; it.slot = r.slot;
+      it.sr_l = jl.first; it.sr_r = jl.second; it.pad = 0;
+    }
+    std::vector<int> sr_status, sr_iters;
+    NEGF_TRY(solve_sr(jobs, sr_status, sr_iters));
+    const int S = (int)jobs.size();
+    std::vector<double> dos(2 * S);
+    NEGF_CUDA_TRY(cudaMemcpyAsync(dos.data(), dSrDos_, sizeof(double) * S, cudaMemcpyDeviceToHost, st_));
+    NEGF_CUDA_TRY(cudaMemcpyAsync(dos.data() + S, dSrDos_ + S, sizeof(double) * S, cudaMemcpyDeviceToHost, st_));
+    NEGF_TRY(solve_rgf(items, false));
+    std::vector<double> ed, hd;
+    NEGF_TRY(densities(items, ed, hd));
+    NEGF_TRY(reduce_sites(nb, (int)total, nslots, dItems_, dSite_, dAcc_, st_));
+    std::vector<double> tr(4 * (size_t)nb);
+    std::vector<int> rst(nb);
+    NEGF_CUDA_TRY(cudaMemcpyAsync(tr.data(), dTr_, sizeof(double) * 4 * nb, cudaMemcpyDeviceToHost, st_));
+    NEGF_CUDA_TRY(cudaMemcpyAsync(rst.data(), dStatus_, sizeof(int) * nb, cudaMemcpyDeviceToHost, st_));
+    NEGF_CUDA_TRY(cudaStreamSynchronize(st_));
+    for (int i = 0; i < nb; ++i) {
+      negf_result& o = res[c0 + i];
+      const Item& it = items[i];
+      o.T12 = tr[4 * i + 1];
+      o.modes[0] = tr[4 * i + 0] + tr[4 * i + 1];
+      o.modes[1] = tr[4 * i + 2] + tr[4 * i + 3];
+      o.EDensity = ed[i];
+      o.HDensity = hd[i];
+      o.dosc[0] = dos[it.sr_l];
+      o.dosc[1] = dos[S + it.sr_r];
+      int stv = sr_status[it.sr_l] ? sr_status[it.sr_l] : sr_status[it.sr_r];
+      if (stv == 0) stv = rst[i];
+      o.status = stv;
+      o.sr_iters = std::max(sr_iters[it.sr_l], sr_iters[S + it.sr_r]);
+      if (stv != 0 && first_err == 0) first_err = stv;
+    }
+  }
+  // add the slot-resolved site sums into the caller's arrays
+  const size_t acc_n = (size_t)nslots * 5 * total;
+  NEGF_CUDA_TRY(cudaMemcpyAsync(hPin_, dAcc_, sizeof(double) * acc_n, cudaMemcpyDeviceToHost, st_));
+  NEGF_CUDA_TRY(cudaStreamSynchronize(st_));
+  double* outs[5] = {RhoN, RhoP, SigX, SigY, SigZ};
+  for (int f = 0; f < 5; ++f) {
+    if (!outs[f]) continue;
+    if (f >= 2 && !p_.calc_spin) continue;
+    for (int s = 0; s < nslots; ++s)
+      for (long long i = 0; i < total; ++i) outs[f][(size_t)s * total + i] += hPin_[((size_t)s * 5 + f) * total + i];
+  }
+  return first_err;
+}
+
+}  // namespace negf

@@ -1,0 +1,121 @@
+// Host-side engine: owns the device state of one negf_handle and orchestrates the
+// per-energy solve as batched device kernels.
+#pragma once
+
+#include <array>
+#include <vector>
+
+#include "negf_internal.cuh"
+
+namespace negf {
+
+struct SrJob {          // one Sancho-Rubio problem
+  double energy;
+  int slot;             // device end slice comes from this slot
+  int use_last;         // alpha from H_N (1) or H_1 (0)
+  int want_l, want_r;   // which lead outputs are used
+};
+
+class Engine {
+ public:
+  ~Engine();
+  int init(const negf_params& p);
+  int set_hamiltonian(int slot, const double* Htotd, const double* HopX);
+
+  // Sancho-Rubio for a list of problems; outputs into sr_* buffers (index = problem)
+  int solve_sr(const std::vector<SrJob>& jobs, std::vector<int>& status, std::vector<int>& iters);
+  // RGF + Gn site blocks + traces for a batch of items (Sigma/Gamma gathered from SR)
+  int solve_rgf(const std::vector<Item>& items, bool keep_columns);
+  // densities/spin for the current batch (after solve_rgf) with the items' f1,f2,dE
+  int densities(const std::vector<Item>& items, std::vector<double>& edens, std::vector<double>& hdens);
+
+  int batch_solve(const negf_request* req, int n, negf_result* res, double* RhoN, double* RhoP, double* SigX,
+                  double* SigY, double* SigZ);
+
+  // accessors used by the per-energy API
+  int M() const { return M_; }
+  int npx() const { return p_.npx; }
+  int nsite_total() const { return p_.npx * p_.npy * p_.npz; }
+  long long bytes() const { return bytes_; }
+
+  negf_params p_{};
+  int M_ = 0, nsite_ = 0, B_ = 0, S_ = 0;
+  long long MM_ = 0;
+  cudaStream_t st_ = nullptr;       // stream the work runs on
+  cudaStream_t own_st_ = nullptr;   // the handle's own stream
+  long long bytes_ = 0;
+
+  // Hamiltonian
+  double2* dH_ = nullptr;
+  double2* dHop_ = nullptr;
+  double2* dHopBD_ = nullptr;
+  bool hop_bd_ = false;
+  bool hop_set_ = false;
+  std::vector<int> slot_set_;
+  // Slots whose end slices H_1 / H_N are bitwise identical share the Sancho-Rubio
+  // decimation at a given energy: slot_rep_[s] is the first such slot.  slot_joint_[s]
+  // is set when H_1 == H_N, so one decimation gives both leads.
+  std::vector<std::vector<double2>> end_h1_, end_hn_;
+  std::vector<int> slot_rep_, slot_joint_;
+  void recompute_lead_classes();
+  double2* dSpin_ = nullptr;
+
+  // batch workspace
+  double2 *dG_ = nullptr, *dC1_ = nullptr, *dCN_ = nullptr, *dZ_ = nullptr, *dY_ = nullptr, *dQ_ = nullptr;
+  double2 *dSigL_ = nullptr, *dSigR_ = nullptr, *dGamL_ = nullptr, *dGamR_ = nullptr;
+  double2 *dP1_ = nullptr, *dP2_ = nullptr;
+  double2 *dCol1_ = nullptr, *dColN_ = nullptr;  // optional full columns for item 0
+  double* dSite_ = nullptr;
+  double* dSums_ = nullptr;
+  double* dTr_ = nullptr;
+  double* dAcc_ = nullptr;  // slots * 5 * nsite_total
+  int* dStatus_ = nullptr;
+  Item* dItems_ = nullptr;
+  int sums_blocks_ = 0;
+
+  // Sancho-Rubio workspace (S_ problems)
+  double2* dSr_ = nullptr;  // kSrBlocks * S_ blocks
+  double2 *dSrSigL_ = nullptr, *dSrSigR_ = nullptr, *dSrGamL_ = nullptr, *dSrGamR_ = nullptr;
+  double* dSrCmax_ = nullptr;
+  double* dSrDos_ = nullptr;
+  int* dSrActive_ = nullptr;
+  double* dSrE_ = nullptr;
+  const double2** dSrHend_ = nullptr;
+  int* dSrStatus_ = nullptr;
+
+  // pinned host staging
+  double* hPin_ = nullptr;
+  size_t hPinBytes_ = 0;
+
+  InvWork inv_;
+  HopBD hop() const {
+    HopBD h;
+    h.hb = dHopBD_;
+    h.norb = p_.norb;
+    h.nsite = nsite_;
+    return h;
+  }
+
+  // per-energy API state
+  bool sr_valid_ = false, rgf_valid_ = false, dens_valid_ = false;
+  double cur_energy_ = 0.0;
+  std::array<double, 2> cur_dos_{};
+  int cur_sr_status_ = 0;
+  int cur_sr_iters_ = 0;
+  int cur_rgf_status_ = 0;
+  std::vector<double> last_site_;  // 5 * nsite_total for item 0
+  double last_edens_ = 0.0, last_hdens_ = 0.0;
+  bool keep_columns_ = false;
+
+ private:
+  int alloc();
+  // Y = op(H) X (left) or X op(H) (right) for every block of a strided batch
+  int hop_mul(int left, Op op, const double2* X, long long sX, double2* Y, long long sY, int batch);
+  int gemm(int batch, Op opA, const double2* A, long long sA, Op opB, const double2* B, long long sB, double2* C,
+           long long sC, double2 alpha, double2 beta);
+  int merge_info(int batch);
+};
+
+int merge_info_kernel_launch(int batch, const int* info, int* status, cudaStream_t st);
+
+}  // namespace negf

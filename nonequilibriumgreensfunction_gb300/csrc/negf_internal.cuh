@@ -1,0 +1,220 @@
+// Internal declarations shared by the translation units of libnegf_gb300.so.
+//
+// Device layout: every M x M complex block is column-major, interleaved double2
+// (the memory layout of the reference's COMPLEX(8) arrays, Source/NEGF_Module.F90:56-75),
+// so blocks cross the C ABI with a plain memcpy.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <vector>
+
+#include "../../include/negf.h"
+
+namespace negf {
+
+// ----------------------------------------------------------------------------------
+// complex helpers (double2 = (re, im))
+// ----------------------------------------------------------------------------------
+__host__ __device__ __forceinline__ double2 cmake(double r, double i) { return make_double2(r, i); }
+__host__ __device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__host__ __device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+__host__ __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__host__ __device__ __forceinline__ double2 cconj(double2 a) { return make_double2(a.x, -a.y); }
+__host__ __device__ __forceinline__ double2 cscale(double2 a, double s) { return make_double2(a.x * s, a.y * s); }
+// acc += a * b
+__host__ __device__ __forceinline__ void cfma(double2& acc, double2 a, double2 b) {
+  acc.x = fma(a.x, b.x, acc.x);
+  acc.x = fma(-a.y, b.y, acc.x);
+  acc.y = fma(a.x, b.y, acc.y);
+  acc.y = fma(a.y, b.x, acc.y);
+}
+// 1 / a, scaled to avoid overflow in |a|^2
+__host__ __device__ __forceinline__ double2 crcp(double2 a) {
+  double s = fmax(fabs(a.x), fabs(a.y));
+  if (s == 0.0) return make_double2(1.0 / 0.0, 0.0);
+  double ar = a.x / s, ai = a.y / s;
+  double d = s * (ar * ar + ai * ai);
+  return make_double2(ar / d, -ai / d);
+}
+// |re| + |im|, the pivot measure of LAPACK izamax/dcabs1
+__host__ __device__ __forceinline__ double cabs1(double2 a) { return fabs(a.x) + fabs(a.y); }
+
+// ----------------------------------------------------------------------------------
+// error handling
+// ----------------------------------------------------------------------------------
+#define NEGF_CUDA_TRY(expr)                                                                 \
+  do {                                                                                      \
+    cudaError_t _e = (expr);                                                                \
+    if (_e != cudaSuccess) {                                                                \
+      ::negf::record_cuda_error(_e, #expr, __FILE__, __LINE__);                             \
+      return NEGF_ECUDA;                                                                    \
+    }                                                                                       \
+  } while (0)
+
+#define NEGF_TRY(expr)                                                                      \
+  do {                                                                                      \
+    int _s = (expr);                                                                        \
+    if (_s < 0) return _s;                                                                  \
+  } while (0)
+
+void record_cuda_error(cudaError_t e, const char* what, const char* file, int line);
+const char* last_cuda_error_text();
+
+// ----------------------------------------------------------------------------------
+// instrumentation (process-wide; the library is driven by one host thread per handle and
+// the counters are only read by the instrumentation entry points)
+// ----------------------------------------------------------------------------------
+enum TimedKind { TK_GEMM = 0, TK_PANEL = 1, TK_COUNT = 2 };
+struct Instrument {
+  long long launches = 0;
+  long long kind_launches[TK_COUNT] = {0, 0};
+  double kind_flops[TK_COUNT] = {0, 0};
+  bool timing = false;
+  struct Rec { cudaEvent_t a, b; int kind; };
+  std::vector<Rec> pending;
+  double kind_ms[TK_COUNT] = {0, 0};
+  std::vector<cudaEvent_t> pool;
+};
+Instrument& instrument();
+inline void count_launch(int n = 1) { instrument().launches += n; }
+// start/stop a timed region on `st` around one launch of `kind`
+void timed_begin(cudaStream_t st, int kind, double flops, cudaEvent_t* a);
+void timed_end(cudaStream_t st, int kind, cudaEvent_t a);
+void instrument_resolve();   // accumulate the elapsed times of finished event pairs
+
+// ----------------------------------------------------------------------------------
+// GEMM: C = alpha * op(A) * op(B) + beta * C, strided batch (FP64 complex, SIMT DFMA)
+// ----------------------------------------------------------------------------------
+enum Op : int { OP_N = 0, OP_T = 1, OP_C = 2 };
+
+struct GemmBatch {
+  int m, n, k;
+  double2 alpha, beta;
+  const double2* A; int lda; long long sA; Op opA;
+  const double2* B; int ldb; long long sB; Op opB;
+  double2* C; int ldc; long long sC;
+  int batch;
+};
+int zgemm_f64(const GemmBatch& g, cudaStream_t st);
+
+// ----------------------------------------------------------------------------------
+// Batched in-place inverse (blocked Gauss-Jordan with partial row pivoting)
+// ----------------------------------------------------------------------------------
+struct InvWork {
+  double2* rbuf = nullptr;   // batch * nb * n
+  int* ipiv = nullptr;       // batch * n
+  int* info = nullptr;       // batch
+  int n_cap = 0, batch_cap = 0, nb = 0;
+};
+int inv_work_alloc(InvWork& w, int n, int batch);
+void inv_work_free(InvWork& w);
+int panel_width(int n);
+// A: batch matrices of n x n, column-major, consecutive at stride sA.  On return A holds
+// the inverses; w.info[b] (device) holds the LAPACK-style INFO of each matrix.
+int zinv_f64(double2* A, long long sA, int n, int batch, InvWork& w, cudaStream_t st);
+
+// ----------------------------------------------------------------------------------
+// per-item description of a batch (uploaded once per batch)
+// ----------------------------------------------------------------------------------
+struct Item {
+  double energy;
+  double f1, f2, dE;
+  int slot;      // Hamiltonian slot
+  int sr_l;      // Sancho-Rubio problem giving Sigma_L
+  int sr_r;      // Sancho-Rubio problem giving Sigma_R
+  int pad;
+};
+
+// ----------------------------------------------------------------------------------
+// element-wise / structured kernels (ops.cu)
+// ----------------------------------------------------------------------------------
+// Block-diagonal hopping matrix, compact form: nsite blocks of norb x norb (row-major
+// per block: hb[s*norb*norb + a*norb + b] = H(s*norb+a, s*norb+b)).
+struct HopBD {
+  const double2* hb = nullptr;
+  int norb = 4, nsite = 0;
+};
+
+// W[b] = (E_b + i eta) I - Hslice[b] - (x==0 ? SigL[b] : 0) - (x==N-1 ? SigR[b] : 0)
+//        - coupling term, where the coupling term is, if gprev != nullptr:
+//          side 0:  H^H gprev[b] H    (left-connected sweep, Recursive_Greens.F90:18-20)
+//          side 1:  H gprev[b] H^H    (right-connected sweep, Recursive_Greens.F90:70-72)
+//        using the block-diagonal H, or, if zsub != nullptr, zsub[b] (dense path).
+struct FormW {
+  int n, batch, npx, x;
+  double eta;
+  const Item* items;
+  const double2* Hall;       // slots * npx * n*n
+  const double2* sigL; long long sSig;   // per item, may be null
+  const double2* sigR;
+  const double2* gprev; long long sG;   // per item
+  int side;
+  HopBD hop;
+  const double2* zsub; long long sZ;
+  double2* W; long long sW;
+};
+int form_w(const FormW& a, cudaStream_t st);
+
+// Y[b] = op(H) X[b] (left == 1) or X[b] op(H) (left == 0), H block diagonal; op in {N, C}
+int hop_apply(const HopBD& h, int n, int batch, int left, Op op, const double2* X, long long sX,
+              double2* Y, long long sY, cudaStream_t st);
+
+// Site blocks of P = X Gamma X^H: P[b][r][a] = sum_k Y[b](r,k) conj(X[b](site(r)*norb + a, k)),
+// with Y = X Gamma (precomputed).  Output stride per item sP (n*norb elements per slice).
+int site_blocks(int n, int norb, int batch, const double2* Y, long long sY, const double2* X, long long sX,
+                double2* P, long long sP, cudaStream_t st);
+
+// out[b] = Re sum_ij Q[b](i,j) conj(X[b](i,j))   (trace of Q X^H), one value per item.
+int trace_dot(int n, int batch, const double2* Q, long long sQ, const double2* X, long long sX,
+              double* out, int out_stride, cudaStream_t st);
+
+// gather per-item copies: dst[b] = src[idx[b]] (M x M blocks)
+int gather_blocks(int n, int batch, const double2* src, const int* idx_dev, int idx_stride,
+                  double2* dst, long long sDst, cudaStream_t st);
+
+int copy_blocks(int n, int batch, const double2* src, long long sSrc, double2* dst, long long sDst, cudaStream_t st);
+int set_identity(int n, int batch, double2* A, long long sA, cudaStream_t st);
+
+// Sancho-Rubio helpers
+struct SrProblem {
+  double energy;
+  const double2* h_end;  // the end slice H_1 (left) or H_N (right) used for alpha
+  int want_l, want_r;
+};
+// A[s] = (E_s + i*(eta + extra_eta)) I - Hend[s]
+int form_alpha(int n, int nprob, const double* energies, const double2* const* hend, double eta,
+               double extra_eta, double2* A, long long sA, cudaStream_t st);
+// T += (active[s] ? change : 0); cmax[s] = max |change| (NaN -> NaN)
+int sr_accumulate(int n, int nprob, const int* active, const double2* change, long long sC, double2* T,
+                  long long sT, double* cmax, cudaStream_t st);
+// W = alpha - H^H T  (lead 0)   or  alpha - H T (lead 1) with block-diagonal H
+int sr_form_final(const HopBD& h, int n, int nprob, int lead, const double2* alpha, long long sA,
+                  const double2* T, long long sT, double2* W, long long sW, cudaStream_t st);
+// Sigma = H^H g H (lead 0) or H g H^H (lead 1); Gamma = i (Sigma - Sigma^H); dos = -Im Tr Sigma / pi
+int sr_sigma(const HopBD& h, int n, int nprob, int lead, const double2* g, long long sg, double2* sig,
+             long long sSig, double2* gam, long long sGam, double* dos, cudaStream_t st);
+
+// density / spin from the site blocks of both leads.  P1, P2: [item][x][n][norb].
+// site_out: [item][5][npx*npy*npz] = (RhoN, RhoP, SigX, SigY, SigZ) already weighted
+// by dE/(2 pi); sums: [item][2] = (EDensity, HDensity).
+struct DensityArgs {
+  int n, norb, npx, npy, npz, batch, calc_spin;
+  const Item* items;
+  const double2* P1; const double2* P2; long long sP;
+  const double2* spin_ops;  // 3 * norb*norb (row-major)
+  double* site_out;         // batch * 5 * nsite_total
+  double* sums;             // batch * 2
+};
+int density_spin(const DensityArgs& a, cudaStream_t st);
+
+// acc[slot][f][i] += sum over items b with items[b].slot == slot (in order) of site_out[b][f][i]
+int reduce_sites(int batch, int nsite_total, int nslots, const Item* items, const double* site_out,
+                 double* acc, cudaStream_t st);
+
+// convert to / from the Fortran layout on the host side is a plain copy (same layout)
+
+}  // namespace negf

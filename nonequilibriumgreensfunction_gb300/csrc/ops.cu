@@ -1,0 +1,491 @@
+// Structured and element-wise kernels of the FP64 solve: assembly of the matrices to
+// invert, block-diagonal hopping products, the site blocks of Gn/Gp, traces and the
+// density / spin reductions.  All are O(n^2) per block; the O(n^3) work is in
+// gemm_f64.cu and inverse_f64.cu.
+#include "negf_internal.cuh"
+
+namespace negf {
+
+namespace {
+
+constexpr int EW_THREADS = 256;
+
+inline dim3 ew_grid(long long elems, int batch) {
+  long long bx = (elems + EW_THREADS - 1) / EW_THREADS;
+  if (bx > 65535) bx = 65535;
+  return dim3((unsigned)bx, (unsigned)batch);
+}
+
+// hop block element: H(s*no + a, s*no + c)
+__device__ __forceinline__ double2 hbe(const HopBD& h, int s, int a, int c) {
+  return h.hb[((long long)s * h.norb + a) * h.norb + c];
+}
+
+// ---- W assembly (Energy_Sweep.F90:31-38 + Recursive_Greens.F90:18-20 / :70-72) ----------
+__global__ void form_w_kernel(FormW a) {
+  const int b = blockIdx.y;
+  const int n = a.n;
+  const long long nn = (long long)n * n;
+  const Item it = a.items[b];
+  const double2* Hx = a.Hall + ((long long)it.slot * a.npx + a.x) * nn;
+  const double2* gp = a.gprev ? a.gprev + (long long)b * a.sG : nullptr;
+  const double2* zs = a.zsub ? a.zsub + (long long)b * a.sZ : nullptr;
+  const double2* sl = (a.x == 0 && a.sigL) ? a.sigL + (long long)b * a.sSig : nullptr;
+  const double2* sr = (a.x == a.npx - 1 && a.sigR) ? a.sigR + (long long)b * a.sSig : nullptr;
+  double2* W = a.W + (long long)b * a.sW;
+  const int no = a.hop.norb;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nn; e += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(e % n), j = (int)(e / n);
+    double2 v = make_double2(-Hx[e].x, -Hx[e].y);
+    if (i == j) { v.x += it.energy; v.y += a.eta; }
+    if (sl) v = csub(v, sl[e]);
+    if (sr) v = csub(v, sr[e]);
+    if (zs) v = csub(v, zs[e]);
+    if (gp && a.hop.hb) {
+      // sum_{p in site(i), q in site(j)} L(i,p) g(p,q) R(q,j)
+      const int si = i / no, ai = i % no, sj = j / no, aj = j % no;
+      double2 acc = make_double2(0.0, 0.0);
+      for (int pa = 0; pa < no; ++pa) {
+        // side 0: L = H^H -> L(i,p) = conj(H(p,i));  side 1: L = H -> H(i,p)
+        const double2 l = a.side == 0 ? cconj(hbe(a.hop, si, pa, ai)) : hbe(a.hop, si, ai, pa);
+        double2 row = make_double2(0.0, 0.0);
+        const int p = si * no + pa;
+        for (int qa = 0; qa < no; ++qa) {
+          // side 0: R = H -> H(q,j);  side 1: R = H^H -> conj(H(j,q))
+          const double2 r = a.side == 0 ? hbe(a.hop, sj, qa, aj) : cconj(hbe(a.hop, sj, aj, qa));
+          const int q = sj * no + qa;
+          cfma(row, gp[(long long)q * n + p], r);
+        }
+        cfma(acc, l, row);
+      }
+      v = csub(v, acc);
+    }
+    W[e] = v;
+  }
+}
+
+// ---- Y = op(H) X  or  X op(H), H block diagonal ------------------------------------
+__global__ void hop_apply_kernel(HopBD h, int n, int left, int op, const double2* X, long long sX, double2* Y,
+                                 long long sY) {
+  const int b = blockIdx.y;
+  const long long nn = (long long)n * n;
+  const double2* Xb = X + (long long)b * sX;
+  double2* Yb = Y + (long long)b * sY;
+  const int no = h.norb;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nn; e += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(e % n), j = (int)(e / n);
+    double2 acc = make_double2(0.0, 0.0);
+    if (left) {
+      // Y(i,j) = sum_p op(H)(i,p) X(p,j), p in site(i)
+      const int s = i / no, ai = i % no;
+      for (int pa = 0; pa < no; ++pa) {
+        const double2 hv = (op == OP_C) ? cconj(hbe(h, s, pa, ai)) : hbe(h, s, ai, pa);
+        cfma(acc, hv, Xb[(long long)j * n + s * no + pa]);
+      }
+    } else {
+      // Y(i,j) = sum_q X(i,q) op(H)(q,j), q in site(j)
+      const int s = j / no, aj = j % no;
+      for (int qa = 0; qa < no; ++qa) {
+        const double2 hv = (op == OP_C) ? cconj(hbe(h, s, aj, qa)) : hbe(h, s, qa, aj);
+        cfma(acc, Xb[(long long)(s * no + qa) * n + i], hv);
+      }
+    }
+    Yb[e] = acc;
+  }
+}
+
+// ---- site blocks of X Gamma X^H ------------------------------------------------------
+// P[r][a] = sum_k Y(r,k) conj(X(site(r)*no + a, k)); one thread per row r, the k loop is
+// split over KSPLIT groups of threads and reduced in shared memory (fixed order).
+constexpr int SB_ROWS = 64, SB_KSPLIT = 4;
+__global__ void __launch_bounds__(SB_ROWS* SB_KSPLIT) site_blocks_kernel(int n, int no, const double2* Y, long long sY,
+                                                                         const double2* X, long long sX, double2* P,
+                                                                         long long sP) {
+  __shared__ double2 part[SB_KSPLIT][SB_ROWS][4];
+  const int b = blockIdx.y;
+  const int lr = threadIdx.x % SB_ROWS, kg = threadIdx.x / SB_ROWS;
+  const int r = blockIdx.x * SB_ROWS + lr;
+  const double2* Yb = Y + (long long)b * sY;
+  const double2* Xb = X + (long long)b * sX;
+  double2 acc[4] = {make_double2(0, 0), make_double2(0, 0), make_double2(0, 0), make_double2(0, 0)};
+  if (r < n) {
+    const int base = (r / no) * no;
+    const int k_per = (n + SB_KSPLIT - 1) / SB_KSPLIT;
+    const int k_lo = kg * k_per, k_hi = min(n, k_lo + k_per);
+    for (int k = k_lo; k < k_hi; ++k) {
+      const double2 y = Yb[(long long)k * n + r];
+      for (int a = 0; a < no && a < 4; ++a) cfma(acc[a], y, cconj(Xb[(long long)k * n + base + a]));
+    }
+  }
+  for (int a = 0; a < 4; ++a) part[kg][lr][a] = acc[a];
+  __syncthreads();
+  if (kg == 0 && r < n) {
+    for (int a = 0; a < no && a < 4; ++a) {
+      double2 s = part[0][lr][a];
+      for (int q = 1; q < SB_KSPLIT; ++q) s = cadd(s, part[q][lr][a]);
+      P[(long long)b * sP + (long long)r * no + a] = s;
+    }
+  }
+}
+
+// ---- Re sum Q .* conj(X) (one CTA per item, fixed reduction order) -------------------
+__global__ void trace_dot_kernel(int n, const double2* Q, long long sQ, const double2* X, long long sX, double* out,
+                                 int out_stride) {
+  __shared__ double red[EW_THREADS];
+  const int b = blockIdx.x;
+  const long long nn = (long long)n * n;
+  const double2* Qb = Q + (long long)b * sQ;
+  const double2* Xb = X + (long long)b * sX;
+  double s = 0.0;
+  for (long long e = threadIdx.x; e < nn; e += EW_THREADS) {
+    const double2 q = Qb[e], x = Xb[e];
+    s = fma(q.x, x.x, s);
+    s = fma(q.y, x.y, s);
+  }
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = EW_THREADS / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[(long long)b * out_stride] = red[0];
+}
+
+__global__ void gather_kernel(int n, const double2* src, const int* idx, int idx_stride, double2* dst, long long sDst) {
+  const int b = blockIdx.y;
+  const long long nn = (long long)n * n;
+  const double2* s = src + (long long)idx[(long long)b * idx_stride] * nn;
+  double2* d = dst + (long long)b * sDst;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nn; e += (long long)gridDim.x * blockDim.x)
+    d[e] = s[e];
+}
+
+__global__ void copy_kernel(int n, const double2* src, long long sSrc, double2* dst, long long sDst) {
+  const int b = blockIdx.y;
+  const long long nn = (long long)n * n;
+  const double2* s = src + (long long)b * sSrc;
+  double2* d = dst + (long long)b * sDst;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nn; e += (long long)gridDim.x * blockDim.x)
+    d[e] = s[e];
+}
+
+__global__ void identity_kernel(int n, double2* A, long long sA) {
+  const int b = blockIdx.y;
+  const long long nn = (long long)n * n;
+  double2* d = A + (long long)b * sA;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nn; e += (long long)gridDim.x * blockDim.x)
+    d[e] = make_double2((e % n) == (e / n) ? 1.0 : 0.0, 0.0);
+}
+
+// ---- Sancho-Rubio pieces (Contact_Self_Energy.F90:156-269) ---------------------------
+__global__ void form_alpha_kernel(int n, const double* energies, const double2* const* hend, double eta, double extra,
+                                  double2* A, long long sA) {
+  const int b = blockIdx.y;
+  const long long nn = (long long)n * n;
+  const double2* H = hend[b];
+  double2* d = A + (long long)b * sA;
+  const double e0 = energies[b];
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nn; e += (long long)gridDim.x * blockDim.x) {
+    double2 v = make_double2(-H[e].x, -H[e].y);
+    if ((e % n) == (e / n)) { v.x += e0; v.y += eta + extra; }
+    d[e] = v;
+  }
+}
+
+// T += change (if active); cmax = max |change| over the block (NaN propagates)
+__global__ void sr_accumulate_kernel(int n, const int* active, const double2* change, long long sC, double2* T,
+                                     long long sT, double* cmax) {
+  __shared__ double red[EW_THREADS];
+  __shared__ int nan_seen;
+  const int b = blockIdx.x;
+  const long long nn = (long long)n * n;
+  const double2* c = change + (long long)b * sC;
+  double2* t = T + (long long)b * sT;
+  const bool act = active[b] != 0;
+  if (threadIdx.x == 0) nan_seen = 0;
+  __syncthreads();
+  double m = 0.0;
+  bool nan = false;
+  for (long long e = threadIdx.x; e < nn; e += EW_THREADS) {
+    const double2 v = c[e];
+    const double a = hypot(v.x, v.y);
+    if (isnan(a)) nan = true;
+    m = fmax(m, a);
+    if (act) t[e] = cadd(t[e], v);
+  }
+  if (nan) atomicOr(&nan_seen, 1);
+  red[threadIdx.x] = m;
+  __syncthreads();
+  for (int w = EW_THREADS / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + w]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) cmax[b] = nan_seen ? (0.0 / 0.0) : red[0];
+}
+
+// W = alpha - L T with L = H^H (lead 0) or H (lead 1), H block diagonal
+__global__ void sr_form_final_kernel(HopBD h, int n, int lead, const double2* alpha, long long sA, const double2* T,
+                                     long long sT, double2* W, long long sW) {
+  const int b = blockIdx.y;
+  const long long nn = (long long)n * n;
+  const double2* al = alpha + (long long)b * sA;
+  const double2* Tb = T + (long long)b * sT;
+  double2* Wb = W + (long long)b * sW;
+  const int no = h.norb;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nn; e += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(e % n), j = (int)(e / n);
+    const int s = i / no, ai = i % no;
+    double2 acc = make_double2(0.0, 0.0);
+    for (int pa = 0; pa < no; ++pa) {
+      const double2 l = lead == 0 ? cconj(hbe(h, s, pa, ai)) : hbe(h, s, ai, pa);
+      cfma(acc, l, Tb[(long long)j * n + s * no + pa]);
+    }
+    Wb[e] = csub(al[e], acc);
+  }
+}
+
+// Sigma = L g R; lead 0: H^H g H; lead 1: H g H^H.  Gamma = i (Sigma - Sigma^H).
+__global__ void sr_sigma_kernel(HopBD h, int n, int lead, const double2* g, long long sg, double2* sig, long long sS) {
+  const int b = blockIdx.y;
+  const long long nn = (long long)n * n;
+  const double2* gb = g + (long long)b * sg;
+  double2* Sb = sig + (long long)b * sS;
+  const int no = h.norb;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nn; e += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(e % n), j = (int)(e / n);
+    const int si = i / no, ai = i % no, sj = j / no, aj = j % no;
+    double2 acc = make_double2(0.0, 0.0);
+    for (int pa = 0; pa < no; ++pa) {
+      const double2 l = lead == 0 ? cconj(hbe(h, si, pa, ai)) : hbe(h, si, ai, pa);
+      double2 row = make_double2(0.0, 0.0);
+      const int p = si * no + pa;
+      for (int qa = 0; qa < no; ++qa) {
+        const double2 r = lead == 0 ? hbe(h, sj, qa, aj) : cconj(hbe(h, sj, aj, qa));
+        cfma(row, gb[(long long)(sj * no + qa) * n + p], r);
+      }
+      cfma(acc, l, row);
+    }
+    Sb[e] = acc;
+  }
+}
+
+__global__ void gamma_dos_kernel(int n, const double2* sig, long long sS, double2* gam, long long sG, double* dos) {
+  __shared__ double red[EW_THREADS];
+  const int b = blockIdx.x;
+  const long long nn = (long long)n * n;
+  const double2* Sb = sig + (long long)b * sS;
+  double2* Gb = gam + (long long)b * sG;
+  for (long long e = threadIdx.x; e < nn; e += EW_THREADS) {
+    const int i = (int)(e % n), j = (int)(e / n);
+    const double2 s = Sb[e], st = Sb[(long long)i * n + j];
+    // i (S - S^H): S^H(i,j) = conj(S(j,i))
+    const double2 d = make_double2(s.x - st.x, s.y + st.y);
+    Gb[e] = make_double2(-d.y, d.x);
+  }
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += EW_THREADS) s += Sb[(long long)i * n + i].y;
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = EW_THREADS / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) dos[b] = -red[0] / 3.14159265358979323846;
+}
+
+// ---- densities and spin from the site blocks (Calculate_Gnp.F90:117-124,
+//      Calculate_Observables.F90:10-43) -------------------------------------------------
+// One thread per (item, x, site).  Gn_site = f1 P1 + f2 P2, Gp_site = (1-f1) P1 + (1-f2) P2.
+__global__ void density_spin_kernel(DensityArgs a) {
+  const int b = blockIdx.y;
+  const int nsite = a.npy * a.npz;
+  const int total = a.npx * nsite;
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  const int no = a.norb;
+  const Item it = a.items[b];
+  const double w = it.dE / (2.0 * 3.14159265358979323846);
+  double e_n = 0.0, e_p = 0.0;
+  if (idx < total) {
+    const int x = idx / nsite, s = idx % nsite;          // s = y + z*npy (orbital index order)
+    const int y = s % a.npy, z = s / a.npy;
+    const double2* p1 = a.P1 + (long long)b * a.sP + ((long long)x * a.n + (long long)s * no) * no;
+    const double2* p2 = a.P2 + (long long)b * a.sP + ((long long)x * a.n + (long long)s * no) * no;
+    double rn = 0.0, rp = 0.0;
+    double sp[3] = {0.0, 0.0, 0.0};
+    for (int ia = 0; ia < no; ++ia) {
+      const double2 q1 = p1[ia * no + ia], q2 = p2[ia * no + ia];
+      rn += it.f1 * q1.x + it.f2 * q2.x;
+      rp += (1.0 - it.f1) * q1.x + (1.0 - it.f2) * q2.x;
+    }
+    if (a.calc_spin) {
+      // Re sum_{ia,ib} Gn(ia,ib) gM(ib,ia), P stored as P[row ia][col ib]
+      for (int j = 0; j < 3; ++j) {
+        const double2* gm = a.spin_ops + j * no * no;
+        double acc = 0.0;
+        for (int ia = 0; ia < no; ++ia)
+          for (int ib = 0; ib < no; ++ib) {
+            const double2 q1 = p1[ia * no + ib], q2 = p2[ia * no + ib];
+            const double2 gn = make_double2(it.f1 * q1.x + it.f2 * q2.x, it.f1 * q1.y + it.f2 * q2.y);
+            const double2 g = gm[ib * no + ia];
+            acc += gn.x * g.x - gn.y * g.y;
+          }
+        sp[j] = acc;
+      }
+    }
+    // site arrays are (x, y, z) column-major: x fastest
+    const long long o = (long long)x + (long long)a.npx * (y + (long long)a.npy * z);
+    double* so = a.site_out + (long long)b * 5 * total;
+    so[o] = rn * w;
+    so[total + o] = rp * w;
+    so[2 * total + o] = sp[0] * w;
+    so[3 * total + o] = sp[1] * w;
+    so[4 * total + o] = sp[2] * w;
+    e_n = rn;
+    e_p = rp;
+  }
+  // per-item EDensity/HDensity partial sums: written per thread block, summed by host-ordered kernel
+  __shared__ double red_n[256], red_p[256];
+  red_n[threadIdx.x] = e_n;
+  red_p[threadIdx.x] = e_p;
+  __syncthreads();
+  for (int s2 = blockDim.x / 2; s2 > 0; s2 >>= 1) {
+    if (threadIdx.x < s2) {
+      red_n[threadIdx.x] += red_n[threadIdx.x + s2];
+      red_p[threadIdx.x] += red_p[threadIdx.x + s2];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    // partials[b][blockIdx.x][2]
+    a.sums[((long long)b * gridDim.x + blockIdx.x) * 2 + 0] = red_n[0];
+    a.sums[((long long)b * gridDim.x + blockIdx.x) * 2 + 1] = red_p[0];
+  }
+}
+
+__global__ void reduce_sites_kernel(int batch, int total, int nslots, const Item* items, const double* site_out,
+                                    double* acc) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long per_slot = 5LL * total;
+  if (i >= per_slot * nslots) return;
+  const int slot = (int)(i / per_slot);
+  const long long f = i % per_slot;
+  double s = acc[i];
+  for (int b = 0; b < batch; ++b)
+    if (items[b].slot == slot) s += site_out[(long long)b * per_slot + f];
+  acc[i] = s;
+}
+
+}  // namespace
+
+// =====================================================================================
+int form_w(const FormW& a, cudaStream_t st) {
+  form_w_kernel<<<ew_grid((long long)a.n * a.n, a.batch), EW_THREADS, 0, st>>>(a);
+  NEGF_CUDA_TRY(cudaGetLastError());
+  count_launch();
+  return NEGF_OK;
+}
+
+int hop_apply(const HopBD& h, int n, int batch, int left, Op op, const double2* X, long long sX, double2* Y,
+              long long sY, cudaStream_t st) {
+  hop_apply_kernel<<<ew_grid((long long)n * n, batch), EW_THREADS, 0, st>>>(h, n, left, (int)op, X, sX, Y, sY);
+  NEGF_CUDA_TRY(cudaGetLastError());
+  count_launch();
+  return NEGF_OK;
+}
+
+int site_blocks(int n, int norb, int batch, const double2* Y, long long sY, const double2* X, long long sX, double2* P,
+                long long sP, cudaStream_t st) {
+  if (norb > 4) return NEGF_EINVAL;
+  dim3 grid((n + SB_ROWS - 1) / SB_ROWS, batch);
+  site_blocks_kernel<<<grid, SB_ROWS * SB_KSPLIT, 0, st>>>(n, norb, Y, sY, X, sX, P, sP);
+  NEGF_CUDA_TRY(cudaGetLastError());
+  count_launch();
+  return NEGF_OK;
+}
+
+int trace_dot(int n, int batch, const double2* Q, long long sQ, const double2* X, long long sX, double* out,
+              int out_stride, cudaStream_t st) {
+  trace_dot_kernel<<<batch, EW_THREADS, 0, st>>>(n, Q, sQ, X, sX, out, out_stride);
+  NEGF_CUDA_TRY(cudaGetLastError());
+  count_launch();
+  return NEGF_OK;
+}
+
+int gather_blocks(int n, int batch, const double2* src, const int* idx, int idx_stride, double2* dst, long long sDst,
+                  cudaStream_t st) {
+  gather_kernel<<<ew_grid((long long)n * n, batch), EW_THREADS, 0, st>>>(n, src, idx, idx_stride, dst, sDst);
+  NEGF_CUDA_TRY(cudaGetLastError());
+  count_launch();
+  return NEGF_OK;
+}
+
+int copy_blocks(int n, int batch, const double2* src, long long sSrc, double2* dst, long long sDst, cudaStream_t st) {
+  copy_kernel<<<ew_grid((long long)n * n, batch), EW_THREADS, 0, st>>>(n, src, sSrc, dst, sDst);
+  NEGF_CUDA_TRY(cudaGetLastError());
+  count_launch();
+  return NEGF_OK;
+}
+
+int set_identity(int n, int batch, double2* A, long long sA, cudaStream_t st) {
+  identity_kernel<<<ew_grid((long long)n * n, batch), EW_THREADS, 0, st>>>(n, A, sA);
+  NEGF_CUDA_TRY(cudaGetLastError());
+  count_launch();
+  return NEGF_OK;
+}
+
+int form_alpha(int n, int nprob, const double* energies, const double2* const* hend, double eta, double extra_eta,
+               double2* A, long long sA, cudaStream_t st) {
+  form_alpha_kernel<<<ew_grid((long long)n * n, nprob), EW_THREADS, 0, st>>>(n, energies, hend, eta, extra_eta, A, sA);
+  NEGF_CUDA_TRY(cudaGetLastError());
+  count_launch();
+  return NEGF_OK;
+}
+
+int sr_accumulate(int n, int nprob, const int* active, const double2* change, long long sC, double2* T, long long sT,
+                  double* cmax, cudaStream_t st) {
+  sr_accumulate_kernel<<<nprob, EW_THREADS, 0, st>>>(n, active, change, sC, T, sT, cmax);
+  NEGF_CUDA_TRY(cudaGetLastError());
+  count_launch();
+  return NEGF_OK;
+}
+
+int sr_form_final(const HopBD& h, int n, int nprob, int lead, const double2* alpha, long long sA, const double2* T,
+                  long long sT, double2* W, long long sW, cudaStream_t st) {
+  sr_form_final_kernel<<<ew_grid((long long)n * n, nprob), EW_THREADS, 0, st>>>(h, n, lead, alpha, sA, T, sT, W, sW);
+  NEGF_CUDA_TRY(cudaGetLastError());
+  count_launch();
+  return NEGF_OK;
+}
+
+int sr_sigma(const HopBD& h, int n, int nprob, int lead, const double2* g, long long sg, double2* sig, long long sSig,
+             double2* gam, long long sGam, double* dos, cudaStream_t st) {
+  if (lead >= 0) {  // lead < 0: sig already formed (dense HopX), only Gamma and DOS
+    sr_sigma_kernel<<<ew_grid((long long)n * n, nprob), EW_THREADS, 0, st>>>(h, n, lead, g, sg, sig, sSig);
+    NEGF_CUDA_TRY(cudaGetLastError());
+    count_launch();
+  }
+  gamma_dos_kernel<<<nprob, EW_THREADS, 0, st>>>(n, sig, sSig, gam, sGam, dos);
+  NEGF_CUDA_TRY(cudaGetLastError());
+  count_launch();
+  return NEGF_OK;
+}
+
+int density_spin(const DensityArgs& a, cudaStream_t st) {
+  const int total = a.npx * a.npy * a.npz;
+  dim3 grid((total + 255) / 256, a.batch);
+  density_spin_kernel<<<grid, 256, 0, st>>>(a);
+  NEGF_CUDA_TRY(cudaGetLastError());
+  count_launch();
+  return NEGF_OK;
+}
+
+int reduce_sites(int batch, int nsite_total, int nslots, const Item* items, const double* site_out, double* acc,
+                 cudaStream_t st) {
+  const long long n = 5LL * nsite_total * nslots;
+  reduce_sites_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(batch, nsite_total, nslots, items, site_out, acc);
+  NEGF_CUDA_TRY(cudaGetLastError());
+  count_launch();
+  return NEGF_OK;
+}
+
+}  // namespace negf

@@ -1,0 +1,114 @@
+"""Model-0 topological-insulator nanowire Hamiltonian (the solve's input producer).
+
+The reference builds Htotd (M x M x Npx) and HopX (M x M) in Build_Hamiltonian
+(Source/Build_Hamiltonian.F90:13-18,59-100) on the MPI root.  This module builds the same
+arrays on the host with NumPy for the wire the benchmarks use:
+
+    on-site  (M0 - 6B) tau_z sigma_0 + V_i + Z tau_0 sigma_z
+    hop_j    B tau_z sigma_0 - (i A / 2) tau_x sigma_j        (j = x, y, z)
+
+in the tau (x) sigma basis (orbital = 2*tau + sigma), or, with ``basis="reference"``,
+the reference's own Dirac matrices g0..g3 (Source/Read_In_Allocate.F90:161-181) with
+AA = (MM - 3/a0^2) g0 and Hop_j = (g0/a0^2 - i g_j/a0)/2.
+
+Layout conventions follow the reference: in-slice orbital index
+orb + y*norb + z*norb*npy (Source/Build_Hamiltonian.F90:160); the y-hop carries the
+Aharonov-Bohm phase exp(i 2 pi z Phi / ((npy-1)(npz-1))) (Landau gauge,
+Source/Build_Hamiltonian.F90:186-207); Anderson disorder is added on slices 2..npx-1
+only (Source/Build_Hamiltonian.F90:279-296), so the end slices equal the leads.
+Arrays are returned slice-first: htotd[x, row, col], hopx[row, col].
+"""
+from __future__ import annotations
+
+import numpy as np
+
+NORB = 4
+
+_s0 = np.eye(2, dtype=complex)
+_sx = np.array([[0, 1], [1, 0]], dtype=complex)
+_sy = np.array([[0, -1j], [1j, 0]], dtype=complex)
+_sz = np.array([[1, 0], [0, -1]], dtype=complex)
+
+
+def tau_sigma(t, s):
+    return np.kron(t, s)
+
+
+def spin_operators():
+    """tau_0 sigma_{x,y,z}: the spin operators gMx, gMy, gMz (Source/Read_In_Allocate.F90:183-196)."""
+    return tau_sigma(_s0, _sx), tau_sigma(_s0, _sy), tau_sigma(_s0, _sz)
+
+
+def site_blocks(M0=0.3, B=0.25, A=0.5, zeeman=0.0, basis="tau_sigma"):
+    """(onsite, hop_x, hop_y, hop_z) 4x4 blocks."""
+    if basis == "tau_sigma":
+        tz = tau_sigma(_sz, _s0)
+        onsite = (M0 - 6.0 * B) * tz + zeeman * tau_sigma(_s0, _sz)
+        hops = [B * tz - 0.5j * A * tau_sigma(_sx, s) for s in (_sx, _sy, _sz)]
+        return onsite, hops[0], hops[1], hops[2]
+    if basis == "reference":
+        c0, c1, ci = 0j, 1 + 0j, 1j
+        g0 = np.diag([c1, c1, -c1, -c1])
+        g1 = np.array([[c0, c0, c0, -ci], [c0, c0, ci, c0], [c0, -ci, c0, c0], [ci, c0, c0, c0]])
+        g2 = np.array([[c0, c0, c0, -c1], [c0, c0, -c1, c0], [c0, -c1, c0, c0], [-c1, c0, c0, c0]])
+        g3 = np.array([[c0, c0, -ci, c0], [c0, c0, c0, -ci], [ci, c0, c0, c0], [c0, ci, c0, c0]])
+        mm, a0 = 1.5, 1.0
+        onsite = (mm - 3.0 / (a0 * a0)) * g0 + zeeman * tau_sigma(_s0, _sz)
+        hops = [0.5 * (g0 / (a0 * a0) - 1j / a0 * g) for g in (g1, g2, g3)]
+        return onsite, hops[0], hops[1], hops[2]
+    raise ValueError("basis must be 'tau_sigma' or 'reference'")
+
+
+def disorder_potential(npx, npy, npz, W, seed):
+    """Uniform V in [-W/2, W/2] per site on slices 2..npx-1 (zero on the end slices),
+    drawn in (x, y, z) order from numpy's PCG64 seeded with ``seed``."""
+    v = np.zeros((npx, npy, npz))
+    if W != 0.0 and npx > 2:
+        rng = np.random.Generator(np.random.PCG64(seed))
+        v[1:npx - 1] = (rng.random((npx - 2, npy, npz)) - 0.5) * W
+    return v
+
+
+def ti_wire(npx, npy, npz, M0=0.3, B=0.25, A=0.5, zeeman=0.0, flux=0.0, W=0.0, seed=0,
+            basis="tau_sigma", disorder=None):
+    """Build (htotd[npx, M, M], hopx[M, M]) complex128 for an open-boundary wire.
+
+    ``flux`` is the Aharonov-Bohm flux through the cross-section in units of Phi_0;
+    ``W``/``seed`` give Anderson disorder unless an explicit ``disorder`` array
+    (npx, npy, npz) is passed.
+    """
+    onsite, hx, hy, hz = site_blocks(M0, B, A, zeeman, basis)
+    nsite = npy * npz
+    m = NORB * nsite
+    h = np.zeros((m, m), dtype=complex)
+    hopx = np.zeros((m, m), dtype=complex)
+
+    def sl(y, z):
+        i = (y + z * npy) * NORB
+        return slice(i, i + NORB)
+
+    for z in range(npz):
+        for y in range(npy):
+            s = sl(y, z)
+            h[s, s] = onsite
+            hopx[s, s] = hx
+            if y + 1 < npy:
+                t = sl(y + 1, z)
+                blk = hy
+                if flux != 0.0 and npy > 1 and npz > 1:
+                    blk = hy * np.exp(1j * 2.0 * np.pi * z * flux / ((npy - 1) * (npz - 1)))
+                h[s, t] = blk
+                h[t, s] = blk.conj().T
+            if z + 1 < npz:
+                t = sl(y, z + 1)
+                h[s, t] = hz
+                h[t, s] = hz.conj().T
+    htotd = np.repeat(h[None], npx, axis=0)
+    if disorder is None:
+        disorder = disorder_potential(npx, npy, npz, W, seed)
+    if np.any(disorder != 0.0):
+        # v[x, y, z] on the diagonal of site (y, z): orbital index (y + z*npy)*NORB + orb
+        diag = np.repeat(disorder.transpose(0, 2, 1).reshape(npx, nsite), NORB, axis=1)
+        idx = np.arange(m)
+        htotd[:, idx, idx] += diag
+    return htotd, hopx

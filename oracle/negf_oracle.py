@@ -1,0 +1,469 @@
+"""CPU oracle for the per-energy NEGF solve.
+
+TEST INFRASTRUCTURE ONLY.  Nothing in the product path imports this module; it is the
+checker that the CUDA path is compared against (tests/, ``__graft_entry__.smoke()`` and
+the ``cpu_baseline`` / ``--impl reference`` legs of ``bench.py``).
+
+It restates, in NumPy complex128 with LAPACK ``zgetrf``/``zgetri`` (the routines the
+reference calls through MKL), the reference's per-energy path:
+
+    Source/Energy_Sweep.F90:1-46            energy_sweep()
+    Source/Contact_Self_Energy.F90:1-152    contact_self_energy()
+    Source/Contact_Self_Energy.F90:156-269  sancho_rubio()
+    Source/MKL_Routines_Cluster.F90:2-33    invert_matrix()
+    Source/Recursive_Greens.F90:2-107       get_retarded_greens()
+    Source/Calculate_Gnp.F90:1-136          calculate_gnp()
+    Source/Calculate_Observables.F90:2-169  calculate_observables()
+    Source/Build_Hamiltonian.F90:1-207      build_hamiltonian_reference() (model 0 only)
+    Source/Read_In_Allocate.F90:161-197     gamma matrices
+
+The algorithm follows the reference step by step: the backward GRd/GRu/GRl recursion
+is kept, Gn/Gp are formed as full blocks, and the same zgemm products are taken in
+the same order.  The reference's naive quadruple loops in Calculate_Gnp are written
+here as matrix products of the same operands, so results differ from a literal loop
+only by floating-point summation order.
+
+Parity status: UNPINNED against the reference executable.  The reference is Fortran 90
++ MKL + MPI; no Fortran compiler exists in the build container or on the GPU host, and
+the reference ships no tests, golden vectors or fixtures.  The oracle is pinned instead
+by (i) a dense inversion of the full (Npx*M)^2 matrix, (ii) physics invariants (integer
+transmission of a clean wire, L<->R reciprocity, the A = Gn + Gp sum rule, the surface
+Dyson equation of the lead self-energy) and (iii) committed golden vectors it generated
+(tests/golden/make_golden.py).
+
+Reference quirks are exposed as parameters of ``SolveOptions``; the defaults are the
+reference's own values (eta = 1e-4, Sancho-Rubio tolerance 1e-8, T=0 step occupations).
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+from typing import Optional
+
+import numpy as np
+from scipy.linalg import lapack
+
+# Source/Constants.F90:3-7
+Q_E = 1.602e-19
+H_PLANCK = 6.626e-34
+PI = 4.0 * math.atan(1.0)
+HBAR = H_PLANCK / (2.0 * PI)
+ETA_SIGMA_REFERENCE = 1e-4
+
+
+# ---------------------------------------------------------------------------
+# Gamma / spin matrices, Source/Read_In_Allocate.F90:161-197 (Nh == 4)
+# ---------------------------------------------------------------------------
+def reference_gamma_matrices():
+    """Return (g0, g1, g2, g3, gMx, gMy, gMz) exactly as Read_In_Allocate.F90:161-197."""
+    c0, c1, ci = 0j, 1 + 0j, 1j
+    g1 = np.array([[c0, c0, c0, -ci], [c0, c0, ci, c0], [c0, -ci, c0, c0], [ci, c0, c0, c0]])
+    g2 = np.array([[c0, c0, c0, -c1], [c0, c0, -c1, c0], [c0, -c1, c0, c0], [-c1, c0, c0, c0]])
+    g3 = np.array([[c0, c0, -ci, c0], [c0, c0, c0, -ci], [ci, c0, c0, c0], [c0, ci, c0, c0]])
+    g0 = np.diag([c1, c1, -c1, -c1])
+    gMx = np.array([[c0, c1, c0, c0], [c1, c0, c0, c0], [c0, c0, c0, c1], [c0, c0, c1, c0]])
+    gMy = np.array([[c0, -ci, c0, c0], [ci, c0, c0, c0], [c0, c0, c0, -ci], [c0, c0, ci, c0]])
+    gMz = np.diag([c1, -c1, c1, -c1])
+    return g0, g1, g2, g3, gMx, gMy, gMz
+
+
+# ---------------------------------------------------------------------------
+# Hamiltonian, model 0 (channelType == 0), Source/Build_Hamiltonian.F90
+# ---------------------------------------------------------------------------
+def build_hamiltonian_reference(npx, npy, npz, a0=1.0, mu_t=0.0, ab_phi=0.0, bcy=0, bcz=0,
+                                disorder=None, onsite_blocks=None, hops=None):
+    """Model-0 slice Hamiltonian, following Build_Hamiltonian.F90:13-18,59-100,154-207.
+
+    ``disorder`` is an optional real array (npx, npy, npz) of on-site potentials added by
+    Insert_Impurity (Build_Hamiltonian.F90:154-165); the reference only fills slices
+    2..npx-1 (Build_Hamiltonian.F90:279-296) and the caller is expected to do the same.
+    ``onsite_blocks``/``hops`` override the 4x4 AA and (HopX, HopY, HopZ) blocks; by
+    default they are the reference's own (MM = 1.5, Build_Hamiltonian.F90:14-18).
+    Returns (Htotd[npx, M, M], HopX[M, M]) as complex128, slice index first.
+    """
+    norb = 4
+    g0, g1, g2, g3, *_ = reference_gamma_matrices()
+    ident = np.eye(4, dtype=complex)
+    if onsite_blocks is None:
+        mm = 1.5
+        aa = (mm - 3.0 / (a0 * a0)) * g0 - mu_t * ident
+    else:
+        aa = np.asarray(onsite_blocks, dtype=complex)
+    if hops is None:
+        hx = 0.5 * (1.0 / (a0 * a0) * g0 - 1j / a0 * g1)
+        hy = 0.5 * (1.0 / (a0 * a0) * g0 - 1j / a0 * g2)
+        hz = 0.5 * (1.0 / (a0 * a0) * g0 - 1j / a0 * g3)
+    else:
+        hx, hy, hz = (np.asarray(h, dtype=complex) for h in hops)
+    nn = npy * norb
+    m = npz * nn
+    # Build_Hamiltonian.F90:59-64: HopZ is block diagonal over y, HopX over (y, z)
+    hopz_full = np.zeros((nn, nn), dtype=complex)
+    for yy in range(npy):
+        hopz_full[yy * norb:(yy + 1) * norb, yy * norb:(yy + 1) * norb] = hz
+    hopx = np.zeros((m, m), dtype=complex)
+    for s in range(npy * npz):
+        hopx[s * norb:(s + 1) * norb, s * norb:(s + 1) * norb] = hx
+    # :66-79 intraslice y chain
+    hh1d = np.zeros((nn, nn), dtype=complex)
+    for yy in range(npy - 1):
+        hh1d[norb * yy:norb * (yy + 1), norb * yy:norb * (yy + 1)] = aa
+        hh1d[norb * yy:norb * (yy + 1), norb * (yy + 1):norb * (yy + 2)] = hy
+        hh1d[norb * (yy + 1):norb * (yy + 2), norb * yy:norb * (yy + 1)] = hy.conj().T
+    hh1d[nn - norb:nn, nn - norb:nn] = aa
+    if bcy == 1:
+        hh1d[0:norb, nn - norb:nn] = hy.conj().T
+        hh1d[nn - norb:nn, 0:norb] = hy
+    # :82-94 z stacking
+    hh2d = np.zeros((m, m), dtype=complex)
+    for zz in range(npz - 1):
+        hh2d[zz * nn:(zz + 1) * nn, zz * nn:(zz + 1) * nn] = hh1d
+        hh2d[zz * nn:(zz + 1) * nn, (zz + 1) * nn:(zz + 2) * nn] = hopz_full
+        hh2d[(zz + 1) * nn:(zz + 2) * nn, zz * nn:(zz + 1) * nn] = hopz_full.conj().T
+    hh2d[m - nn:m, m - nn:m] = hh1d
+    if bcz == 1:
+        hh2d[0:nn, nn * (npz - 1):nn * npz] = hopz_full.conj().T
+        hh2d[nn * (npz - 1):nn * npz, 0:nn] = hopz_full
+    htotd = np.repeat(hh2d[None, :, :], npx, axis=0)
+    # :186-207 Aharonov-Bohm phase on the y hops (Landau gauge)
+    if ab_phi > 1e-10:
+        for zz in range(1, npz + 1):
+            phase = np.exp(1j * 2.0 * PI * float(zz - 1) * ab_phi / float(npy - 1) / float(npz - 1))
+            for xx in range(npx):
+                for yy in range(1, npy):
+                    idx = (yy - 1) * norb + (zz - 1) * nn
+                    blk = htotd[xx, idx:idx + norb, idx + norb:idx + 2 * norb] * phase
+                    htotd[xx, idx:idx + norb, idx + norb:idx + 2 * norb] = blk
+                    htotd[xx, idx + norb:idx + 2 * norb, idx:idx + norb] = blk.conj().T
+    # :154-165 Insert_Impurity (on-site potential times identity on the site block)
+    if disorder is not None:
+        for xx in range(npx):
+            for yy in range(npy):
+                for zz in range(npz):
+                    v = disorder[xx, yy, zz]
+                    if v != 0.0:
+                        idx = yy * norb + zz * nn
+                        htotd[xx, idx:idx + norb, idx:idx + norb] += v * ident
+    return htotd, hopx
+
+
+# ---------------------------------------------------------------------------
+# Options (reference quirks as switches)
+# ---------------------------------------------------------------------------
+@dataclasses.dataclass
+class SolveOptions:
+    """Per-run switches.  Defaults are the reference's own values."""
+    eta: float = ETA_SIGMA_REFERENCE        # Source/Constants.F90:7
+    sr_tol: float = 1e-8                     # Source/Contact_Self_Energy.F90:200
+    sr_max_iter: int = 20000                 # Source/Contact_Self_Energy.F90:200,248
+    kT: float = 0.0                          # 0 -> T=0 step, Source/Energy_Sweep.F90:11-21
+    calc_spin: bool = False                  # calcSigExp, Source/Read_In_Allocate.F90:93
+    norb: int = 4
+
+
+def fermi(energy: float, mu_c: float, kT: float) -> float:
+    """Occupation of a lead.  kT == 0 is the reference's step ``energy <= mu_c``
+    (Source/Energy_Sweep.F90:11-21, with mu_c = muT - mu(c)); kT > 0 is Fermi-Dirac."""
+    if kT <= 0.0:
+        return 1.0 if energy <= mu_c else 0.0
+    x = (energy - mu_c) / kT
+    if x > 700:
+        return 0.0
+    return 1.0 / (1.0 + math.exp(x))
+
+
+# ---------------------------------------------------------------------------
+# Dense LA, Source/MKL_Routines_Cluster.F90:2-33
+# ---------------------------------------------------------------------------
+def invert_matrix(g: np.ndarray):
+    """ZGETRF then, if INFO == 0, ZGETRI.  Returns (inverse, info)."""
+    lu, piv, info = lapack.zgetrf(np.asfortranarray(g))
+    if info != 0:
+        return lu, int(info)
+    inv, info2 = lapack.zgetri(lu, piv)
+    return inv, int(info2)
+
+
+# ---------------------------------------------------------------------------
+# Sancho-Rubio, Source/Contact_Self_Energy.F90:156-269
+# ---------------------------------------------------------------------------
+def sancho_rubio(alpha: np.ndarray, beta: np.ndarray, eta: float, tol: float, max_iter: int):
+    """Lopez-Sancho/Rubio decimation.  Returns (Sigma, error_flag, iterations).
+
+    The iteration counter is local to the call; in the reference it is an implicitly
+    SAVEd ``INTEGER :: counter=1`` (Contact_Self_Energy.F90:165) shared by all calls, a
+    difference that only matters when the 20000-iteration cap is hit.
+    """
+    nn = alpha.shape[0]
+    ident = np.eye(nn, dtype=complex)
+    betad = beta.conj().T
+    # :187 tmp = inv(alpha + i*eta) (an extra i*eta on top of the one in alpha)
+    tmp, err = invert_matrix(alpha + ident * complex(0.0, eta))
+    t = -tmp @ betad                    # :193
+    tt = -tmp @ beta                    # :195
+    cap_t = t.copy()                    # :197
+    toldt = ident.copy()                # :198
+    change_max = 1.0                    # change initialised to c1, :181
+    counter = 1
+    while counter <= max_iter and change_max > tol:       # :200
+        counter += 1
+        toldt = toldt @ tt                                  # :203-204
+        cmat1 = ident - t @ tt - tt @ t                     # :206-208
+        tmp, err = invert_matrix(cmat1)                     # :209
+        if err:
+            raise RuntimeError("Sancho_Rubio: singular inv(Id - t*tt - tt*t)")  # :210-213 STOP
+        t = (tmp @ t) @ t                                   # :216-218
+        tt = (tmp @ tt) @ tt                                # :220-222
+        change = toldt @ t                                  # :224
+        cap_t = cap_t + change                              # :226
+        abs_change = np.abs(change)
+        if np.isnan(abs_change).any():                      # :228-237
+            return None, 1, counter - 1
+        change_max = float(abs_change.max())
+    cmat1 = beta @ cap_t + alpha                            # :241-242
+    gfinal, err = invert_matrix(cmat1)                      # :243
+    if counter == max_iter:                                 # :248-251
+        err = 1
+    sigma = (beta @ gfinal) @ beta.conj().T                 # :254-255
+    return sigma, err, counter - 1
+
+
+# ---------------------------------------------------------------------------
+# Contact_Self_Energy (contactType 0), Source/Contact_Self_Energy.F90:1-152
+# ---------------------------------------------------------------------------
+def contact_self_energy(htotd, hopx, energy, opt: SolveOptions):
+    """Returns dict with SigmaL, SigmaR, GammaL, GammaR, dosc (2,), sr_err (2,), sr_iters (2,)."""
+    npx, m, _ = htotd.shape
+    ident = np.eye(m, dtype=complex)
+    ce = complex(energy, opt.eta)                           # :62
+    alpha = -htotd[0] + ident * ce                          # :117-120
+    sig_l, err_l, it_l = sancho_rubio(alpha, -hopx.conj().T, opt.eta, opt.sr_tol, opt.sr_max_iter)
+    alpha = -htotd[npx - 1] + ident * ce                    # :129-132
+    sig_r, err_r, it_r = sancho_rubio(alpha, -hopx, opt.eta, opt.sr_tol, opt.sr_max_iter)
+    if sig_l is None or sig_r is None:
+        raise FloatingPointError("Sancho_Rubio produced NaN")
+    dosc = np.array([-np.imag(np.trace(sig_l)) / PI, -np.imag(np.trace(sig_r)) / PI])  # :140-143
+    gam_l = 1j * (sig_l - sig_l.conj().T)                   # :146
+    gam_r = 1j * (sig_r - sig_r.conj().T)                   # :147
+    return dict(SigmaL=sig_l, SigmaR=sig_r, GammaL=gam_l, GammaR=gam_r, dosc=dosc,
+                sr_err=np.array([err_l, err_r]), sr_iters=np.array([it_l, it_r]))
+
+
+# ---------------------------------------------------------------------------
+# Get_Retarded_Greens, Source/Recursive_Greens.F90:2-107
+# ---------------------------------------------------------------------------
+def get_retarded_greens(inv_grd, hopx):
+    """inv_grd: (npx, M, M).  Returns dict with GRLef (npx, M, M) = G_{x,1},
+    GRRgt (npx, M, M) = G_{x,N}, GRd, GRu, GRl and the error flags of the inverses."""
+    npx, m, _ = inv_grd.shape
+    mh = -hopx
+    mhd = mh.conj().T
+    ident = np.eye(m, dtype=complex)
+    infos = []
+    glr = np.empty_like(inv_grd)
+    for i in range(npx):                                    # :16-34
+        if i > 0:
+            cmat1 = inv_grd[i] - (mhd @ glr[i - 1]) @ mh    # :18-20
+        else:
+            cmat1 = inv_grd[i]
+        glr[i], info = invert_matrix(cmat1)                 # :26
+        infos.append(info)
+    grd = np.empty_like(inv_grd)
+    gru = np.empty((max(npx - 1, 0), m, m), dtype=complex)
+    grl = np.empty((max(npx - 1, 0), m, m), dtype=complex)
+    grd[npx - 1] = glr[npx - 1]                             # :37
+    for i in range(npx - 2, -1, -1):                        # :38-51
+        grl[i] = (-(grd[i + 1] @ mhd)) @ glr[i]             # :40-41
+        gru[i] = (-(glr[i] @ mh)) @ grd[i + 1]              # :43-44
+        cmat1 = -(mh @ grl[i]) + ident                      # :46-49
+        grd[i] = glr[i] @ cmat1                             # :50
+    grrgt = np.zeros_like(inv_grd)                          # :53-63
+    grrgt[npx - 1] = grd[npx - 1]
+    if npx >= 2:
+        grrgt[npx - 2] = gru[npx - 2]
+    for ii in range(1, npx - 1):
+        jj = npx - 1 - ii                                   # 1-based jj; block jj-1 <- block jj
+        grrgt[jj - 1] = (-(glr[jj - 1] @ mh)) @ grrgt[jj]
+    grr = np.empty_like(inv_grd)                            # :67-86
+    for i in range(npx - 1, -1, -1):
+        if i < npx - 1:
+            cmat1 = inv_grd[i] - (mh @ grr[i + 1]) @ mhd
+        else:
+            cmat1 = inv_grd[i]
+        grr[i], info = invert_matrix(cmat1)
+        infos.append(info)
+    grlef = np.zeros_like(inv_grd)                          # :88-96
+    grlef[0] = grd[0]
+    if npx >= 2:
+        grlef[1] = grl[0]
+    for i in range(0, npx - 1):
+        grlef[i + 1] = (-(grr[i + 1] @ mhd)) @ grlef[i]     # :92-96 (the first pass overwrites GRl(1))
+    return dict(GRLef=grlef, GRRgt=grrgt, GRd=grd, GRu=gru, GRl=grl, infos=np.array(infos))
+
+
+# ---------------------------------------------------------------------------
+# Calculate_Gnp, Source/Calculate_Gnp.F90:1-136
+# ---------------------------------------------------------------------------
+def calculate_gnp(grlef, grrgt, gam_l, gam_r, f1, f2, with_offdiag=True):
+    """Gn/Gp diagonal (npx, M, M) and, optionally, the +-1 blocks (npx-1, M, M)."""
+    npx = grlef.shape[0]
+    out = {}
+    for name, fa, fb in (("n", f1, f2), ("p", 1.0 - f1, 1.0 - f2)):
+        c_l = fa * (grlef @ gam_l)                          # :12-18 / :64-70
+        c_r = fb * (grrgt @ gam_r)                          # :37-43 / :90-96
+        d = c_l @ grlef.conj().transpose(0, 2, 1) + c_r @ grrgt.conj().transpose(0, 2, 1)
+        out["G%sd" % name] = d                              # :20-35 diagonal blocks
+        if with_offdiag and npx > 1:
+            out["G%su" % name] = (c_l[:-1] @ grlef[1:].conj().transpose(0, 2, 1)
+                                  + c_r[:-1] @ grrgt[1:].conj().transpose(0, 2, 1))
+            out["G%sl" % name] = (c_l[1:] @ grlef[:-1].conj().transpose(0, 2, 1)
+                                  + c_r[1:] @ grrgt[:-1].conj().transpose(0, 2, 1))
+    return out
+
+
+def site_density(gd, npy, npz, norb=4):
+    """Re diag(G?d) summed over the orbitals of each site -> (npx, npy, npz);
+    index ii+(yy-1)*Norb+(zz-1)*NN as Calculate_Gnp.F90:118-124."""
+    npx = gd.shape[0]
+    diag = np.real(np.diagonal(gd, axis1=1, axis2=2))       # (npx, M)
+    per_site = diag.reshape(npx, npz, npy, norb).sum(axis=3)  # in-slice index (orb, y, z), z slowest
+    return per_site.transpose(0, 2, 1)                      # -> (x, y, z)
+
+
+# ---------------------------------------------------------------------------
+# Calculate_Observables, Source/Calculate_Observables.F90:2-169 (non-BdG branch)
+# ---------------------------------------------------------------------------
+def calculate_observables(gnp, grrgt, gam_l, gam_r, htotd, hopx, f1, f2, de, npy, npz,
+                          calc_spin=False, calc_currents=True, norb=4):
+    npx = htotd.shape[0]
+    nn = npy * norb
+    res = {}
+    gnd, gpd = gnp["Gnd"], gnp["Gpd"]
+    _, _, _, _, gmx, gmy, gmz = reference_gamma_matrices()
+    if calc_spin:                                           # :10-30
+        # site blocks Gnd(idx+ii, idx+jj) with idx = y*Norb + z*NN, summed against gM(jj, ii)
+        nsite = npy * npz
+        blocks = gnd.reshape(npx, nsite, norb, nsite, norb)
+        diag_blocks = blocks[:, np.arange(nsite), :, np.arange(nsite), :]   # (nsite, npx, norb, norb)
+        sig = np.zeros((3, npx, npy, npz))
+        for j, gm in enumerate((gmx, gmy, gmz)):
+            v = de / (2.0 * PI) * np.real(np.einsum("sxab,ba->xs", diag_blocks, gm))
+            sig[j] = v.reshape(npx, npz, npy).transpose(0, 2, 1)
+        res["SigExp"] = sig
+    # :33-43 electron/hole DOS at this energy
+    res["EDensity"] = float(np.real(np.trace(gnd, axis1=1, axis2=2)).sum() / (2.0 * PI))
+    res["HDensity"] = float(np.real(np.trace(gpd, axis1=1, axis2=2)).sum() / (2.0 * PI))
+    # :46-53 injected modes
+    res["Modec1"] = float(np.real(np.sum(gam_l * (gnd[0] + gpd[0]).T)))
+    res["Modec2"] = float(np.real(np.sum(gam_r * (gnd[npx - 1] + gpd[npx - 1]).T)))
+    # :85-100 transmission
+    g1n = grrgt[0]
+    cmat1 = gam_l @ g1n
+    cmat2 = gam_r @ g1n.conj().T
+    t12 = float(np.real(np.sum(cmat1 * cmat2.T)))
+    res["T12"] = t12
+    res["ContactCurrent"] = np.array([Q_E * de / H_PLANCK * (t12 * (f2 - f1)),
+                                      Q_E * de / H_PLANCK * (t12 * (f1 - f2))])  # :102-103
+    if calc_currents and "Gnu" in gnp:                      # :110-169, dumVar is REAL(4)
+        jx = np.zeros((npx, npy, npz))
+        jy = np.zeros((npx, npy, npz))
+        jz = np.zeros((npx, npy, npz))
+        gnu, gnl, gpu_, gpl = gnp["Gnu"], gnp["Gnl"], gnp["Gpu"], gnp["Gpl"]
+        pref = 1j * Q_E * Q_E / HBAR
+        w = de / (2.0 * PI)
+        for xx in range(npx):
+            h = htotd[xx]
+            for yy in range(npy):
+                for zz in range(npz):
+                    idx = yy * norb + zz * nn
+                    a = slice(idx, idx + norb)
+                    if yy < npy - 1:
+                        b = slice(idx + norb, idx + 2 * norb)
+                        v = (h[a, b] * gnd[xx][b, a].T - gnd[xx][a, b] * h[b, a].T
+                             - h[a, b] * gpd[xx][b, a].T + gpd[xx][a, b] * h[b, a].T)
+                        jy[xx, yy, zz] = np.sum(np.float32(np.real(pref * v)).astype(np.float64) * w)
+                    if zz < npz - 1:
+                        b = slice(idx + nn, idx + nn + norb)
+                        v = (h[a, b] * gnd[xx][b, a].T - gnd[xx][a, b] * h[b, a].T
+                             - h[a, b] * gpd[xx][b, a].T + gpd[xx][a, b] * h[b, a].T)
+                        jz[xx, yy, zz] = np.sum(np.float32(np.real(pref * v)).astype(np.float64) * w)
+                    if xx < npx - 1:
+                        hx = hopx[a, a]
+                        v = (hx * gnl[xx][a, a].T - gnu[xx][a, a] * np.conj(hx)
+                             - hx * gpl[xx][a, a].T + gpu_[xx][a, a] * np.conj(hx))
+                        jx[xx, yy, zz] = np.sum(np.float32(np.real(pref * v)).astype(np.float64) * w)
+        res["Jx"], res["Jy"], res["Jz"] = jx, jy, jz
+    return res
+
+
+# ---------------------------------------------------------------------------
+# Energy_Sweep, Source/Energy_Sweep.F90:1-46
+# ---------------------------------------------------------------------------
+def energy_sweep(htotd, hopx, energy, mu_lead, de, npy, npz, opt: SolveOptions,
+                 calc_currents=False, keep_blocks=False):
+    """One energy point.  ``mu_lead`` = (muT - mu(1), muT - mu(2)), the lead
+    electrochemical potentials.  Returns a dict of per-energy results, with RhoN/RhoP
+    and spin already weighted by dE/(2 pi) as the reference accumulates them."""
+    npx, m, _ = htotd.shape
+    f1 = fermi(energy, mu_lead[0], opt.kT)
+    f2 = fermi(energy, mu_lead[1], opt.kT)
+    cse = contact_self_energy(htotd, hopx, energy, opt)
+    ident = np.eye(m, dtype=complex)
+    inv_grd = -htotd + ident[None] * complex(energy, opt.eta)   # :31-36
+    inv_grd[0] = inv_grd[0] - cse["SigmaL"]                     # :37
+    inv_grd[npx - 1] = inv_grd[npx - 1] - cse["SigmaR"]         # :38
+    rg = get_retarded_greens(inv_grd, hopx)
+    gnp = calculate_gnp(rg["GRLef"], rg["GRRgt"], cse["GammaL"], cse["GammaR"], f1, f2,
+                        with_offdiag=calc_currents)
+    out = dict(energy=energy, f1=f1, f2=f2, dosc=cse["dosc"], sr_iters=cse["sr_iters"],
+               sr_err=cse["sr_err"], rgf_infos=rg["infos"])
+    out["RhoN"] = site_density(gnp["Gnd"], npy, npz, opt.norb) * (de / (2.0 * PI))
+    out["RhoP"] = site_density(gnp["Gpd"], npy, npz, opt.norb) * (de / (2.0 * PI))
+    obs = calculate_observables(gnp, rg["GRRgt"], cse["GammaL"], cse["GammaR"], htotd, hopx,
+                                f1, f2, de, npy, npz, calc_spin=opt.calc_spin,
+                                calc_currents=calc_currents, norb=opt.norb)
+    out.update(obs)
+    if keep_blocks:
+        out.update(cse)
+        out.update(rg)
+        out.update(gnp)
+    return out
+
+
+def energy_axis_reference(mu, mu_t, n_e=600):
+    """Source/Read_In_Allocate.F90:248-259 (no Poisson, normal contacts)."""
+    e_min = mu_t - max(mu) - 1e-10
+    e_max = mu_t - min(mu) + 1e-10
+    de = (e_max - e_min) / (n_e - 1)
+    return e_min + de * np.arange(n_e), de
+
+
+def energy_weights(eaxis, de0):
+    """dE used at each energy: EAxis(e+1)-EAxis(e), except the last point which keeps
+    the previous value (Source/Energy_Sweep.F90:7-9; deltaE is a module variable that
+    starts at (eMax-eMin)/(eStpnum-1), Source/Read_In_Allocate.F90:255)."""
+    n = len(eaxis)
+    w = np.empty(n)
+    prev = de0
+    for e in range(n):
+        if e != n - 1:
+            prev = eaxis[e + 1] - eaxis[e]
+        w[e] = prev
+    return w
+
+
+# ---------------------------------------------------------------------------
+# Dense cross-check (not the reference algorithm): full (npx*M)^2 inverse
+# ---------------------------------------------------------------------------
+def dense_retarded_greens(htotd, hopx, sig_l, sig_r, energy, eta):
+    npx, m, _ = htotd.shape
+    n = npx * m
+    a = np.zeros((n, n), dtype=complex)
+    for x in range(npx):
+        a[x * m:(x + 1) * m, x * m:(x + 1) * m] = complex(energy, eta) * np.eye(m) - htotd[x]
+        if x + 1 < npx:
+            a[x * m:(x + 1) * m, (x + 1) * m:(x + 2) * m] = -hopx
+            a[(x + 1) * m:(x + 2) * m, x * m:(x + 1) * m] = -hopx.conj().T
+    a[0:m, 0:m] -= sig_l
+    a[n - m:n, n - m:n] -= sig_r
+    return np.linalg.inv(a)

@@ -1,0 +1,85 @@
+"""C ABI checks that need no GPU: the library builds, loads and exports every symbol
+include/negf.h declares; the ctypes structures match the C layout; without a device the
+library refuses to run (there is no CPU fallback)."""
+import ctypes
+import os
+import re
+import subprocess
+import tempfile
+
+import pytest
+
+from conftest import REPO, gpu_available
+from nonequilibriumgreensfunction_gb300 import capi
+
+HEADER = os.path.join(REPO, "include", "negf.h")
+
+
+def declared_symbols():
+    txt = open(HEADER).read()
+    return sorted(set(re.findall(r"NEGF_API\s+[a-z_ ]+\**\s*(negf_[a-z_]+)\s*\(", txt)))
+
+
+def test_header_declarations_match_binding_list():
+    assert declared_symbols() == sorted(capi.EXPORTED_SYMBOLS)
+
+
+def test_library_exports_every_declared_symbol():
+    capi.load()
+    out = subprocess.run(["nm", "-D", "--defined-only", capi.library_path()], capture_output=True, text=True,
+                         check=True).stdout
+    exported = set(re.findall(r"\bT\s+(negf_\w+)", out))
+    missing = [s for s in declared_symbols() if s not in exported]
+    assert not missing, missing
+    lib = ctypes.CDLL(capi.library_path())
+    for s in declared_symbols():
+        assert hasattr(lib, s)
+
+
+def test_struct_layout_matches_header():
+    src = r"""
+#include <stdio.h>
+#include <stddef.h>
+#include "negf.h"
+int main(void) {
+  printf("%zu %zu %zu %zu %zu %zu %zu\n", sizeof(negf_params), offsetof(negf_params, eta),
+         offsetof(negf_params, spin_ops), offsetof(negf_params, keep_g_columns), sizeof(negf_request),
+         sizeof(negf_result), offsetof(negf_result, status));
+  return 0;
+}
+"""
+    with tempfile.TemporaryDirectory() as d:
+        c = os.path.join(d, "t.c")
+        exe = os.path.join(d, "t")
+        open(c, "w").write(src)
+        subprocess.run(["gcc", "-I", os.path.join(REPO, "include"), c, "-o", exe], check=True)
+        vals = [int(v) for v in subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()]
+    want = [ctypes.sizeof(capi.NegfParams), capi.NegfParams.eta.offset, capi.NegfParams.spin_ops.offset,
+            capi.NegfParams.keep_g_columns.offset, ctypes.sizeof(capi.NegfRequest), ctypes.sizeof(capi.NegfResult),
+            capi.NegfResult.status.offset]
+    assert vals == want
+
+
+def test_strerror_covers_codes():
+    capi.load()
+    for code in range(-11, 1):
+        assert capi.strerror(code) not in ("", "unknown error")
+    assert "pivot" in capi.strerror(3)
+
+
+@pytest.mark.skipif(gpu_available(), reason="checks the no-device path")
+def test_no_device_fails_loudly():
+    from nonequilibriumgreensfunction_gb300 import Solver
+    with pytest.raises(capi.NegfError) as ei:
+        Solver(4, 3, 3)
+    assert ei.value.code == capi.NEGF_ENODEV
+
+
+def test_c_driver_compiles_against_header():
+    """The reference-side caller: a C translation of Energy_Sweep's call sequence
+    compiles and links against the library (it is run on the GPU by the gpu tests)."""
+    drv = os.path.join(REPO, "nonequilibriumgreensfunction_gb300", "fortran", "energy_sweep_driver.c")
+    with tempfile.TemporaryDirectory() as d:
+        exe = os.path.join(d, "drv")
+        subprocess.run(["gcc", "-O1", "-I", os.path.join(REPO, "include"), drv, "-o", exe,
+                        "-L", os.path.dirname(capi.library_path()), "-lnegf_gb300", "-lm"], check=True)

@@ -1,0 +1,168 @@
+"""Pinning the CPU oracle (no GPU): the reference publishes no test vectors and cannot be
+built here, so the oracle is checked against a dense inverse of the full block-tridiagonal
+matrix and against physics invariants, and the committed golden vectors are checked to be
+the oracle's own output."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+from oracle import negf_oracle as O
+from nonequilibriumgreensfunction_gb300 import hamiltonian as HB
+
+
+def _wire(npx=5, npy=3, npz=2, **kw):
+    return HB.ti_wire(npx, npy, npz, **kw)
+
+
+@pytest.mark.parametrize("energy", [-0.2, 0.0, 0.13, 0.4])
+@pytest.mark.parametrize("basis", ["tau_sigma", "reference"])
+def test_rgf_columns_equal_dense_inverse(energy, basis):
+    htotd, hopx = _wire(basis=basis, W=0.2, seed=7, flux=0.3, zeeman=0.02)
+    opt = O.SolveOptions(eta=1e-4)
+    r = O.energy_sweep(htotd, hopx, energy, (0.05, -0.05), 1e-3, 3, 2, opt, keep_blocks=True)
+    g = O.dense_retarded_greens(htotd, hopx, r["SigmaL"], r["SigmaR"], energy, opt.eta)
+    m = htotd.shape[1]
+    npx = htotd.shape[0]
+    scale = np.abs(g).max()
+    for x in range(npx):
+        assert np.abs(g[x * m:(x + 1) * m, :m] - r["GRLef"][x]).max() < 1e-11 * scale
+        assert np.abs(g[x * m:(x + 1) * m, -m:] - r["GRRgt"][x]).max() < 1e-11 * scale
+        assert np.abs(g[x * m:(x + 1) * m, x * m:(x + 1) * m] - r["GRd"][x]).max() < 1e-11 * scale
+
+
+def test_transmission_reciprocity_and_sum_rule():
+    htotd, hopx = _wire(W=0.3, seed=2, zeeman=0.01)
+    opt = O.SolveOptions(eta=1e-5, sr_tol=1e-10)
+    e = 0.11
+    r = O.energy_sweep(htotd, hopx, e, (0.1, -0.1), 1e-3, 3, 2, opt, keep_blocks=True, calc_currents=True)
+    g = O.dense_retarded_greens(htotd, hopx, r["SigmaL"], r["SigmaR"], e, opt.eta)
+    m = htotd.shape[1]
+    g1n, gn1 = g[:m, -m:], g[-m:, :m]
+    t_lr = np.real(np.trace(r["GammaL"] @ g1n @ r["GammaR"] @ g1n.conj().T))
+    t_rl = np.real(np.trace(r["GammaR"] @ gn1 @ r["GammaL"] @ gn1.conj().T))
+    assert abs(t_lr - r["T12"]) < 1e-12 * max(1.0, abs(t_lr))
+    # L <-> R reciprocity holds up to the eta-broadening of the device
+    assert abs(t_lr - t_rl) < 1e-6
+    # sum rule i(G - G^H) = G (Gamma_L + Gamma_R + 2 eta) G^H on every diagonal block
+    a_full = 1j * (g - g.conj().T)
+    gam = np.zeros_like(g)
+    gam[:m, :m] = r["GammaL"]
+    gam[-m:, -m:] = r["GammaR"]
+    rhs = g @ (gam + 2 * opt.eta * np.eye(g.shape[0])) @ g.conj().T
+    assert np.abs(a_full - rhs).max() < 1e-9 * np.abs(a_full).max()
+    # and Gn + Gp of the reference equals the contact part of the spectral function
+    contact = g @ gam @ g.conj().T
+    for x in range(htotd.shape[0]):
+        blk = slice(x * m, (x + 1) * m)
+        assert np.abs(r["Gnd"][x] + r["Gpd"][x] - contact[blk, blk]).max() < 1e-10 * np.abs(contact).max()
+
+
+def test_clean_wire_has_integer_transmission():
+    htotd, hopx = _wire(npx=6, npy=3, npz=3)
+    opt = O.SolveOptions(eta=1e-7, sr_tol=1e-12)
+    for e in (0.05, 0.25, 0.45):
+        r = O.energy_sweep(htotd, hopx, e, (0.0, 0.0), 1e-3, 3, 3, opt)
+        assert abs(r["T12"] - round(r["T12"])) < 1e-3, (e, r["T12"])
+        assert abs(r["Modec1"] - r["Modec2"]) < 1e-3
+
+
+def test_self_energy_satisfies_surface_dyson_equation():
+    # Sigma_L = H^H (alpha - Sigma_L)^-1 H, Sigma_R = H (alpha - Sigma_R)^-1 H^H, alpha = (E + i eta) - H_1.
+    # The reference seeds the decimation with inv(alpha + i eta) (an extra i eta,
+    # Contact_Self_Energy.F90:187) while the final g uses alpha, so the equation holds up to
+    # O(eta): the residual must shrink in proportion to eta.
+    htotd, hopx = _wire(npx=3, W=0.0)
+    m = htotd.shape[1]
+    for e in (-0.1, 0.2):
+        rel = []
+        for eta in (1e-5, 1e-7):
+            opt = O.SolveOptions(eta=eta, sr_tol=1e-13)
+            cse = O.contact_self_energy(htotd, hopx, e, opt)
+            alpha = complex(e, eta) * np.eye(m) - htotd[0]
+            sl, sr = cse["SigmaL"], cse["SigmaR"]
+            res_l = sl - hopx.conj().T @ np.linalg.inv(alpha - sl) @ hopx
+            res_r = sr - hopx @ np.linalg.inv(alpha - sr) @ hopx.conj().T
+            r = max(np.abs(res_l).max() / np.abs(sl).max(), np.abs(res_r).max() / np.abs(sr).max())
+            assert r < 20 * eta, (e, eta, r)
+            rel.append(r)
+            for gam in (cse["GammaL"], cse["GammaR"]):   # Hermitian, positive semi-definite
+                assert np.abs(gam - gam.conj().T).max() < 1e-12
+                assert np.linalg.eigvalsh(gam).min() > -1e-9
+        assert rel[1] < rel[0] / 20
+
+
+def test_gauge_and_basis_invariance():
+    # T and density do not depend on the Dirac basis choice (tau_sigma vs the reference's)
+    kw = dict(npx=4, npy=3, npz=2, M0=0.3, B=0.25, A=0.5)
+    h1, x1 = HB.ti_wire(**kw, basis="tau_sigma")
+    opt = O.SolveOptions(eta=1e-5, sr_tol=1e-11)
+    r1 = O.energy_sweep(h1, x1, 0.07, (0.1, -0.1), 1e-3, 3, 2, opt)
+    # a unitary site rotation U: H -> U H U^H on every site leaves T and site density invariant
+    rng = np.random.default_rng(5)
+    q, _ = np.linalg.qr(rng.standard_normal((4, 4)) + 1j * rng.standard_normal((4, 4)))
+    u = np.kron(np.eye(h1.shape[1] // 4), q)
+    h2 = np.einsum("ij,xjk,lk->xil", u, h1, u.conj())
+    x2 = u @ x1 @ u.conj().T
+    r2 = O.energy_sweep(h2, x2, 0.07, (0.1, -0.1), 1e-3, 3, 2, opt)
+    assert abs(r1["T12"] - r2["T12"]) < 1e-9
+    assert np.abs(r1["RhoN"] - r2["RhoN"]).max() < 1e-9 * np.abs(r1["RhoN"]).max()
+
+
+def test_reference_builder_matches_package_builder():
+    # oracle's literal Build_Hamiltonian restatement == the package's builder in the reference basis
+    dis = HB.disorder_potential(5, 3, 4, 0.2, 11)
+    h_o, x_o = O.build_hamiltonian_reference(5, 3, 4, ab_phi=0.35, disorder=dis)
+    h_p, x_p = HB.ti_wire(5, 3, 4, basis="reference", flux=0.35, disorder=dis)
+    assert np.abs(h_o - h_p).max() < 1e-15
+    assert np.abs(x_o - x_p).max() == 0.0
+    # and with the tau_sigma blocks passed explicitly
+    onsite, hx, hy, hz = HB.site_blocks(0.3, 0.25, 0.5, 0.01)
+    h_o, x_o = O.build_hamiltonian_reference(4, 2, 3, ab_phi=0.5, onsite_blocks=onsite, hops=(hx, hy, hz))
+    h_p, x_p = HB.ti_wire(4, 2, 3, zeeman=0.01, flux=0.5)
+    assert np.abs(h_o - h_p).max() < 1e-15
+    assert np.abs(x_o - x_p).max() == 0.0
+
+
+def test_hamiltonian_is_hermitian_and_leads_match_end_slices():
+    h, x = HB.ti_wire(6, 3, 3, W=0.2, seed=4, flux=0.5, zeeman=0.01)
+    for s in h:
+        assert np.abs(s - s.conj().T).max() < 1e-15
+    assert np.array_equal(h[0], h[-1])      # disorder only on slices 2..npx-1
+    assert not np.array_equal(h[1], h[0])
+
+
+def test_sancho_rubio_iteration_cap_and_quirks():
+    htotd, hopx = _wire(npx=3)
+    opt = O.SolveOptions(eta=1e-5, sr_tol=1e-10, sr_max_iter=1)
+    cse = O.contact_self_energy(htotd, hopx, 0.1, opt)
+    assert list(cse["sr_iters"]) == [1, 1]
+
+
+def test_energy_weights_follow_energy_sweep():
+    eaxis, de0 = O.energy_axis_reference((-0.1, 0.0), 0.0, 600)
+    w = O.energy_weights(eaxis, de0)
+    assert np.allclose(w[:-1], np.diff(eaxis))
+    assert w[-1] == w[-2]
+
+
+@pytest.mark.parametrize("case", ["ref_debug", "flux_zeeman", "c1"])
+def test_golden_vectors_are_oracle_output(case):
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("make_golden", os.path.join(GOLDEN, "make_golden.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    g = np.load(os.path.join(GOLDEN, case + ".npz"))
+    c = mg.CASES[case]
+    htotd, hopx = mg.build_inputs(case)
+    assert str(g["h_sha256"]) == mg.h_digest(htotd, hopx)
+    opt = O.SolveOptions(eta=c["eta"], sr_tol=c["sr_tol"], kT=c["kT"], calc_spin=c["calc_spin"])
+    idx = [0, len(c["energies"]) - 1]
+    for i in idx:
+        r = O.energy_sweep(htotd, hopx, float(c["energies"][i]), c["mu_lead"], c["dE"], c["npy"], c["npz"], opt)
+        assert abs(r["T12"] - g["T12"][i]) <= 1e-12 * max(1.0, abs(g["T12"][i]))
+        assert abs(r["EDensity"] - g["EDensity"][i]) <= 1e-12 * max(1.0, abs(g["EDensity"][i]))
+    p = json.loads(str(g["params"]))
+    assert p["npx"] == c["npx"]
