@@ -115,8 +115,8 @@ class Solver:
         if hf.shape != (self.npx, self.M, self.M):
             raise ValueError("htotd must be (npx, M, M) = %s" % ((self.npx, self.M, self.M),))
         xf = None if hopx is None else np.asfortranarray(np.asarray(hopx, dtype=np.complex128))
-        check(self.lib.negf_set_hamiltonian(self._h, slot, _ptr(hf.view(np.float64)),
-                                            None if xf is None else _ptr(xf.view(np.float64))),
+        check(self.lib.negf_set_hamiltonian(self._h, slot, _ptr(hf),
+                                            None if xf is None else _ptr(xf)),
               "negf_set_hamiltonian")
 
     def set_hamiltonian_fortran(self, htotd_f, hopx_f=None, slot=0):
@@ -128,8 +128,8 @@ class Solver:
             raise ValueError("htotd_f must be contiguous complex128 with npx*M*M elements")
         if hopx_f is not None and (hopx_f.dtype != np.complex128 or not hopx_f.flags.f_contiguous):
             raise ValueError("hopx_f must be Fortran-ordered complex128")
-        check(self.lib.negf_set_hamiltonian(self._h, slot, _ptr(htotd_f.view(np.float64)),
-                                            None if hopx_f is None else _ptr(hopx_f.view(np.float64))),
+        check(self.lib.negf_set_hamiltonian(self._h, slot, _ptr(htotd_f),
+                                            None if hopx_f is None else _ptr(hopx_f)),
               "negf_set_hamiltonian")
 
     # -- the reference's four subroutines --------------------------------------------
@@ -138,7 +138,7 @@ class Solver:
         mats = [np.zeros((m, m), dtype=np.complex128, order="F") for _ in range(4)] if want_matrices else [None] * 4
         dosc = np.zeros(2)
         st = check(self.lib.negf_contact_self_energy(
-            self._h, float(energy), *[None if a is None else _ptr(a.view(np.float64)) for a in mats],
+            self._h, float(energy), *[None if a is None else _ptr(a) for a in mats],
             _ptr(dosc)), "negf_contact_self_energy")
         out = dict(dosc=dosc, status=st)
         if want_matrices:
@@ -153,7 +153,7 @@ class Solver:
         ntot = self.npx * self.M
         a = np.zeros((ntot, self.M), dtype=np.complex128, order="F")
         b = np.zeros((ntot, self.M), dtype=np.complex128, order="F")
-        check(self.lib.negf_copy_g_columns(self._h, _ptr(a.view(np.float64)), _ptr(b.view(np.float64))),
+        check(self.lib.negf_copy_g_columns(self._h, _ptr(a), _ptr(b)),
               "negf_copy_g_columns")
         return a.reshape(self.npx, self.M, self.M), b.reshape(self.npx, self.M, self.M)
 

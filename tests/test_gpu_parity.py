@@ -238,3 +238,43 @@ def test_bad_arguments_are_rejected(need_gpu):
         assert ei.value.code == capi.NEGF_ENOHAM
         with pytest.raises(capi.NegfError):
             s.get_retarded_greens()                    # before contact_self_energy
+
+
+def test_c_driver_energy_loop_matches_oracle(need_gpu, tmp_path):
+    """A C caller making Energy_Sweep's calls in the reference's order (the sequence the
+    Fortran ISO_C_BINDING shim makes), on arrays in the reference's memory layout."""
+    import subprocess
+    from conftest import REPO
+    npx, npy, npz = 4, 3, 3
+    htotd, hopx = HB.ti_wire(npx, npy, npz, basis="reference", W=0.05, seed=2)
+    m = htotd.shape[1]
+    hf = np.ascontiguousarray(htotd.transpose(0, 2, 1))       # Htotd(M, M, npx) memory
+    xf = np.asfortranarray(hopx)
+    (tmp_path / "h.bin").write_bytes(hf.tobytes())
+    (tmp_path / "x.bin").write_bytes(xf.tobytes(order="F"))
+    libdir = os.path.dirname(capi.library_path())
+    exe = str(tmp_path / "drv")
+    subprocess.run(["gcc", "-O1", "-I", os.path.join(REPO, "include"),
+                    os.path.join(REPO, "nonequilibriumgreensfunction_gb300", "fortran", "energy_sweep_driver.c"),
+                    "-o", exe, "-L", libdir, "-lnegf_gb300", "-Wl,-rpath," + libdir], check=True)
+    mu1, mu2, n_e = 0.1, 0.0, 12
+    e_min, e_max = -1e-10, 0.1 + 1e-10
+    out = tmp_path / "out.bin"
+    subprocess.run([exe, str(npx), str(npy), str(npz), str(tmp_path / "h.bin"), str(tmp_path / "x.bin"),
+                    "1e-4", "1e-8", repr(mu1), repr(mu2), str(n_e), repr(e_min), repr(e_max), str(out)], check=True)
+    vals = np.fromfile(out, dtype=np.float64)
+    nsites = npx * npy * npz
+    per_e = vals[:7 * n_e].reshape(n_e, 7)
+    rhon = vals[7 * n_e:7 * n_e + nsites].reshape((npx, npy, npz), order="F")
+    opt = O.SolveOptions(eta=1e-4, sr_tol=1e-8)
+    eaxis = e_min + (e_max - e_min) / (n_e - 1) * np.arange(n_e)
+    w = O.energy_weights(eaxis, (e_max - e_min) / (n_e - 1))
+    want_rn = np.zeros((npx, npy, npz))
+    for k, e in enumerate(eaxis):
+        ref = O.energy_sweep(htotd, hopx, float(e), (mu1, mu2), w[k], npy, npz, opt)
+        got = dict(zip(["T12", "EDensity", "HDensity", "Modec1", "Modec2"], per_e[k, :5]))
+        for key, v in got.items():
+            assert_close(v, ref[key], "%s[%d]" % (key, k), floor=1e-6)
+        assert_close(per_e[k, 5:7], ref["dosc"], "dosc[%d]" % k)
+        want_rn += ref["RhoN"]
+    assert_close(rhon, want_rn, "RhoN")
