@@ -174,7 +174,10 @@ typedef struct negf_result {
 } negf_result;
 
 /* RhoN, RhoP, SigX/Y/Z (may be NULL) are npx x npy x npz x n_hamiltonians arrays
- * (slot slowest) that the requests' dE-weighted densities are ADDED to.                 */
+ * (slot slowest) that the requests' dE-weighted densities are ADDED to.  The call
+ * returns < 0 only for call-level failures (arguments, CUDA); the outcome of each
+ * request (INFO > 0, NEGF_ESR_NOCONV, NEGF_ENAN) is in res[i].status, and the batch
+ * continues past failed requests as the reference's energy loop does.                  */
 NEGF_API int negf_solve_batch(negf_handle* h, const negf_request* req, int32_t n, negf_result* res,
                      double* RhoN, double* RhoP, double* SigX, double* SigY, double* SigZ);
 

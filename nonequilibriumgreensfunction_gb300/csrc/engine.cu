@@ -577,7 +577,7 @@ int Engine::batch_solve(const negf_request* req, int n, negf_result* res, double
       if (stv == 0) stv = rst[i];
       o.status = stv;
       o.sr_iters = std::max(sr_iters[it.sr_l], sr_iters[S + it.sr_r]);
-      if (stv != 0 && first_err == 0) first_err = stv;
+      (void)first_err;
     }
   }
   // add the slot-resolved site sums into the caller's arrays
@@ -591,7 +591,7 @@ int Engine::batch_solve(const negf_request* req, int n, negf_result* res, double
     for (int s = 0; s < nslots; ++s)
       for (long long i = 0; i < total; ++i) outs[f][(size_t)s * total + i] += hPin_[((size_t)s * 5 + f) * total + i];
   }
-  return first_err;
+  return NEGF_OK;   // per-request failures are reported in res[i].status
 }
 
 }  // namespace negf
