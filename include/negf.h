@@ -101,6 +101,11 @@ typedef struct negf_stats {
     double  gemm_flops;      /* their real flops, 8*m*n*k per complex GEMM                 */
     int64_t panel_launches;  /* Gauss-Jordan panel factorisations                          */
     double  panel_ms;
+    int64_t tc_launches;     /* tcgen05 sliced-BF16 GEMM launches (mixed form)             */
+    double  tc_ms;
+    double  tc_flops;        /* complex-equivalent flops 8*m*n*k of those GEMMs            */
+    int64_t fallbacks;       /* mixed form: inverses redone in FP64 (residual too large)   */
+    double  ns_residual_max; /* mixed form: largest accepted first Newton-Schulz residual  */
 } negf_stats;
 NEGF_API int negf_profile(negf_handle* h, int enable);
 NEGF_API int negf_get_stats(negf_handle* h, negf_stats* out);
@@ -180,6 +185,25 @@ typedef struct negf_result {
  * continues past failed requests as the reference's energy loop does.                  */
 NEGF_API int negf_solve_batch(negf_handle* h, const negf_request* req, int32_t n, negf_result* res,
                      double* RhoN, double* RhoP, double* SigX, double* SigY, double* SigZ);
+
+/* ---- stateless dense kernels -------------------------------------------------------
+ * Drop-ins for the reference's dense calls on host arrays (column-major, interleaved
+ * complex), run on the current CUDA device; `batch` matrices are consecutive in memory
+ * (A at stride lda*k, B at ldb*n, C at ldc*n, G at n*n).                               */
+
+/* zgemm('N','N', m, n, k, alpha, A, lda, B, ldb, beta, C, ldc) as called throughout
+ * Source/Recursive_Greens.F90 and Source/Contact_Self_Energy.F90.  slices = 0 runs the
+ * FP64 DFMA kernel; slices in {3, 4, 5, 7} runs the tcgen05 tensor-core kernel on exact
+ * 7-bit integer BF16 slices of row/column-scaled operands (truncation <= 2^(-7*slices)
+ * of max|A_i.| max|B_.j| per term; 7 slices is FP64-class).  NEGF_ETIMEDOUT if a
+ * bounded device wait expired.                                                          */
+NEGF_API int negf_zgemm(int32_t slices, int32_t m, int32_t n, int32_t k, const double* alpha,
+                        const double* A, int32_t lda, const double* B, int32_t ldb,
+                        const double* beta, double* C, int32_t ldc, int32_t batch);
+
+/* Invert_Matrix(invG, G, N, errorFlag) (Source/MKL_Routines_Cluster.F90:2-33): returns
+ * the LAPACK INFO of the first singular matrix, 0 if all are invertible.               */
+NEGF_API int negf_zinv(int32_t n, const double* G, double* invG, int32_t batch);
 
 #ifdef __cplusplus
 }

@@ -34,7 +34,7 @@ EXPORTED_SYMBOLS = (
     "negf_set_stream", "negf_profile", "negf_get_stats",
     "negf_set_hamiltonian", "negf_contact_self_energy", "negf_get_retarded_greens",
     "negf_copy_g_columns", "negf_calculate_gnp", "negf_calculate_observables",
-    "negf_solve_batch",
+    "negf_solve_batch", "negf_zgemm", "negf_zinv",
 )
 
 
@@ -63,7 +63,9 @@ class NegfResult(ctypes.Structure):
 
 class NegfStats(ctypes.Structure):
     _fields_ = [("launches", c_int64), ("gemm_launches", c_int64), ("gemm_ms", c_double),
-                ("gemm_flops", c_double), ("panel_launches", c_int64), ("panel_ms", c_double)]
+                ("gemm_flops", c_double), ("panel_launches", c_int64), ("panel_ms", c_double),
+                ("tc_launches", c_int64), ("tc_ms", c_double), ("tc_flops", c_double),
+                ("fallbacks", c_int64), ("ns_residual_max", c_double)]
 
 
 class NegfError(RuntimeError):
@@ -93,6 +95,9 @@ def _declare(lib):
         "negf_calculate_gnp": (c_int, [h, c_double, c_double, c_double, _dp, _dp]),
         "negf_calculate_observables": (c_int, [h, c_double, c_double, c_double, _dp, _dp, _dp, _dp,
                                                _dp, _dp, _dp, _dp]),
+        "negf_zgemm": (c_int, [c_int32, c_int32, c_int32, c_int32, _dp, _dp, c_int32, _dp, c_int32, _dp, _dp,
+                               c_int32, c_int32]),
+        "negf_zinv": (c_int, [c_int32, _dp, _dp, c_int32]),
         "negf_solve_batch": (c_int, [h, POINTER(NegfRequest), c_int32, POINTER(NegfResult),
                                      _dp, _dp, _dp, _dp, _dp]),
     }
@@ -132,3 +137,52 @@ def check(code: int, where: str) -> int:
     if code < 0:
         raise NegfError(code, where)
     return code
+
+
+def _p(a):
+    import numpy as np  # noqa: F401
+    return a.ctypes.data_as(_dp)
+
+
+def zgemm(A, B, C=None, alpha=1.0, beta=0.0, slices=0):
+    """C = alpha A B + beta C on the GPU for batches of complex matrices.
+
+    A: (batch, m, k) or (m, k); B: (batch, k, n) or (k, n).  slices = 0 uses the FP64
+    DFMA kernel, slices in {3, 4, 5, 7} the tcgen05 sliced-BF16 kernel."""
+    import numpy as np
+    lib = load()
+    A = np.asarray(A, dtype=np.complex128)
+    B = np.asarray(B, dtype=np.complex128)
+    squeeze = A.ndim == 2
+    if squeeze:
+        A, B = A[None], B[None]
+    batch, m, k = A.shape
+    n = B.shape[2]
+    af = np.ascontiguousarray(A.transpose(0, 2, 1))     # column-major blocks
+    bf = np.ascontiguousarray(B.transpose(0, 2, 1))
+    if C is None:
+        cf = np.zeros((batch, n, m), dtype=np.complex128)
+    else:
+        Cc = np.asarray(C, dtype=np.complex128)
+        cf = np.ascontiguousarray((Cc[None] if squeeze else Cc).transpose(0, 2, 1))
+    al = np.array([complex(alpha).real, complex(alpha).imag])
+    be = np.array([complex(beta).real, complex(beta).imag])
+    check(lib.negf_zgemm(slices, m, n, k, _p(al), _p(af), m, _p(bf), k, _p(be), _p(cf), m, batch), "negf_zgemm")
+    out = cf.transpose(0, 2, 1)
+    return out[0] if squeeze else out
+
+
+def zinv(G):
+    """Batched inverse (Invert_Matrix); returns (inverse, info)."""
+    import numpy as np
+    lib = load()
+    G = np.asarray(G, dtype=np.complex128)
+    squeeze = G.ndim == 2
+    if squeeze:
+        G = G[None]
+    batch, n, _ = G.shape
+    gf = np.ascontiguousarray(G.transpose(0, 2, 1))
+    out = np.zeros_like(gf)
+    info = check(lib.negf_zinv(n, _p(gf), _p(out), batch), "negf_zinv")
+    inv = out.transpose(0, 2, 1)
+    return (inv[0] if squeeze else inv), info

@@ -145,6 +145,8 @@ int negf_profile(negf_handle* h, int enable) {
   I.launches = 0;
   for (int k = 0; k < negf::TK_COUNT; ++k) { I.kind_launches[k] = 0; I.kind_flops[k] = 0; I.kind_ms[k] = 0; }
   I.timing = enable != 0;
+  h->eng.fallbacks_ = 0;
+  h->eng.last_rnorm_max_ = 0.0;
   return NEGF_OK;
 }
 
@@ -159,6 +161,11 @@ int negf_get_stats(negf_handle* h, negf_stats* out) {
   out->gemm_flops = I.kind_flops[negf::TK_GEMM];
   out->panel_launches = I.kind_launches[negf::TK_PANEL];
   out->panel_ms = I.kind_ms[negf::TK_PANEL];
+  out->tc_launches = I.kind_launches[negf::TK_TC];
+  out->tc_ms = I.kind_ms[negf::TK_TC];
+  out->tc_flops = I.kind_flops[negf::TK_TC];
+  out->fallbacks = h->eng.fallbacks_;
+  out->ns_residual_max = h->eng.last_rnorm_max_;
   return NEGF_OK;
 }
 

@@ -61,6 +61,12 @@ void dfree(T*& p) {
 
 bool blocks_equal(const double2* a, const double2* b, size_t n) { return std::memcmp(a, b, n * sizeof(double2)) == 0; }
 
+double __longlong_as_double_host(unsigned long long v) {
+  double d;
+  std::memcpy(&d, &v, sizeof(d));
+  return d;
+}
+
 }  // namespace
 
 int merge_info_kernel_launch(int batch, const int* info, int* status, cudaStream_t st) {
@@ -80,6 +86,8 @@ Engine::~Engine() {
   dfree(dSr_); dfree(dSrSigL_); dfree(dSrSigR_); dfree(dSrGamL_); dfree(dSrGamR_);
   dfree(dSrCmax_); dfree(dSrDos_); dfree(dSrActive_); dfree(dSrE_); dfree(dSrHend_); dfree(dSrStatus_);
   inv_work_free(inv_);
+  dfree(dWinv_); dfree(dW32_); dfree(dT_); dfree(sa_.data); dfree(sb_.data); dfree(sa_.exps); dfree(sb_.exps);
+  dfree(dRnorm_); dfree(dTcErr_);
   if (hPin_) cudaFreeHost(hPin_);
   if (own_st_) cudaStreamDestroy(own_st_);
 }
@@ -88,7 +96,10 @@ int Engine::init(const negf_params& p) {
   if (p.npx < 2 || p.npy < 1 || p.npz < 1 || p.norb < 1 || p.norb > 4) return NEGF_EINVAL;
   if (p.n_hamiltonians < 1 || p.max_batch < 1 || p.max_batch > 4096) return NEGF_EINVAL;
   if (!(p.eta >= 0.0) || !(p.sr_tol > 0.0) || p.sr_max_iter < 1) return NEGF_EINVAL;
-  if (p.precision != NEGF_PREC_FP64) return NEGF_EINVAL;
+  if (p.precision != NEGF_PREC_FP64 && p.precision != NEGF_PREC_MIXED) return NEGF_EINVAL;
+  if (p.precision == NEGF_PREC_MIXED && p.mixed_slices != 0 && !tc_supported_slices(p.mixed_slices))
+    return NEGF_EINVAL;
+  if (p.precision == NEGF_PREC_MIXED && 2 * p.norb * p.npy * p.npz >= 4096) return NEGF_EINVAL;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return NEGF_ENODEV;
   if (p.device < 0 || p.device >= ndev) return NEGF_EINVAL;
@@ -99,6 +110,8 @@ int Engine::init(const negf_params& p) {
   B_ = p.max_batch;
   S_ = 2 * p.max_batch;
   keep_columns_ = p.keep_g_columns != 0;
+  mixed_ = p.precision == NEGF_PREC_MIXED;
+  if (mixed_ && p.mixed_slices != 0) s_rgf_ = p.mixed_slices;
   NEGF_CUDA_TRY(cudaSetDevice(p.device));
   NEGF_CUDA_TRY(cudaStreamCreateWithFlags(&own_st_, cudaStreamNonBlocking));
   st_ = own_st_;
@@ -143,6 +156,21 @@ int Engine::alloc() {
   NEGF_TRY(dalloc(&dSrHend_, (size_t)S_, bytes_));
   NEGF_TRY(dalloc(&dSrStatus_, (size_t)S_, bytes_));
   NEGF_TRY(inv_work_alloc(inv_, M_, std::max(B_, S_)));
+  if (mixed_) {
+    const int cap = std::max(B_, S_);
+    const int smax = 7;
+    NEGF_TRY(dalloc(&dWinv_, (size_t)(cap * MM_), bytes_));
+    NEGF_TRY(dalloc(&dW32_, (size_t)(cap * MM_), bytes_));
+    NEGF_TRY(dalloc(&dT_, (size_t)(cap * MM_), bytes_));
+    const int kp = padded_k(M_);
+    NEGF_TRY(dalloc(reinterpret_cast<char**>(&sa_.data), sliced_bytes(M_, kp, smax, cap), bytes_));
+    NEGF_TRY(dalloc(reinterpret_cast<char**>(&sb_.data), sliced_bytes(2 * M_, kp, smax, cap), bytes_));
+    NEGF_TRY(dalloc(&sa_.exps, (size_t)cap * M_, bytes_));
+    NEGF_TRY(dalloc(&sb_.exps, (size_t)cap * M_, bytes_));
+    NEGF_TRY(dalloc(&dRnorm_, (size_t)cap, bytes_));
+    NEGF_TRY(dalloc(&dTcErr_, (size_t)1, bytes_));
+    NEGF_CUDA_TRY(cudaMemset(dTcErr_, 0, sizeof(int)));
+  }
   hPinBytes_ = sizeof(double) * (size_t)std::max<long long>(
                    {(long long)B_ * sums_blocks_ * 2, (long long)B_ * 4, 4LL * S_,
                     (long long)p_.n_hamiltonians * 5 * total, 5LL * total, 64});
@@ -235,8 +263,17 @@ void Engine::recompute_lead_classes() {
   }
 }
 
+int Engine::gemm_tc_nn(int batch, const double2* A, long long sA, const double2* B, long long sB, double2* C,
+                       long long sC, double2 alpha, double2 beta, int slices) {
+  NEGF_TRY(slice_a(A, M_, sA, M_, M_, batch, slices, sa_, st_));
+  NEGF_TRY(slice_b(B, M_, sB, M_, M_, batch, slices, sb_, st_));
+  return zgemm_tc(sa_, sb_, alpha, beta, C, M_, sC, dTcErr_, st_);
+}
+
 int Engine::gemm(int batch, Op opA, const double2* A, long long sA, Op opB, const double2* B, long long sB, double2* C,
                  long long sC, double2 alpha, double2 beta) {
+  if (mixed_ && opA == OP_N && opB == OP_N && sA != 0 && sB != 0)
+    return gemm_tc_nn(batch, A, sA, B, sB, C, sC, alpha, beta, cur_slices_);
   GemmBatch g{};
   g.m = M_; g.n = M_; g.k = M_;
   g.alpha = alpha; g.beta = beta;
@@ -255,6 +292,58 @@ int Engine::hop_mul(int left, Op op, const double2* X, long long sX, double2* Y,
 }
 
 int Engine::merge_info(int batch) { return merge_info_kernel_launch(batch, inv_.info, dStatus_, st_); }
+
+// In-place inverse of `batch` matrices at stride sA; INFO of singular ones merged into
+// status_dev.  FP64 form: blocked Gauss-Jordan.  Mixed form: FP32 Gauss-Jordan, then
+// ns_steps_ Newton-Schulz steps X <- X + X (I - W X) with W X formed at s_res_ slices
+// (FP64-class) and X R at s_upd_ slices; a matrix whose first residual norm is above
+// ns_accept_ (or whose FP32 factorisation met a zero pivot) is inverted again in FP64.
+int Engine::invert(double2* A, long long sA, int batch, int* status_dev) {
+  if (!mixed_) {
+    NEGF_TRY(zinv_f64(A, sA, M_, batch, inv_, st_));
+    return merge_info_kernel_launch(batch, inv_.info, status_dev, st_);
+  }
+  const double2 one = make_double2(1, 0), zero = make_double2(0, 0);
+  NEGF_TRY(copy_blocks(M_, batch, A, sA, dWinv_, MM_, st_));
+  NEGF_TRY(to_f32(M_, batch, A, sA, dW32_, MM_, st_));
+  NEGF_TRY(cinv_f32(dW32_, MM_, M_, batch, inv_, st_));
+  NEGF_TRY(to_f64(M_, batch, dW32_, MM_, A, sA, st_));
+  std::vector<int> info32(batch);
+  NEGF_CUDA_TRY(cudaMemcpyAsync(info32.data(), inv_.info, sizeof(int) * batch, cudaMemcpyDeviceToHost, st_));
+  NEGF_CUDA_TRY(cudaMemsetAsync(dRnorm_, 0, sizeof(unsigned long long) * batch, st_));
+  NEGF_TRY(slice_a(dWinv_, M_, MM_, M_, M_, batch, s_res_, sa_, st_));
+  std::vector<unsigned long long> r0(batch);
+  for (int step = 0; step < ns_steps_; ++step) {
+    if (step > 0) {
+      NEGF_CUDA_TRY(cudaMemsetAsync(dRnorm_, 0, sizeof(unsigned long long) * batch, st_));
+      NEGF_TRY(slice_a(dWinv_, M_, MM_, M_, M_, batch, s_res_, sa_, st_));
+    }
+    NEGF_TRY(slice_b(A, M_, sA, M_, M_, batch, s_res_, sb_, st_));
+    NEGF_TRY(zgemm_tc(sa_, sb_, one, zero, dT_, M_, MM_, dTcErr_, st_));          // T = W X
+    NEGF_TRY(ns_residual(M_, batch, dT_, MM_, dRnorm_, st_));                     // R = I - T
+    if (step == 0)
+      NEGF_CUDA_TRY(cudaMemcpyAsync(r0.data(), dRnorm_, sizeof(unsigned long long) * batch, cudaMemcpyDeviceToHost, st_));
+    NEGF_TRY(slice_a(A, M_, sA, M_, M_, batch, s_upd_, sa_, st_));
+    NEGF_TRY(slice_b(dT_, M_, MM_, M_, M_, batch, s_upd_, sb_, st_));
+    NEGF_TRY(zgemm_tc(sa_, sb_, one, one, A, M_, sA, dTcErr_, st_));              // X += X R
+  }
+  NEGF_CUDA_TRY(cudaStreamSynchronize(st_));
+  double worst = 0.0;
+  for (int b = 0; b < batch; ++b) {
+    const double r = __longlong_as_double_host(r0[b]);
+    if (info32[b] != 0 || !(r <= ns_accept_)) {
+      // FP64 inverse of the saved matrix
+      NEGF_TRY(copy_blocks(M_, 1, dWinv_ + (long long)b * MM_, MM_, A + (long long)b * sA, sA, st_));
+      NEGF_TRY(zinv_f64(A + (long long)b * sA, sA, M_, 1, inv_, st_));
+      NEGF_TRY(merge_info_kernel_launch(1, inv_.info, status_dev + b, st_));
+      ++fallbacks_;
+    } else if (r > worst) {
+      worst = r;
+    }
+  }
+  last_rnorm_max_ = std::max(last_rnorm_max_, worst);
+  return NEGF_OK;
+}
 
 // -------------------------------------------------------------------------------------
 // Sancho-Rubio (Source/Contact_Self_Energy.F90:156-269), batched over problems
@@ -280,10 +369,8 @@ int Engine::solve_sr(const std::vector<SrJob>& jobs, std::vector<int>& status, s
   for (int r = 0; r < kSrBlocks; ++r) role[r] = r;
   auto buf = [&](int r) { return dSr_ + (long long)role[r] * S_ * MM_; };
   const long long sM = MM_;
-  auto inv_merge = [&](double2* A) -> int {
-    NEGF_TRY(zinv_f64(A, sM, M_, S, inv_, st_));
-    return merge_info_kernel_launch(S, inv_.info, dSrStatus_, st_);
-  };
+  auto inv_merge = [&](double2* A) -> int { return invert(A, sM, S, dSrStatus_); };
+  cur_slices_ = s_sr_;
 
   // alpha = (E + i eta) I - H_end (:117-120 / :129-132)
   NEGF_TRY(form_alpha(M_, S, dSrE_, dSrHend_, p_.eta, 0.0, buf(SR_ALPHA), sM, st_));
@@ -421,9 +508,9 @@ int Engine::solve_rgf(const std::vector<Item>& items, bool keep_columns) {
       }
     }
     NEGF_TRY(form_w(fw, st_));
-    NEGF_TRY(zinv_f64(dG_ + (long long)x * MM_, sG, M_, B, inv_, st_));
-    return merge_info(B);
+    return invert(dG_ + (long long)x * MM_, sG, B, dStatus_);
   };
+  cur_slices_ = s_rgf_;
 
   // right-connected sweep gR_x = inv(A_x - H gR_{x+1} H^H), x = N..1 (Recursive_Greens.F90:67-86)
   for (int x = N - 1; x >= 0; --x) NEGF_TRY(form(x, 1, x < N - 1 ? dG_ + (long long)(x + 1) * MM_ : nullptr));
@@ -518,7 +605,6 @@ int Engine::batch_solve(const negf_request* req, int n, negf_result* res, double
     if (!slot_set_[s]) return NEGF_ENOHAM;
   }
   NEGF_CUDA_TRY(cudaMemsetAsync(dAcc_, 0, sizeof(double) * nslots * 5 * total, st_));
-  int first_err = NEGF_OK;
   for (int c0 = 0; c0 < n; c0 += B_) {
     const int nb = std::min(B_, n - c0);
     // Sancho-Rubio problems: one per (energy, lead class), two if H_1 != H_N
@@ -577,7 +663,6 @@ int Engine::batch_solve(const negf_request* req, int n, negf_result* res, double
       if (stv == 0) stv = rst[i];
       o.status = stv;
       o.sr_iters = std::max(sr_iters[it.sr_l], sr_iters[S + it.sr_r]);
-      (void)first_err;
     }
   }
   // add the slot-resolved site sums into the caller's arrays

@@ -6,6 +6,7 @@
 #include <vector>
 
 #include "negf_internal.cuh"
+#include "zgemm_tc.h"
 
 namespace negf {
 
@@ -88,6 +89,26 @@ class Engine {
   size_t hPinBytes_ = 0;
 
   InvWork inv_;
+
+  // mixed form (NEGF_PREC_MIXED): tensor-core GEMMs on S integer BF16 slices, inverses as
+  // FP32 Gauss-Jordan + Newton-Schulz steps with the residual at s_res_ slices
+  bool mixed_ = false;
+  int s_rgf_ = 4;      // RGF block products
+  int s_sr_ = 7;       // Sancho-Rubio products (FP64-class)
+  int s_res_ = 7;      // Newton-Schulz residual W X (FP64-class)
+  int s_upd_ = 4;      // Newton-Schulz update X R (R is small)
+  int ns_steps_ = 2;
+  double ns_accept_ = 0.5;   // first residual norm above this -> FP64 inverse for that matrix
+  int cur_slices_ = 4;       // slices for the GEMMs issued now (set per phase)
+  double2* dWinv_ = nullptr; // copy of the matrix being inverted (FP64)
+  float2* dW32_ = nullptr;
+  double2* dT_ = nullptr;
+  SlicedOperand sa_, sb_;
+  unsigned long long* dRnorm_ = nullptr;
+  int* dTcErr_ = nullptr;
+  long long fallbacks_ = 0;
+  double last_rnorm_max_ = 0.0;
+  int invert(double2* A, long long sA, int batch, int* status_dev);
   HopBD hop() const {
     HopBD h;
     h.hb = dHopBD_;
@@ -113,6 +134,8 @@ class Engine {
   int hop_mul(int left, Op op, const double2* X, long long sX, double2* Y, long long sY, int batch);
   int gemm(int batch, Op opA, const double2* A, long long sA, Op opB, const double2* B, long long sB, double2* C,
            long long sC, double2 alpha, double2 beta);
+  int gemm_tc_nn(int batch, const double2* A, long long sA, const double2* B, long long sB, double2* C, long long sC,
+                 double2 alpha, double2 beta, int slices);
   int merge_info(int batch);
 };
 

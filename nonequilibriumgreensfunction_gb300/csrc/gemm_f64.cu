@@ -15,35 +15,35 @@ namespace {
 
 constexpr int BM = 64, BN = 64, BK = 8, NT = 256;
 
-template <int OP>
-__device__ __forceinline__ double2 opval(double2 v) {
+template <int OP, typename T>
+__device__ __forceinline__ T opval(T v) {
   if (OP == OP_C) return cconj(v);
   return v;
 }
 
 // op(A)(i, k) for column-major A
-template <int OP>
-__device__ __forceinline__ double2 load_a(const double2* __restrict__ A, int lda, int m, int k, int i, int kk) {
-  if (i >= m || kk >= k) return make_double2(0.0, 0.0);
+template <int OP, typename T>
+__device__ __forceinline__ T load_a(const T* __restrict__ A, int lda, int m, int k, int i, int kk) {
+  if (i >= m || kk >= k) return CplxTraits<T>::make(0, 0);
   if (OP == OP_N) return A[(long long)kk * lda + i];
   return opval<OP>(A[(long long)i * lda + kk]);
 }
 // op(B)(kk, j)
-template <int OP>
-__device__ __forceinline__ double2 load_b(const double2* __restrict__ B, int ldb, int n, int k, int kk, int j) {
-  if (j >= n || kk >= k) return make_double2(0.0, 0.0);
+template <int OP, typename T>
+__device__ __forceinline__ T load_b(const T* __restrict__ B, int ldb, int n, int k, int kk, int j) {
+  if (j >= n || kk >= k) return CplxTraits<T>::make(0, 0);
   if (OP == OP_N) return B[(long long)j * ldb + kk];
   return opval<OP>(B[(long long)kk * ldb + j]);
 }
 
-template <int OPA, int OPB>
-__global__ void __launch_bounds__(NT) zgemm_kernel(GemmBatch g) {
-  __shared__ double2 As[2][BK][BM];
-  __shared__ double2 Bs[2][BK][BN];
+template <int OPA, int OPB, typename T>
+__global__ void __launch_bounds__(NT) zgemm_kernel(GemmBatchT<T> g) {
+  __shared__ T As[2][BK][BM];
+  __shared__ T Bs[2][BK][BN];
   const int b = blockIdx.z;
-  const double2* __restrict__ A = g.A + (long long)b * g.sA;
-  const double2* __restrict__ B = g.B + (long long)b * g.sB;
-  double2* __restrict__ C = g.C + (long long)b * g.sC;
+  const T* __restrict__ A = g.A + (long long)b * g.sA;
+  const T* __restrict__ B = g.B + (long long)b * g.sB;
+  T* __restrict__ C = g.C + (long long)b * g.sC;
   const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
   const int t = threadIdx.x;
   const int tx = t & 15, ty = t >> 4;
@@ -59,18 +59,18 @@ __global__ void __launch_bounds__(NT) zgemm_kernel(GemmBatch g) {
     else { bj[r] = e & (BN - 1); bk[r] = e >> 6; }
   }
 
-  double2 acc[4][4];
+  T acc[4][4];
 #pragma unroll
   for (int i = 0; i < 4; ++i)
 #pragma unroll
-    for (int j = 0; j < 4; ++j) acc[i][j] = make_double2(0.0, 0.0);
+    for (int j = 0; j < 4; ++j) acc[i][j] = CplxTraits<T>::make(0, 0);
 
-  double2 ra[2], rb[2];
+  T ra[2], rb[2];
   const int ktiles = (g.k + BK - 1) / BK;
 #pragma unroll
   for (int r = 0; r < 2; ++r) {
-    ra[r] = load_a<OPA>(A, g.lda, g.m, g.k, m0 + ai[r], ak[r]);
-    rb[r] = load_b<OPB>(B, g.ldb, g.n, g.k, bk[r], n0 + bj[r]);
+    ra[r] = load_a<OPA, T>(A, g.lda, g.m, g.k, m0 + ai[r], ak[r]);
+    rb[r] = load_b<OPB, T>(B, g.ldb, g.n, g.k, bk[r], n0 + bj[r]);
   }
 #pragma unroll
   for (int r = 0; r < 2; ++r) {
@@ -86,13 +86,13 @@ __global__ void __launch_bounds__(NT) zgemm_kernel(GemmBatch g) {
       const int k0 = (kt + 1) * BK;
 #pragma unroll
       for (int r = 0; r < 2; ++r) {
-        ra[r] = load_a<OPA>(A, g.lda, g.m, g.k, m0 + ai[r], k0 + ak[r]);
-        rb[r] = load_b<OPB>(B, g.ldb, g.n, g.k, k0 + bk[r], n0 + bj[r]);
+        ra[r] = load_a<OPA, T>(A, g.lda, g.m, g.k, m0 + ai[r], k0 + ak[r]);
+        rb[r] = load_b<OPB, T>(B, g.ldb, g.n, g.k, k0 + bk[r], n0 + bj[r]);
       }
     }
 #pragma unroll
     for (int kk = 0; kk < BK; ++kk) {
-      double2 av[4], bv[4];
+      T av[4], bv[4];
 #pragma unroll
       for (int i = 0; i < 4; ++i) av[i] = As[cur][kk][tx + 16 * i];
 #pragma unroll
@@ -121,18 +121,18 @@ __global__ void __launch_bounds__(NT) zgemm_kernel(GemmBatch g) {
     for (int j = 0; j < 4; ++j) {
       const int col = n0 + ty + 16 * j;
       if (col >= g.n) continue;
-      double2* cp = C + (long long)col * g.ldc + row;
-      double2 v = cmul(g.alpha, acc[i][j]);
+      T* cp = C + (long long)col * g.ldc + row;
+      T v = cmul(g.alpha, acc[i][j]);
       if (!beta0) v = cadd(v, cmul(g.beta, *cp));
       *cp = v;
     }
   }
 }
 
-template <int OPA, int OPB>
-void launch(const GemmBatch& g, cudaStream_t st) {
+template <int OPA, int OPB, typename T>
+void launch(const GemmBatchT<T>& g, cudaStream_t st) {
   dim3 grid((g.m + BM - 1) / BM, (g.n + BN - 1) / BN, g.batch);
-  zgemm_kernel<OPA, OPB><<<grid, NT, 0, st>>>(g);
+  zgemm_kernel<OPA, OPB, T><<<grid, NT, 0, st>>>(g);
 }
 
 }  // namespace
@@ -144,7 +144,7 @@ int zgemm_f64(const GemmBatch& g, cudaStream_t st) {
   if (g.opA == a && g.opB == b) {                                                            \
     cudaEvent_t ev;                                                                          \
     timed_begin(st, TK_GEMM, 8.0 * g.m * g.n * (double)g.k * g.batch, &ev);                  \
-    launch<a, b>(g, st);                                                                     \
+    launch<a, b, double2>(g, st);                                                            \
     NEGF_CUDA_TRY(cudaGetLastError());                                                       \
     timed_end(st, TK_GEMM, ev);                                                              \
     count_launch();                                                                          \
@@ -158,6 +158,19 @@ int zgemm_f64(const GemmBatch& g, cudaStream_t st) {
   NEGF_GEMM_CASE(OP_C, OP_C)
 #undef NEGF_GEMM_CASE
   return NEGF_EINVAL;
+}
+
+}  // namespace negf
+
+namespace negf {
+
+int cgemm_f32(const GemmBatchT<float2>& g, cudaStream_t st) {
+  if (g.m <= 0 || g.n <= 0 || g.batch <= 0) return NEGF_OK;
+  if (g.batch > 65535 || g.opA != OP_N || g.opB != OP_N) return NEGF_EINVAL;
+  launch<OP_N, OP_N, float2>(g, st);
+  NEGF_CUDA_TRY(cudaGetLastError());
+  count_launch();
+  return NEGF_OK;
 }
 
 }  // namespace negf

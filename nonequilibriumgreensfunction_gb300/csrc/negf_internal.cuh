@@ -43,6 +43,31 @@ __host__ __device__ __forceinline__ double2 crcp(double2 a) {
 // |re| + |im|, the pivot measure of LAPACK izamax/dcabs1
 __host__ __device__ __forceinline__ double cabs1(double2 a) { return fabs(a.x) + fabs(a.y); }
 
+// single-precision twins (FP32 form of the inverse)
+__host__ __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__host__ __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__host__ __device__ __forceinline__ float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
+__host__ __device__ __forceinline__ void cfma(float2& acc, float2 a, float2 b) {
+  acc.x = fmaf(a.x, b.x, acc.x);
+  acc.x = fmaf(-a.y, b.y, acc.x);
+  acc.y = fmaf(a.x, b.y, acc.y);
+  acc.y = fmaf(a.y, b.x, acc.y);
+}
+__host__ __device__ __forceinline__ float2 crcp(float2 a) {
+  float s = fmaxf(fabsf(a.x), fabsf(a.y));
+  if (s == 0.0f) return make_float2(1.0f / 0.0f, 0.0f);
+  float ar = a.x / s, ai = a.y / s;
+  float d = s * (ar * ar + ai * ai);
+  return make_float2(ar / d, -ai / d);
+}
+__host__ __device__ __forceinline__ float cabs1(float2 a) { return fabsf(a.x) + fabsf(a.y); }
+
+template <typename T> struct CplxTraits;
+template <> struct CplxTraits<double2> { using R = double; static __host__ __device__ double2 make(double r, double i) { return make_double2(r, i); } };
+template <> struct CplxTraits<float2> { using R = float; static __host__ __device__ float2 make(float r, float i) { return make_float2(r, i); } };
+
 // ----------------------------------------------------------------------------------
 // error handling
 // ----------------------------------------------------------------------------------
@@ -68,15 +93,15 @@ const char* last_cuda_error_text();
 // instrumentation (process-wide; the library is driven by one host thread per handle and
 // the counters are only read by the instrumentation entry points)
 // ----------------------------------------------------------------------------------
-enum TimedKind { TK_GEMM = 0, TK_PANEL = 1, TK_COUNT = 2 };
+enum TimedKind { TK_GEMM = 0, TK_PANEL = 1, TK_TC = 2, TK_COUNT = 3 };
 struct Instrument {
   long long launches = 0;
-  long long kind_launches[TK_COUNT] = {0, 0};
-  double kind_flops[TK_COUNT] = {0, 0};
+  long long kind_launches[TK_COUNT] = {0, 0, 0};
+  double kind_flops[TK_COUNT] = {0, 0, 0};
   bool timing = false;
   struct Rec { cudaEvent_t a, b; int kind; };
   std::vector<Rec> pending;
-  double kind_ms[TK_COUNT] = {0, 0};
+  double kind_ms[TK_COUNT] = {0, 0, 0};
   std::vector<cudaEvent_t> pool;
 };
 Instrument& instrument();
@@ -91,31 +116,36 @@ void instrument_resolve();   // accumulate the elapsed times of finished event p
 // ----------------------------------------------------------------------------------
 enum Op : int { OP_N = 0, OP_T = 1, OP_C = 2 };
 
-struct GemmBatch {
+template <typename T>
+struct GemmBatchT {
   int m, n, k;
-  double2 alpha, beta;
-  const double2* A; int lda; long long sA; Op opA;
-  const double2* B; int ldb; long long sB; Op opB;
-  double2* C; int ldc; long long sC;
+  T alpha, beta;
+  const T* A; int lda; long long sA; Op opA;
+  const T* B; int ldb; long long sB; Op opB;
+  T* C; int ldc; long long sC;
   int batch;
 };
+using GemmBatch = GemmBatchT<double2>;
 int zgemm_f64(const GemmBatch& g, cudaStream_t st);
+int cgemm_f32(const GemmBatchT<float2>& g, cudaStream_t st);   // FP32 twin (inverse updates)
 
 // ----------------------------------------------------------------------------------
 // Batched in-place inverse (blocked Gauss-Jordan with partial row pivoting)
 // ----------------------------------------------------------------------------------
 struct InvWork {
-  double2* rbuf = nullptr;   // batch * nb * n
+  double2* rbuf = nullptr;   // batch * nb * n (FP64; reused as float2 storage by the FP32 form)
   int* ipiv = nullptr;       // batch * n
   int* info = nullptr;       // batch
   int n_cap = 0, batch_cap = 0, nb = 0;
 };
 int inv_work_alloc(InvWork& w, int n, int batch);
 void inv_work_free(InvWork& w);
-int panel_width(int n);
+int panel_width(int n, int elem_bytes = 16);
 // A: batch matrices of n x n, column-major, consecutive at stride sA.  On return A holds
 // the inverses; w.info[b] (device) holds the LAPACK-style INFO of each matrix.
 int zinv_f64(double2* A, long long sA, int n, int batch, InvWork& w, cudaStream_t st);
+// FP32 twin (the first guess of the mixed-form inverse)
+int cinv_f32(float2* A, long long sA, int n, int batch, InvWork& w, cudaStream_t st);
 
 // ----------------------------------------------------------------------------------
 // per-item description of a batch (uploaded once per batch)
@@ -215,6 +245,10 @@ int density_spin(const DensityArgs& a, cudaStream_t st);
 int reduce_sites(int batch, int nsite_total, int nslots, const Item* items, const double* site_out,
                  double* acc, cudaStream_t st);
 
-// convert to / from the Fortran layout on the host side is a plain copy (same layout)
+// mixed form: precision conversion and the Newton-Schulz residual R = I - T (in place),
+// rnorm[b] = atomic max of the row-sum norm of R as the bit pattern of a double
+int to_f32(int n, int batch, const double2* src, long long sS, float2* dst, long long sD, cudaStream_t st);
+int to_f64(int n, int batch, const float2* src, long long sS, double2* dst, long long sD, cudaStream_t st);
+int ns_residual(int n, int batch, double2* T, long long sT, unsigned long long* rnorm, cudaStream_t st);
 
 }  // namespace negf

@@ -489,3 +489,80 @@ int reduce_sites(int batch, int nsite_total, int nslots, const Item* items, cons
 }
 
 }  // namespace negf
+
+// =====================================================================================
+// mixed-form helpers: precision conversion and the Newton-Schulz residual
+// =====================================================================================
+namespace negf {
+
+namespace {
+
+__global__ void to_f32_kernel(int n, const double2* src, long long sS, float2* dst, long long sD) {
+  const int b = blockIdx.y;
+  const long long nn = (long long)n * n;
+  const double2* s = src + (long long)b * sS;
+  float2* d = dst + (long long)b * sD;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nn; e += (long long)gridDim.x * blockDim.x)
+    d[e] = make_float2((float)s[e].x, (float)s[e].y);
+}
+
+__global__ void to_f64_kernel(int n, const float2* src, long long sS, double2* dst, long long sD) {
+  const int b = blockIdx.y;
+  const long long nn = (long long)n * n;
+  const float2* s = src + (long long)b * sS;
+  double2* d = dst + (long long)b * sD;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nn; e += (long long)gridDim.x * blockDim.x)
+    d[e] = make_double2((double)s[e].x, (double)s[e].y);
+}
+
+// R = I - T in place; rnorm[b] = max over rows of sum_j |R_ij| (the infinity norm, the
+// Newton-Schulz contraction factor); one thread per row, columns strided (coalesced)
+__global__ void ns_residual_kernel(int n, double2* T, long long sT, unsigned long long* rnorm) {
+  const int b = blockIdx.y;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double s = 0.0;
+  if (i < n) {
+    double2* Tb = T + (long long)b * sT;
+    for (int j = 0; j < n; ++j) {
+      double2 v = Tb[(long long)j * n + i];
+      v = make_double2((i == j ? 1.0 : 0.0) - v.x, -v.y);
+      Tb[(long long)j * n + i] = v;
+      s += fabs(v.x) + fabs(v.y);
+    }
+  }
+  // block max, then one atomicMax per block on the bit pattern (non-negative doubles order as integers)
+  __shared__ double red[128];
+  red[threadIdx.x] = isnan(s) ? 1e300 : s;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + w]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) atomicMax(rnorm + b, (unsigned long long)__double_as_longlong(red[0]));
+}
+
+}  // namespace
+
+int to_f32(int n, int batch, const double2* src, long long sS, float2* dst, long long sD, cudaStream_t st) {
+  to_f32_kernel<<<ew_grid((long long)n * n, batch), EW_THREADS, 0, st>>>(n, src, sS, dst, sD);
+  NEGF_CUDA_TRY(cudaGetLastError());
+  count_launch();
+  return NEGF_OK;
+}
+
+int to_f64(int n, int batch, const float2* src, long long sS, double2* dst, long long sD, cudaStream_t st) {
+  to_f64_kernel<<<ew_grid((long long)n * n, batch), EW_THREADS, 0, st>>>(n, src, sS, dst, sD);
+  NEGF_CUDA_TRY(cudaGetLastError());
+  count_launch();
+  return NEGF_OK;
+}
+
+int ns_residual(int n, int batch, double2* T, long long sT, unsigned long long* rnorm, cudaStream_t st) {
+  dim3 grid((n + 127) / 128, batch);
+  ns_residual_kernel<<<grid, 128, 0, st>>>(n, T, sT, rnorm);
+  NEGF_CUDA_TRY(cudaGetLastError());
+  count_launch();
+  return NEGF_OK;
+}
+
+}  // namespace negf

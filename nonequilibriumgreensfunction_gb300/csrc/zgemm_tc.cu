@@ -1,0 +1,531 @@
+// Complex GEMM on the tcgen05 tensor cores with exact integer-sliced BF16 operands.
+//
+// C = alpha * A * B + beta * C for batches of complex FP64 matrices (column-major).
+//
+// Number format.  Every row i of A is scaled by 2^-e_i (e_i from frexp of the row's
+// largest |re|,|im|) and every column j of B by 2^-f_j, so all scaled entries lie in
+// (-1, 1).  An entry a is then cut into S integer slices of 7 bits,
+//     a = 2^-6 (s_0 + 2^-7 (s_1 + 2^-7 (s_2 + ...))),   s_p in [-64, 64],
+// each of which is exact in BF16.  With the complex product written as one real product
+//     [Cr | Ci] = [Ar  Ai] [[Br, Bi], [-Bi, Br]]      (K' = 2K, N' = 2N),
+// the slice products S_p T_q are integer matrices with |entries| <= K' * 2^12.  The MMAs
+// of one anti-diagonal d = p + q (at most S pairs) accumulate into one FP32 TMEM
+// accumulator; for d < 5 and K' <= 800 every partial sum stays below 2^24, so those
+// accumulators are EXACT (products of 7-bit integers and their sums are representable).
+// Higher diagonals carry weight <= 2^-35 and their rounding is far below FP64 epsilon of
+// the leading term.  The epilogue forms sum_d acc_d 2^-7d in FP64 and scales by
+// 2^(e_i + f_j - 12).  Accuracy is set by S: truncation <= 2^-7S of the row/column
+// maximum (S = 4: 4e-9, S = 5: 3e-11, S = 7: 2e-15).
+//
+// Kernel structure (one 128 x NT output tile per CTA, 6 warps):
+//   warp 0      TMA producer: for each K block of 32, S A-slices (128 x 32) and S B-slices
+//               (NT x 32) into a ring of shared-memory stages (SWIZZLE_64B, K-major).
+//   warp 1      TMEM allocation and the single-thread tcgen05.mma issue loop; commits
+//               release the stage and, at the end, signal the epilogue.
+//   warps 2-5   epilogue: tcgen05.ld of the S accumulators, FP64 recombination, store.
+// Every mbarrier wait is bounded; on expiry the kernel records an error code and returns
+// after draining its own TMA copies and freeing its TMEM.
+//
+// Replaces, in the mixed form, the ZGEMM calls of Source/Recursive_Greens.F90 and the
+// G Gamma products of Source/Calculate_Gnp.F90.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cudaTypedefs.h>
+
+#include "negf_internal.cuh"
+#include "zgemm_tc.h"
+
+namespace negf {
+
+namespace {
+
+constexpr int TC_THREADS = 192;
+constexpr int BK = 32;              // K elements (bf16) per stage row: 64 bytes, SWIZZLE_64B
+constexpr int ROW_BYTES = BK * 2;   // 64
+constexpr int TILE_M = 128;
+constexpr uint32_t kWaitLimit = 1u << 22;   // ~1 s of polling
+
+// ---------------------------------------------------------------------------------
+// PTX wrappers
+// ---------------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.release.cta.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred P1;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 P1, [%1], %2;\n\t"
+      "selp.b32 %0, 1, 0, P1;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// bounded wait: true on success, false when the limit ran out
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  for (uint32_t i = 0; i < kWaitLimit; ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// SWIZZLE_64B, K-major shared-memory matrix descriptor (tcgen05 "matrix descriptor"):
+// start address >> 4 at [0,14), leading byte offset >> 4 at [16,30) (unused for swizzled
+// K-major), stride byte offset >> 4 at [32,46) = 8 rows * 64 B, version 1 at [46,48),
+// layout type at [61,64) = 4 (64-byte swizzle).
+__device__ __forceinline__ uint64_t make_desc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFF);
+  d |= (uint64_t)(16 >> 4) << 16;
+  d |= (uint64_t)((8 * ROW_BYTES) >> 4) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)4 << 61;
+  return d;
+}
+
+// instruction descriptor, kind::f16: D = F32 (bits 4-5 = 1), A = B = BF16 (bits 7-9,
+// 10-12 = 1), both K-major, N >> 3 at [17,23), M >> 4 at [24,29)
+__host__ __device__ constexpr uint32_t make_idesc(int m, int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accum) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+      "l"(a), "l"(b), "r"(idesc), "r"(accum));
+}
+__device__ __forceinline__ void tc_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// ---------------------------------------------------------------------------------
+// slicing
+// ---------------------------------------------------------------------------------
+template <int S>
+__device__ __forceinline__ void slice_value(double x, int e, __nv_bfloat16 (&out)[S]) {
+  double v = ldexp(x, 6 - e);   // |x| < 2^e  ->  |v| < 64
+#pragma unroll
+  for (int p = 0; p < S; ++p) {
+    const double s = rint(v);
+    out[p] = __float2bfloat16_rn((float)s);
+    v = (v - s) * 128.0;
+  }
+}
+
+__device__ __forceinline__ int scale_exponent(double m) {
+  if (!(m > 0.0) || isinf(m)) return 0;
+  int e;
+  frexp(m, &e);   // m = f 2^e, f in [0.5, 1)
+  return e;
+}
+
+// row exponents of A (M x K complex, column-major): one thread per row
+__global__ void row_exp_kernel(const double2* A, int lda, long long sA, int m, int k, int* ea) {
+  const int b = blockIdx.y;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  const double2* Ab = A + (long long)b * sA;
+  double mx = 0.0;
+  for (int kk = 0; kk < k; ++kk) {
+    const double2 v = Ab[(long long)kk * lda + i];
+    mx = fmax(mx, fmax(fabs(v.x), fabs(v.y)));
+  }
+  ea[(long long)b * m + i] = scale_exponent(mx);
+}
+
+// A slices, K-major: out[((b*S + p)*m + i)*kp + k] with kp = 2K: [Ar(i, :), Ai(i, :)].
+// Tiles of 32 rows x 32 k are transposed through shared memory so both sides coalesce.
+template <int S>
+__global__ void slice_a_kernel(const double2* A, int lda, long long sA, int m, int k, const int* ea,
+                               __nv_bfloat16* out, int half) {
+  const int kp = 2 * half;
+  __shared__ double2 tile[32][33];
+  const int b = blockIdx.z;
+  const int i0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
+  const double2* Ab = A + (long long)b * sA;
+  const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
+  for (int r = ty; r < 32; r += 8) {
+    const int kk = k0 + r, i = i0 + tx;
+    tile[r][tx] = (i < m && kk < k) ? Ab[(long long)kk * lda + i] : make_double2(0.0, 0.0);
+  }
+  __syncthreads();
+  for (int r = ty; r < 32; r += 8) {
+    const int i = i0 + r, kk = k0 + tx;
+    if (i >= m || kk >= k) continue;
+    const double2 v = tile[tx][r];
+    const int e = ea[(long long)b * m + i];
+    __nv_bfloat16 sr[S], si[S];
+    slice_value<S>(v.x, e, sr);
+    slice_value<S>(v.y, e, si);
+#pragma unroll
+    for (int p = 0; p < S; ++p) {
+      __nv_bfloat16* row = out + ((long long)(b * S + p) * m + i) * kp;
+      row[kk] = sr[p];
+      row[half + kk] = si[p];
+    }
+  }
+}
+
+// B slices: one warp per column j of B (K x N complex, column-major).  Rows of the
+// K-major operand (output columns): 2j -> [Br(:,j); -Bi(:,j)], 2j+1 -> [Bi(:,j); Br(:,j)].
+template <int S>
+__global__ void slice_b_kernel(const double2* B, int ldb, long long sB, int k, int n, int* fb, __nv_bfloat16* out,
+                               int half) {
+  const int kp = 2 * half;
+  const int b = blockIdx.y;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int j = blockIdx.x * (blockDim.x >> 5) + warp;
+  if (j >= n) return;
+  const double2* col = B + (long long)b * sB + (long long)j * ldb;
+  double mx = 0.0;
+  for (int kk = lane; kk < k; kk += 32) mx = fmax(mx, fmax(fabs(col[kk].x), fabs(col[kk].y)));
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+  const int e = scale_exponent(mx);
+  if (lane == 0) fb[(long long)b * n + j] = e;
+  const long long n2 = 2LL * n;
+  for (int kk = lane; kk < k; kk += 32) {
+    const double2 v = col[kk];
+    __nv_bfloat16 sr[S], si[S];
+    slice_value<S>(v.x, e, sr);
+    slice_value<S>(v.y, e, si);
+#pragma unroll
+    for (int p = 0; p < S; ++p) {
+      __nv_bfloat16* re_row = out + ((long long)(b * S + p) * n2 + 2LL * j) * kp;
+      __nv_bfloat16* im_row = re_row + kp;
+      re_row[kk] = sr[p];
+      re_row[half + kk] = __hneg(si[p]);
+      im_row[kk] = si[p];
+      im_row[half + kk] = sr[p];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------
+// the MMA kernel
+// ---------------------------------------------------------------------------------
+template <int S, int NT>
+struct TcCfg {
+  static constexpr int A_TILE = TILE_M * ROW_BYTES;            // bytes of one A slice tile
+  static constexpr int B_TILE = NT * ROW_BYTES;                // bytes of one B slice tile
+  static constexpr int STAGE = S * (A_TILE + B_TILE);
+  static constexpr int STAGES = (200 * 1024) / STAGE > 4 ? 4 : (200 * 1024) / STAGE;
+  static constexpr int SMEM = STAGES * STAGE + 1024 + 256;     // + alignment + barriers
+  static constexpr int TMEM_COLS_USED = S * NT;
+  static constexpr int TMEM_COLS = TMEM_COLS_USED <= 32 ? 32 : TMEM_COLS_USED <= 64 ? 64
+                                 : TMEM_COLS_USED <= 128 ? 128 : TMEM_COLS_USED <= 256 ? 256 : 512;
+  static_assert(STAGES >= 2, "at least two stages");
+  static_assert(TMEM_COLS_USED <= 512, "TMEM holds 512 columns");
+  static_assert(NT % 16 == 0 && NT >= 16 && NT <= 256, "UMMA N");
+};
+
+struct TcArgs {
+  int m, n, kp;            // rows of C, complex columns of C, K' = 2K
+  int batch;
+  long long rowsA;         // rows of one (item, slice) plane in the A map (= m)
+  long long rowsB;         // rows of one (item, slice) plane in the B map (= 2n)
+  const int* ea;           // [batch][m]
+  const int* fb;           // [batch][n]
+  double2* C; int ldc; long long sC;
+  double2 alpha, beta;
+  int* err;
+};
+
+template <int S, int NT>
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    zgemm_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, TcArgs a) {
+  using Cfg = TcCfg<S, NT>;
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + Cfg::STAGES * Cfg::STAGE);
+  uint64_t* empty = full + Cfg::STAGES;
+  uint64_t* done = empty + Cfg::STAGES;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
+  int* abort_flag = reinterpret_cast<int*>(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int tm = blockIdx.x, tn = blockIdx.y, b = blockIdx.z;
+  const int nk = (a.kp + BK - 1) / BK;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < Cfg::STAGES; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
+    mbar_init(done, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"((uint32_t)Cfg::TMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      // ---- TMA producer
+      const int a_row0 = tm * TILE_M;
+      const int b_row0 = tn * NT;
+      int issued = 0;
+      for (int kb = 0; kb < nk; ++kb) {
+        const int st = kb % Cfg::STAGES;
+        if (!mbar_wait(&empty[st], ((kb / Cfg::STAGES) & 1) ^ 1)) {
+          atomicExch(abort_flag, 1);
+          if (a.err) atomicCAS(a.err, 0, 1);
+          break;
+        }
+        if (*((volatile int*)abort_flag)) break;
+        uint8_t* sa = smem + st * Cfg::STAGE;
+        uint8_t* sb = sa + S * Cfg::A_TILE;
+        mbar_expect_tx(&full[st], (uint32_t)Cfg::STAGE);
+#pragma unroll
+        for (int p = 0; p < S; ++p) {
+          tma_load_2d(sa + p * Cfg::A_TILE, &mapA, kb * BK, (int)((long long)(b * S + p) * a.rowsA + a_row0), &full[st]);
+          tma_load_2d(sb + p * Cfg::B_TILE, &mapB, kb * BK, (int)((long long)(b * S + p) * a.rowsB + b_row0), &full[st]);
+        }
+        ++issued;
+      }
+      // drain: every issued stage must have landed before the CTA may exit
+      for (int kb = (issued > Cfg::STAGES ? issued - Cfg::STAGES : 0); kb < issued; ++kb)
+        mbar_wait(&full[kb % Cfg::STAGES], (kb / Cfg::STAGES) & 1);
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // ---- MMA issue
+      constexpr uint32_t idesc = make_idesc(TILE_M, NT);
+      for (int kb = 0; kb < nk; ++kb) {
+        const int st = kb % Cfg::STAGES;
+        if (!mbar_wait(&full[st], (kb / Cfg::STAGES) & 1)) {
+          atomicExch(abort_flag, 1);
+          if (a.err) atomicCAS(a.err, 0, 2);
+          break;
+        }
+        tc_fence_after();
+        const uint32_t sa = smem_u32(smem + st * Cfg::STAGE);
+        const uint32_t sb = sa + S * Cfg::A_TILE;
+#pragma unroll
+        for (int d = 0; d < S; ++d) {
+#pragma unroll
+          for (int p = 0; p <= d; ++p) {
+            const int q = d - p;
+#pragma unroll
+            for (int kk = 0; kk < BK / 16; ++kk) {
+              const uint64_t da = make_desc(sa + p * Cfg::A_TILE + kk * 32);
+              const uint64_t db = make_desc(sb + q * Cfg::B_TILE + kk * 32);
+              const uint32_t acc = (kb > 0 || p > 0 || kk > 0) ? 1u : 0u;
+              tc_mma(tmem + d * NT, da, db, idesc, acc);
+            }
+          }
+        }
+        tc_commit(&empty[st]);
+      }
+      tc_commit(done);
+    }
+  } else {
+    // ---- epilogue: warps 2..5 -> TMEM lane quarter (warp % 4)
+    const int quarter = warp & 3;
+    const bool ok = mbar_wait(done, 0);
+    if (!ok && a.err) atomicCAS(a.err, 0, 3);
+    tc_fence_after();
+    const int row = tm * TILE_M + quarter * 32 + lane;
+    const bool aborted = !ok || *((volatile int*)abort_flag);
+    const int e_row = (row < a.m) ? a.ea[(long long)b * a.m + row] : 0;
+    double2* Cb = a.C + (long long)b * a.sC;
+    const bool beta0 = (a.beta.x == 0.0 && a.beta.y == 0.0);
+#pragma unroll 1
+    for (int c0 = 0; c0 < NT; c0 += 16) {
+      double v[16];
+#pragma unroll
+      for (int i = 0; i < 16; ++i) v[i] = 0.0;
+      if (ok) {
+#pragma unroll
+        for (int d = S - 1; d >= 0; --d) {
+          float f[16];
+          tmem_ld16(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(d * NT + c0), f);
+          const double w = ldexp(1.0, -7 * d);
+#pragma unroll
+          for (int i = 0; i < 16; ++i) v[i] = fma((double)f[i], w, v[i]);
+        }
+      }
+      if (row >= a.m || aborted) continue;
+#pragma unroll
+      for (int jj = 0; jj < 8; ++jj) {
+        const int col = (tn * NT + c0) / 2 + jj;   // complex output column
+        if (col >= a.n) continue;
+        const int f_col = a.fb[(long long)b * a.n + col];
+        const double sc = ldexp(1.0, e_row + f_col - 12);
+        const double2 prod = make_double2(v[2 * jj] * sc, v[2 * jj + 1] * sc);
+        double2* cp = Cb + (long long)col * a.ldc + row;
+        double2 out = cmul(a.alpha, prod);
+        if (!beta0) out = cadd(out, cmul(a.beta, *cp));
+        *cp = out;
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)Cfg::TMEM_COLS));
+  }
+}
+
+// ---------------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------------
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    cudaDriverEntryPointQueryResult q;
+    void* p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
+// 2D bf16 map {inner = kp, outer = rows}, box {BK, box_rows}, 64-byte swizzle
+int make_map(CUtensorMap* map, const void* base, int kp, long long rows, int box_rows) {
+  auto fn = encode_fn();
+  if (!fn) return NEGF_ECUDA;
+  if (((uintptr_t)base & 15) != 0 || ((long long)kp * 2) % 16 != 0) return NEGF_EINVAL;
+  cuuint64_t dims[2] = {(cuuint64_t)kp, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)kp * 2};
+  cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? NEGF_OK : NEGF_ECUDA;
+}
+
+template <int S, int NT>
+int launch_mma(const SlicedOperand& A, const SlicedOperand& B, const TcArgs& args, cudaStream_t st) {
+  using Cfg = TcCfg<S, NT>;
+  CUtensorMap ma, mb;
+  NEGF_TRY(make_map(&ma, A.data, args.kp, (long long)args.batch * S * args.rowsA, TILE_M));
+  NEGF_TRY(make_map(&mb, B.data, args.kp, (long long)args.batch * S * args.rowsB, NT));
+  NEGF_CUDA_TRY(cudaFuncSetAttribute(zgemm_tc_kernel<S, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM));
+  dim3 grid((args.m + TILE_M - 1) / TILE_M, (unsigned)((2LL * args.n + NT - 1) / NT), args.batch);
+  cudaEvent_t ev;
+  timed_begin(st, TK_TC, 8.0 * args.m * (double)args.n * (args.kp / 2) * args.batch, &ev);
+  zgemm_tc_kernel<S, NT><<<grid, TC_THREADS, Cfg::SMEM, st>>>(ma, mb, args);
+  NEGF_CUDA_TRY(cudaGetLastError());
+  timed_end(st, TK_TC, ev);
+  count_launch();
+  return NEGF_OK;
+}
+
+template <int S>
+int slice_a_t(const double2* A, int lda, long long sA, int m, int k, int batch, SlicedOperand& out, cudaStream_t st) {
+  if (out.k != k)   // padded K: the pad columns of every slice row must read as zero
+    NEGF_CUDA_TRY(cudaMemsetAsync(out.data, 0, sliced_bytes(m, out.k, S, batch), st));
+  dim3 g1((m + 127) / 128, batch);
+  row_exp_kernel<<<g1, 128, 0, st>>>(A, lda, sA, m, k, out.exps);
+  NEGF_CUDA_TRY(cudaGetLastError());
+  dim3 g2((m + 31) / 32, (k + 31) / 32, batch);
+  slice_a_kernel<S><<<g2, dim3(32, 8), 0, st>>>(A, lda, sA, m, k, out.exps, out.data, out.k);
+  NEGF_CUDA_TRY(cudaGetLastError());
+  count_launch(2);
+  return NEGF_OK;
+}
+
+template <int S>
+int slice_b_t(const double2* B, int ldb, long long sB, int k, int n, int batch, SlicedOperand& out, cudaStream_t st) {
+  if (out.k != k) NEGF_CUDA_TRY(cudaMemsetAsync(out.data, 0, sliced_bytes(2 * n, out.k, S, batch), st));
+  dim3 g((n + 7) / 8, batch);
+  slice_b_kernel<S><<<g, 256, 0, st>>>(B, ldb, sB, k, n, out.exps, out.data, out.k);
+  NEGF_CUDA_TRY(cudaGetLastError());
+  count_launch();
+  return NEGF_OK;
+}
+
+}  // namespace
+
+bool tc_supported_slices(int s) { return s == 3 || s == 4 || s == 5 || s == 7; }
+
+size_t sliced_bytes(int rows, int k, int slices, int batch) {
+  return sizeof(__nv_bfloat16) * (size_t)batch * slices * rows * 2 * (size_t)k;
+}
+
+int padded_k(int k) { return (k + 3) & ~3; }
+
+int slice_a(const double2* A, int lda, long long sA, int m, int k, int batch, int slices, SlicedOperand& out,
+            cudaStream_t st) {
+  out.rows = m; out.k = padded_k(k); out.slices = slices; out.batch = batch;
+  switch (slices) {
+    case 3: return slice_a_t<3>(A, lda, sA, m, k, batch, out, st);
+    case 4: return slice_a_t<4>(A, lda, sA, m, k, batch, out, st);
+    case 5: return slice_a_t<5>(A, lda, sA, m, k, batch, out, st);
+    case 7: return slice_a_t<7>(A, lda, sA, m, k, batch, out, st);
+  }
+  return NEGF_EINVAL;
+}
+
+int slice_b(const double2* B, int ldb, long long sB, int k, int n, int batch, int slices, SlicedOperand& out,
+            cudaStream_t st) {
+  out.rows = 2 * n; out.k = padded_k(k); out.slices = slices; out.batch = batch;
+  switch (slices) {
+    case 3: return slice_b_t<3>(B, ldb, sB, k, n, batch, out, st);
+    case 4: return slice_b_t<4>(B, ldb, sB, k, n, batch, out, st);
+    case 5: return slice_b_t<5>(B, ldb, sB, k, n, batch, out, st);
+    case 7: return slice_b_t<7>(B, ldb, sB, k, n, batch, out, st);
+  }
+  return NEGF_EINVAL;
+}
+
+int zgemm_tc(const SlicedOperand& A, const SlicedOperand& B, double2 alpha, double2 beta, double2* C, int ldc,
+             long long sC, int* err, cudaStream_t st) {
+  if (A.slices != B.slices || A.k != B.k || A.batch != B.batch) return NEGF_EINVAL;
+  // the leading accumulator (one pair) is exact for K' * 2^12 < 2^24; larger K would
+  // round it and lose the FP64-class tail
+  if (2 * A.k >= 4096) return NEGF_EINVAL;
+  TcArgs args{};
+  args.m = A.rows; args.n = B.rows / 2; args.kp = 2 * A.k; args.batch = A.batch;
+  args.rowsA = A.rows; args.rowsB = B.rows;
+  args.ea = A.exps; args.fb = B.exps;
+  args.C = C; args.ldc = ldc; args.sC = sC;
+  args.alpha = alpha; args.beta = beta; args.err = err;
+  switch (A.slices) {
+    case 3: return launch_mma<3, 128>(A, B, args, st);
+    case 4: return launch_mma<4, 128>(A, B, args, st);
+    case 5: return launch_mma<5, 64>(A, B, args, st);
+    case 7: return launch_mma<7, 64>(A, B, args, st);
+  }
+  return NEGF_EINVAL;
+}
+
+}  // namespace negf
