@@ -228,8 +228,11 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--form", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--form", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--batch", type=int, default=16)
+    ap.add_argument("--slices", type=int, default=0, help="mixed form: BF16 slices of the RGF products (0 = default)")
+    ap.add_argument("--fp64-steps", type=int, default=1,
+                    help="mixed form: timed FP64 steps on the same requests (T error and FP64 rate)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
@@ -253,7 +256,7 @@ def main():
     hams = build_hamiltonians()
     m = 4 * NPY * NPZ
     solver = Solver(NPX, NPY, NPZ, n_hamiltonians=SEEDS, max_batch=args.batch, eta=ETA, sr_tol=SR_TOL,
-                    calc_spin=True, precision=args.form, device=local_rank)
+                    calc_spin=True, precision=args.form, device=local_rank, mixed_slices=args.slices)
     stream = torch.cuda.Stream(dev)          # a real stream handle, so events bracket the work
     torch.cuda.set_stream(stream)
     solver.set_stream(stream.cuda_stream)
@@ -280,6 +283,7 @@ def main():
         r = one_step(s)
         assert (r["status"] == 0).all(), r["status"]
     sr_iters = int(np.max(r["sr_iters"]))
+    timed_results = []
 
     clocks_path = os.path.join(REPO, "gpurun_out", "bench_clocks_rank%d.csv" % rank)
     os.makedirs(os.path.dirname(clocks_path), exist_ok=True)
@@ -292,6 +296,7 @@ def main():
         ev0.record(stream)
         for s in range(args.steps):
             r = one_step(args.warmup + s)
+            timed_results.append(r)
         ev1.record(stream)
         torch.cuda.synchronize()
     st = solver.stats()
@@ -329,21 +334,69 @@ def main():
         e2e = {"value": args.batch * args.steps * world / el2, "unit": "solves/s",
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)}
 
+    # FP64 form on the same requests: its rate, and the T error of the mixed form
+    fp64 = None
+    if args.form == "mixed" and args.fp64_steps > 0:
+        st_mixed = st
+        solver.close()
+        ref = Solver(NPX, NPY, NPZ, n_hamiltonians=SEEDS, max_batch=args.batch, eta=ETA, sr_tol=SR_TOL,
+                     calc_spin=True, precision="fp64", device=local_rank)
+        ref.set_stream(stream.cuda_stream)
+        for k, (hf, xf) in enumerate(pinned):
+            ref.set_hamiltonian_fortran(hf, xf, slot=k)
+        n_fp = min(args.fp64_steps, args.steps)
+        rn64 = np.zeros_like(rho_n)
+        ev4, ev5 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        ev4.record(stream)
+        outs = []
+        for s in range(n_fp):
+            e, f1, f2, slots = step_requests(args.warmup + s, args.batch, rank, world)
+            outs.append(ref.solve_batch(e, f1, f2, 0.6 / (N_E - 1), slots=slots, rho_n=rn64))
+        ev5.record(stream)
+        torch.cuda.synchronize()
+        el64 = ev4.elapsed_time(ev5) * 1e-3
+        t_err = 0.0
+        for a, b in zip(timed_results[:n_fp], outs):
+            t_err = max(t_err, float(np.max(np.abs(a["T12"] - b["T12"]) / np.maximum(np.abs(b["T12"]), 1e-3))))
+        fp64 = {"value": args.batch * n_fp / el64, "unit": "solves/s", "steps": n_fp,
+                "t_rel_err_max": t_err, "t_err_gate": 1e-6, "gate_ok": t_err <= 1e-6,
+                "t_err_floor": "denominator max(|T_fp64|, 1e-3)"}
+        ref.close()
+        solver = None
+        st = st_mixed
+
     if rank != 0:
         if world > 1:
             dist.destroy_process_group()
         return
 
     peaks = measured_peaks()
-    fp64_peak = fp64_zgemm_peak_tflops(torch, dev)
-    gemm_tf = st["gemm_flops"] / (st["gemm_ms"] * 1e-3) / 1e12 if st["gemm_ms"] > 0 else None
-    roofline = {
-        "bound": "tensor", "kernel": "zgemm_kernel (FP64 complex GEMM, DFMA)",
-        "achieved": gemm_tf, "peak": fp64_peak, "unit": "TFLOP/s",
-        "frac": (gemm_tf / fp64_peak) if gemm_tf else None, "traffic": None,
-        "peak_source": "cuBLAS ZGEMM 4096^3 complex128 measured live (of measured)",
-        "gemm_launches": st["gemm_launches"], "gemm_share_of_step": st["gemm_ms"] * 1e-3 / elapsed,
-    }
+    if args.form == "fp64":
+        fp64_peak = fp64_zgemm_peak_tflops(torch, dev)
+        gemm_tf = st["gemm_flops"] / (st["gemm_ms"] * 1e-3) / 1e12 if st["gemm_ms"] > 0 else None
+        roofline = {
+            "bound": "tensor", "kernel": "zgemm_kernel (FP64 complex GEMM, DFMA)",
+            "achieved": gemm_tf, "peak": fp64_peak, "unit": "TFLOP/s",
+            "frac": (gemm_tf / fp64_peak) if gemm_tf else None, "traffic": None,
+            "peak_source": "cuBLAS ZGEMM 4096^3 complex128 measured live (of measured)",
+            "launches": st["gemm_launches"], "share_of_step": st["gemm_ms"] * 1e-3 / elapsed,
+        }
+    else:
+        # tensor work actually issued: the slice-pair products, counted from the stats'
+        # complex-equivalent flops; achieved = issued BF16 tensor flops / kernel time
+        tc_issued = st.get("tc_flops") or None
+        tc_tf = (tc_issued / (st["tc_ms"] * 1e-3) / 1e12) if (tc_issued and st["tc_ms"] > 0) else None
+        bf16_peak = peaks.get("bf16_tflops")
+        roofline = {
+            "bound": "tensor", "kernel": "zgemm_tc_kernel (tcgen05 sliced-BF16 complex GEMM)",
+            "achieved": tc_tf, "peak": bf16_peak, "unit": "TFLOP/s",
+            "frac": (tc_tf / bf16_peak) if (tc_tf and bf16_peak) else None, "traffic": None,
+            "peak_source": "MEASURED_PEAKS.json bf16_tflops (of measured, burst)",
+            "launches": st["tc_launches"], "share_of_step": st["tc_ms"] * 1e-3 / elapsed,
+            "complex_equiv_tflops": (st["tc_complex_flops"] / (st["tc_ms"] * 1e-3) / 1e12) if st["tc_ms"] > 0 else None,
+            "fallbacks": st["fallbacks"], "ns_residual_max": st["ns_residual_max"],
+        }
     flops_solve = algorithmic_flops_per_solve(m, NPX, sr_iters)
     cpu = None
     if not args.no_cpu_baseline and world == 1:
@@ -362,13 +415,15 @@ def main():
         "algorithmic_flops_per_solve": flops_solve,
         "sr_iters": sr_iters,
         "cpu_baseline": cpu,
+        "fp64_form": fp64,
         "e2e": e2e,
         "gpu_launches": st["launches"],
         "clocks": clk.summary(local_rank),
         "peaks_file": {k: peaks.get(k) for k in ("hbm_gbs", "bf16_tflops", "bf16_tflops_sustained")},
     }
     print(json.dumps(line), flush=True)
-    solver.close()
+    if solver is not None:
+        solver.close()
     if world > 1:
         dist.destroy_process_group()
 

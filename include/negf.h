@@ -103,7 +103,8 @@ typedef struct negf_stats {
     double  panel_ms;
     int64_t tc_launches;     /* tcgen05 sliced-BF16 GEMM launches (mixed form)             */
     double  tc_ms;
-    double  tc_flops;        /* complex-equivalent flops 8*m*n*k of those GEMMs            */
+    double  tc_flops;        /* BF16 tensor flops issued: S(S+1)/2 slice pairs x 8*m*n*k   */
+    double  tc_complex_flops;/* the complex products they compute, 8*m*n*k                 */
     int64_t fallbacks;       /* mixed form: inverses redone in FP64 (residual too large)   */
     double  ns_residual_max; /* mixed form: largest accepted first Newton-Schulz residual  */
 } negf_stats;
@@ -185,6 +186,64 @@ typedef struct negf_result {
  * continues past failed requests as the reference's energy loop does.                  */
 NEGF_API int negf_solve_batch(negf_handle* h, const negf_request* req, int32_t n, negf_result* res,
                      double* RhoN, double* RhoP, double* SigX, double* SigY, double* SigZ);
+
+/* ---- serving ----------------------------------------------------------------------
+ * A device-resident request loop in place of the MPI energy sweep: wires of different
+ * cross-sections arrive as requests (Hamiltonian + a list of energy points with their
+ * occupations), are admitted while the HBM budget has room for their geometry's block
+ * store (Npx*M^2*16 bytes per in-flight energy point) and a free Hamiltonian slot, and
+ * their energy points are packed, with those of every other admitted request of the same
+ * geometry, into the next device batch (continuous batching).  Each geometry is served by
+ * its own worker thread and CUDA stream, so work of different geometries overlaps on the
+ * device.  A request's results do not depend on what it was batched with.               */
+typedef struct negf_server negf_server;
+
+typedef struct negf_serve_params {
+    int32_t device;
+    int32_t precision;        /* NEGF_PREC_*                                                 */
+    int32_t mixed_slices;     /* as in negf_params                                           */
+    int32_t max_batch;        /* energy points per device batch, per geometry                */
+    int32_t slots_per_geometry; /* Hamiltonians resident per geometry                       */
+    int32_t calc_spin;
+    double  eta, sr_tol;
+    int32_t sr_max_iter;
+    int32_t reserved0;
+    int64_t hbm_budget_bytes; /* device memory the server may hold (0 = 80% of free)         */
+    int32_t reserved[8];
+} negf_serve_params;
+
+typedef struct negf_wire_request {
+    int32_t npx, npy, npz, norb;
+    const double* Htotd;      /* M x M x npx complex, copied at submit                       */
+    const double* HopX;       /* M x M complex, copied at submit                             */
+    int32_t n_energies;
+    int32_t reserved0;
+    const double* energies;   /* n_energies each, copied at submit                           */
+    const double* f1;
+    const double* f2;
+    const double* dE;
+} negf_wire_request;
+
+typedef struct negf_wire_status {
+    int32_t done;             /* 1 when every energy point is solved                         */
+    int32_t status;           /* first non-zero per-energy status                            */
+    int32_t n_done;           /* energy points solved so far                                 */
+    int32_t reserved0;
+    double  t_submit, t_admit, t_done;   /* seconds on the server's monotonic clock         */
+} negf_wire_status;
+
+NEGF_API int negf_server_create(const negf_serve_params* p, negf_server** out);
+NEGF_API int negf_server_submit(negf_server* s, const negf_wire_request* r, int64_t* id);
+/* status only (results NULL) or, once done, copy out: per energy T12/EDensity/HDensity/
+ * Modec1/Modec2/DOSc1/DOSc2 into res7[7*n_energies] and RhoN/RhoP (npx*npy*npz each,
+ * dE-weighted sums) into rho[2*npx*npy*npz]; a finished request is released by the
+ * call that copies its results out (release != 0).                                      */
+NEGF_API int negf_server_poll(negf_server* s, int64_t id, negf_wire_status* st, double* res7, double* rho,
+                              int32_t release);
+/* block until request `id` is done or timeout_s elapses (NEGF_ETIMEDOUT)               */
+NEGF_API int negf_server_wait(negf_server* s, int64_t id, double timeout_s);
+NEGF_API double negf_server_clock(const negf_server* s);
+NEGF_API int negf_server_destroy(negf_server* s);
 
 /* ---- stateless dense kernels -------------------------------------------------------
  * Drop-ins for the reference's dense calls on host arrays (column-major, interleaved

@@ -35,6 +35,8 @@ EXPORTED_SYMBOLS = (
     "negf_set_hamiltonian", "negf_contact_self_energy", "negf_get_retarded_greens",
     "negf_copy_g_columns", "negf_calculate_gnp", "negf_calculate_observables",
     "negf_solve_batch", "negf_zgemm", "negf_zinv",
+    "negf_server_create", "negf_server_submit", "negf_server_poll", "negf_server_wait",
+    "negf_server_clock", "negf_server_destroy",
 )
 
 
@@ -65,7 +67,26 @@ class NegfStats(ctypes.Structure):
     _fields_ = [("launches", c_int64), ("gemm_launches", c_int64), ("gemm_ms", c_double),
                 ("gemm_flops", c_double), ("panel_launches", c_int64), ("panel_ms", c_double),
                 ("tc_launches", c_int64), ("tc_ms", c_double), ("tc_flops", c_double),
+                ("tc_complex_flops", c_double),
                 ("fallbacks", c_int64), ("ns_residual_max", c_double)]
+
+
+class NegfServeParams(ctypes.Structure):
+    _fields_ = [("device", c_int32), ("precision", c_int32), ("mixed_slices", c_int32), ("max_batch", c_int32),
+                ("slots_per_geometry", c_int32), ("calc_spin", c_int32), ("eta", c_double), ("sr_tol", c_double),
+                ("sr_max_iter", c_int32), ("reserved0", c_int32), ("hbm_budget_bytes", c_int64),
+                ("reserved", c_int32 * 8)]
+
+
+class NegfWireRequest(ctypes.Structure):
+    _fields_ = [("npx", c_int32), ("npy", c_int32), ("npz", c_int32), ("norb", c_int32),
+                ("Htotd", c_void_p), ("HopX", c_void_p), ("n_energies", c_int32), ("reserved0", c_int32),
+                ("energies", c_void_p), ("f1", c_void_p), ("f2", c_void_p), ("dE", c_void_p)]
+
+
+class NegfWireStatus(ctypes.Structure):
+    _fields_ = [("done", c_int32), ("status", c_int32), ("n_done", c_int32), ("reserved0", c_int32),
+                ("t_submit", c_double), ("t_admit", c_double), ("t_done", c_double)]
 
 
 class NegfError(RuntimeError):
@@ -98,6 +119,12 @@ def _declare(lib):
         "negf_zgemm": (c_int, [c_int32, c_int32, c_int32, c_int32, _dp, _dp, c_int32, _dp, c_int32, _dp, _dp,
                                c_int32, c_int32]),
         "negf_zinv": (c_int, [c_int32, _dp, _dp, c_int32]),
+        "negf_server_create": (c_int, [POINTER(NegfServeParams), POINTER(c_void_p)]),
+        "negf_server_submit": (c_int, [h, POINTER(NegfWireRequest), POINTER(c_int64)]),
+        "negf_server_poll": (c_int, [h, c_int64, POINTER(NegfWireStatus), _dp, _dp, c_int32]),
+        "negf_server_wait": (c_int, [h, c_int64, c_double]),
+        "negf_server_clock": (c_double, [h]),
+        "negf_server_destroy": (c_int, [h]),
         "negf_solve_batch": (c_int, [h, POINTER(NegfRequest), c_int32, POINTER(NegfResult),
                                      _dp, _dp, _dp, _dp, _dp]),
     }

@@ -24,6 +24,18 @@ Instrument& instrument() {
 }
 
 namespace {
+void resolve_locked() {
+  Instrument& I = instrument();
+  for (const Instrument::Rec& r : I.pending) {
+    float ms = 0.f;
+    if (cudaEventSynchronize(r.b) == cudaSuccess && cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess)
+      I.kind_ms[r.kind] += ms;
+    I.pool.push_back(r.a);
+    I.pool.push_back(r.b);
+  }
+  I.pending.clear();
+}
+
 cudaEvent_t pooled_event() {
   Instrument& I = instrument();
   if (!I.pool.empty()) {
@@ -37,12 +49,19 @@ cudaEvent_t pooled_event() {
 }
 }  // namespace
 
+void add_tc_complex_flops(double f) {
+  Instrument& I = instrument();
+  std::lock_guard<std::mutex> g(I.mu);
+  I.tc_complex_flops += f;
+}
+
 void timed_begin(cudaStream_t st, int kind, double flops, cudaEvent_t* a) {
   Instrument& I = instrument();
-  I.kind_launches[kind] += 1;
-  I.kind_flops[kind] += flops;
+  I.kind_launches[kind].fetch_add(1, std::memory_order_relaxed);
   *a = nullptr;
-  if (!I.timing) return;
+  std::lock_guard<std::mutex> g(I.mu);
+  I.kind_flops[kind] += flops;
+  if (!I.timing.load()) return;
   *a = pooled_event();
   if (*a) cudaEventRecord(*a, st);
 }
@@ -50,23 +69,18 @@ void timed_begin(cudaStream_t st, int kind, double flops, cudaEvent_t* a) {
 void timed_end(cudaStream_t st, int kind, cudaEvent_t a) {
   Instrument& I = instrument();
   if (!a) return;
+  std::lock_guard<std::mutex> g(I.mu);
   cudaEvent_t b = pooled_event();
   if (!b) { I.pool.push_back(a); return; }
   cudaEventRecord(b, st);
   I.pending.push_back(Instrument::Rec{a, b, kind});
-  if (I.pending.size() >= 8192) instrument_resolve();
+  if (I.pending.size() >= 8192) resolve_locked();
 }
 
 void instrument_resolve() {
   Instrument& I = instrument();
-  for (const Instrument::Rec& r : I.pending) {
-    float ms = 0.f;
-    if (cudaEventSynchronize(r.b) == cudaSuccess && cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess)
-      I.kind_ms[r.kind] += ms;
-    I.pool.push_back(r.a);
-    I.pool.push_back(r.b);
-  }
-  I.pending.clear();
+  std::lock_guard<std::mutex> g(I.mu);
+  resolve_locked();
 }
 
 }  // namespace negf
@@ -142,9 +156,13 @@ int negf_profile(negf_handle* h, int enable) {
   NEGF_CUDA_TRY(cudaSetDevice(h->eng.p_.device));
   negf::instrument_resolve();
   negf::Instrument& I = negf::instrument();
-  I.launches = 0;
-  for (int k = 0; k < negf::TK_COUNT; ++k) { I.kind_launches[k] = 0; I.kind_flops[k] = 0; I.kind_ms[k] = 0; }
-  I.timing = enable != 0;
+  {
+    std::lock_guard<std::mutex> g(I.mu);
+    I.launches.store(0);
+    for (int k = 0; k < negf::TK_COUNT; ++k) { I.kind_launches[k].store(0); I.kind_flops[k] = 0; I.kind_ms[k] = 0; }
+    I.tc_complex_flops = 0;
+    I.timing.store(enable != 0);
+  }
   h->eng.fallbacks_ = 0;
   h->eng.last_rnorm_max_ = 0.0;
   return NEGF_OK;
@@ -154,16 +172,18 @@ int negf_get_stats(negf_handle* h, negf_stats* out) {
   if (!h || !out) return NEGF_EINVAL;
   NEGF_CUDA_TRY(cudaSetDevice(h->eng.p_.device));
   negf::instrument_resolve();
-  const negf::Instrument& I = negf::instrument();
-  out->launches = I.launches;
-  out->gemm_launches = I.kind_launches[negf::TK_GEMM];
+  negf::Instrument& I = negf::instrument();
+  std::lock_guard<std::mutex> g(I.mu);
+  out->launches = I.launches.load();
+  out->gemm_launches = I.kind_launches[negf::TK_GEMM].load();
   out->gemm_ms = I.kind_ms[negf::TK_GEMM];
   out->gemm_flops = I.kind_flops[negf::TK_GEMM];
-  out->panel_launches = I.kind_launches[negf::TK_PANEL];
+  out->panel_launches = I.kind_launches[negf::TK_PANEL].load();
   out->panel_ms = I.kind_ms[negf::TK_PANEL];
-  out->tc_launches = I.kind_launches[negf::TK_TC];
+  out->tc_launches = I.kind_launches[negf::TK_TC].load();
   out->tc_ms = I.kind_ms[negf::TK_TC];
   out->tc_flops = I.kind_flops[negf::TK_TC];
+  out->tc_complex_flops = I.tc_complex_flops;
   out->fallbacks = h->eng.fallbacks_;
   out->ns_residual_max = h->eng.last_rnorm_max_;
   return NEGF_OK;

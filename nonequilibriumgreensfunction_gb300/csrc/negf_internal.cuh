@@ -6,8 +6,10 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <atomic>
 #include <cstdint>
 #include <cstdio>
+#include <mutex>
 #include <vector>
 
 #include "../../include/negf.h"
@@ -90,22 +92,26 @@ void record_cuda_error(cudaError_t e, const char* what, const char* file, int li
 const char* last_cuda_error_text();
 
 // ----------------------------------------------------------------------------------
-// instrumentation (process-wide; the library is driven by one host thread per handle and
-// the counters are only read by the instrumentation entry points)
+// instrumentation (process-wide, shared by all handles and server workers: counters are
+// atomic, the flop sums and the event bookkeeping are under `mu`)
 // ----------------------------------------------------------------------------------
 enum TimedKind { TK_GEMM = 0, TK_PANEL = 1, TK_TC = 2, TK_COUNT = 3 };
 struct Instrument {
-  long long launches = 0;
-  long long kind_launches[TK_COUNT] = {0, 0, 0};
+  std::atomic<long long> launches{0};
+  std::atomic<long long> kind_launches[TK_COUNT];
+  std::mutex mu;
   double kind_flops[TK_COUNT] = {0, 0, 0};
-  bool timing = false;
+  std::atomic<bool> timing{false};
   struct Rec { cudaEvent_t a, b; int kind; };
   std::vector<Rec> pending;
   double kind_ms[TK_COUNT] = {0, 0, 0};
+  double tc_complex_flops = 0;
   std::vector<cudaEvent_t> pool;
+  Instrument() { for (auto& k : kind_launches) k.store(0); }
 };
 Instrument& instrument();
-inline void count_launch(int n = 1) { instrument().launches += n; }
+inline void count_launch(int n = 1) { instrument().launches.fetch_add(n, std::memory_order_relaxed); }
+void add_tc_complex_flops(double f);
 // start/stop a timed region on `st` around one launch of `kind`
 void timed_begin(cudaStream_t st, int kind, double flops, cudaEvent_t* a);
 void timed_end(cudaStream_t st, int kind, cudaEvent_t a);

@@ -441,7 +441,9 @@ int launch_mma(const SlicedOperand& A, const SlicedOperand& B, const TcArgs& arg
   NEGF_CUDA_TRY(cudaFuncSetAttribute(zgemm_tc_kernel<S, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM));
   dim3 grid((args.m + TILE_M - 1) / TILE_M, (unsigned)((2LL * args.n + NT - 1) / NT), args.batch);
   cudaEvent_t ev;
-  timed_begin(st, TK_TC, 8.0 * args.m * (double)args.n * (args.kp / 2) * args.batch, &ev);
+  const double cflops = 8.0 * args.m * (double)args.n * (args.kp / 2) * args.batch;
+  add_tc_complex_flops(cflops);
+  timed_begin(st, TK_TC, cflops * (S * (S + 1) / 2), &ev);
   zgemm_tc_kernel<S, NT><<<grid, TC_THREADS, Cfg::SMEM, st>>>(ma, mb, args);
   NEGF_CUDA_TRY(cudaGetLastError());
   timed_end(st, TK_TC, ev);

@@ -1,0 +1,68 @@
+"""Serving: continuous batching of wires of different cross-sections.  Each request's
+results equal those of the same wire solved alone (the batch composition never enters
+a request's arithmetic), and admission under a small HBM budget queues requests until
+memory frees up instead of failing."""
+import numpy as np
+import pytest
+
+from nonequilibriumgreensfunction_gb300 import Solver
+from nonequilibriumgreensfunction_gb300 import hamiltonian as HB
+from nonequilibriumgreensfunction_gb300.serving import Server
+
+pytestmark = pytest.mark.gpu
+
+
+def _wire(n, npx, seed):
+    h, x = HB.ti_wire(npx, n, n, W=0.1, seed=seed, flux=0.3, zeeman=0.01)
+    return h, x
+
+
+def _alone(h, x, npx, n, es, f1, f2, de, precision):
+    with Solver(npx, n, n, eta=1e-5, sr_tol=1e-10, max_batch=len(es), precision=precision) as s:
+        s.set_hamiltonian(h, x)
+        rn = s.new_site_array(1)
+        r = s.solve_batch(es, f1, f2, de, rho_n=rn)
+    return r, rn[..., 0]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_server_results_same_alone_and_in_the_mix(need_gpu, precision):
+    rng = np.random.default_rng(0)
+    wires = [(2, 6, 0), (3, 5, 1), (2, 6, 2), (3, 7, 3), (2, 6, 4)]   # (cross-section, npx, seed)
+    reqs = []
+    with Server(precision=precision, max_batch=4, slots_per_geometry=2) as srv:
+        for n, npx, seed in wires:
+            h, x = _wire(n, npx, seed)
+            es = np.sort(rng.uniform(-0.25, 0.25, size=int(rng.integers(3, 9))))
+            f1 = rng.uniform(0, 1, es.size)
+            f2 = rng.uniform(0, 1, es.size)
+            rid = srv.submit(h, x, es, f1, f2, 1e-3)
+            reqs.append((rid, h, x, n, npx, es, f1, f2))
+        for rid, h, x, n, npx, es, f1, f2 in reqs:
+            srv.wait(rid, timeout=300)
+            got = srv.result(rid)
+            assert got["status"] == 0
+            want, rn = _alone(h, x, npx, n, es, f1, f2, 1e-3, precision)
+            for k in ("T12", "EDensity", "HDensity", "Modec1", "Modec2", "DOSc1", "DOSc2"):
+                assert np.array_equal(got[k], want[k]), (k, got[k], want[k])
+            assert np.array_equal(got["RhoN"], rn)
+            assert got["t_submit"] <= got["t_admit"] <= got["t_done"]
+
+
+def test_server_admission_under_small_budget(need_gpu):
+    """A budget that holds one geometry's engine at a time: requests of the other geometry
+    wait for the idle engine to be released, and every request completes."""
+    rng = np.random.default_rng(1)
+    with Server(precision="fp64", max_batch=2, slots_per_geometry=1, hbm_budget_bytes=100 << 20) as srv:
+        ids = []
+        for i in range(4):
+            n, npx = (2, 6) if i % 2 == 0 else (3, 5)
+            h, x = _wire(n, npx, i)
+            es = rng.uniform(-0.2, 0.2, 3)
+            ids.append((srv.submit(h, x, es, 1.0, 0.0, 1e-3), h, x, n, npx, es))
+        for rid, h, x, n, npx, es in ids:
+            srv.wait(rid, timeout=300)
+            got = srv.result(rid)
+            assert got["status"] == 0
+            want, _ = _alone(h, x, npx, n, es, 1.0, 0.0, 1e-3, "fp64")
+            assert np.array_equal(got["T12"], want["T12"])
