@@ -61,7 +61,7 @@ def test_sliced_gemm_zero_rows_and_wide_exponents(need_gpu):
     got = capi.zgemm(A, B, slices=7)
     assert np.all(got[0, 5, :] == 0.0) and np.all(got[0, :, 3] == 0.0)
     rel = np.abs(got - ref) / np.maximum(np.abs(A).max(axis=-1)[..., None] * np.abs(B).max(axis=-2)[:, None, :], 1e-300)
-    assert rel.max() < 64 * 2.0 ** -49
+    assert rel.max() < 8 * 2.0 ** -49 * A.shape[-1]
 
 
 def test_inverse_matches_lapack(need_gpu):
