@@ -93,7 +93,7 @@ class Engine {
   // mixed form (NEGF_PREC_MIXED): tensor-core GEMMs on S integer BF16 slices, inverses as
   // FP32 Gauss-Jordan + Newton-Schulz steps with the residual at s_res_ slices
   bool mixed_ = false;
-  int s_rgf_ = 4;      // RGF block products
+  int s_rgf_ = 5;      // RGF block products
   int s_sr_ = 7;       // Sancho-Rubio products (FP64-class)
   int s_res_ = 7;      // Newton-Schulz residual W X (FP64-class)
   int s_upd_ = 4;      // Newton-Schulz update X R (R is small)
