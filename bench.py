@@ -52,12 +52,15 @@ def fermi(e, mu, kt):
 
 
 def step_requests(step, batch, rank, world):
-    """Requests of one step: consecutive grid energies, seeds round-robin; ranks take
-    disjoint energies (the units are independent, no exchange between ranks)."""
+    """Requests of one step: batch/4 consecutive grid energies, each for all 4 disorder
+    seeds (the config's 512 energies x 4 seeds, walked energy-major), so the seeds of one
+    energy share its lead decimation; ranks take disjoint energies (the units are
+    independent, no exchange between ranks)."""
     grid = energy_grid()
-    idx = [((step * world + rank) * batch + i) % N_E for i in range(batch)]
+    ne = max(1, batch // SEEDS)
+    idx = [((step * world + rank) * ne + i // SEEDS) % N_E for i in range(batch)]
     e = grid[idx]
-    slots = np.array([(step * batch + i) % SEEDS for i in range(batch)], dtype=np.int32)
+    slots = np.array([i % SEEDS for i in range(batch)], dtype=np.int32)
     f1 = np.array([fermi(x, MU[0], KT) for x in e])
     f2 = np.array([fermi(x, MU[1], KT) for x in e])
     return e, f1, f2, slots
@@ -397,6 +400,9 @@ def main():
             "complex_equiv_tflops": (st["tc_complex_flops"] / (st["tc_ms"] * 1e-3) / 1e12) if st["tc_ms"] > 0 else None,
             "fallbacks": st["fallbacks"], "ns_residual_max": st["ns_residual_max"],
         }
+    roofline["breakdown_s_per_step"] = {
+        k: st[k] * 1e-3 / args.steps for k in ("phase_sr_ms", "phase_rgf_ms", "phase_inv_ms", "phase_dens_ms",
+                                               "tc_ms", "gemm_ms", "panel_ms", "f32_gemm_ms", "slice_ms")}
     flops_solve = algorithmic_flops_per_solve(m, NPX, sr_iters)
     cpu = None
     if not args.no_cpu_baseline and world == 1:

@@ -107,6 +107,12 @@ typedef struct negf_stats {
     double  tc_complex_flops;/* the complex products they compute, 8*m*n*k                 */
     int64_t fallbacks;       /* mixed form: inverses redone in FP64 (residual too large)   */
     double  ns_residual_max; /* mixed form: largest accepted first Newton-Schulz residual  */
+    double  f32_gemm_ms;     /* FP32 Gauss-Jordan rank-nb updates (mixed form)             */
+    double  slice_ms;        /* operand slicing kernels (mixed form)                       */
+    double  phase_sr_ms;     /* whole Sancho-Rubio phases                                  */
+    double  phase_rgf_ms;    /* whole RGF sweeps (including their inverses)                */
+    double  phase_inv_ms;    /* all inverses (Sancho-Rubio and RGF)                        */
+    double  phase_dens_ms;   /* density / spin reductions                                  */
 } negf_stats;
 NEGF_API int negf_profile(negf_handle* h, int enable);
 NEGF_API int negf_get_stats(negf_handle* h, negf_stats* out);

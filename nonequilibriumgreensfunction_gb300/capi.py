@@ -68,7 +68,9 @@ class NegfStats(ctypes.Structure):
                 ("gemm_flops", c_double), ("panel_launches", c_int64), ("panel_ms", c_double),
                 ("tc_launches", c_int64), ("tc_ms", c_double), ("tc_flops", c_double),
                 ("tc_complex_flops", c_double),
-                ("fallbacks", c_int64), ("ns_residual_max", c_double)]
+                ("fallbacks", c_int64), ("ns_residual_max", c_double), ("f32_gemm_ms", c_double),
+                ("slice_ms", c_double), ("phase_sr_ms", c_double), ("phase_rgf_ms", c_double),
+                ("phase_inv_ms", c_double), ("phase_dens_ms", c_double)]
 
 
 class NegfServeParams(ctypes.Structure):

@@ -184,6 +184,12 @@ int negf_get_stats(negf_handle* h, negf_stats* out) {
   out->tc_ms = I.kind_ms[negf::TK_TC];
   out->tc_flops = I.kind_flops[negf::TK_TC];
   out->tc_complex_flops = I.tc_complex_flops;
+  out->f32_gemm_ms = I.kind_ms[negf::TK_F32];
+  out->slice_ms = I.kind_ms[negf::TK_SLICE];
+  out->phase_sr_ms = I.kind_ms[negf::TK_PH_SR];
+  out->phase_rgf_ms = I.kind_ms[negf::TK_PH_RGF];
+  out->phase_inv_ms = I.kind_ms[negf::TK_PH_INV];
+  out->phase_dens_ms = I.kind_ms[negf::TK_PH_DENS];
   out->fallbacks = h->eng.fallbacks_;
   out->ns_residual_max = h->eng.last_rnorm_max_;
   return NEGF_OK;

@@ -299,6 +299,14 @@ int Engine::merge_info(int batch) { return merge_info_kernel_launch(batch, inv_.
 // (FP64-class) and X R at s_upd_ slices; a matrix whose first residual norm is above
 // ns_accept_ (or whose FP32 factorisation met a zero pivot) is inverted again in FP64.
 int Engine::invert(double2* A, long long sA, int batch, int* status_dev) {
+  cudaEvent_t ph;
+  timed_begin(st_, TK_PH_INV, 0.0, &ph);
+  const int rc = invert_impl(A, sA, batch, status_dev);
+  timed_end(st_, TK_PH_INV, ph);
+  return rc;
+}
+
+int Engine::invert_impl(double2* A, long long sA, int batch, int* status_dev) {
   if (!mixed_) {
     NEGF_TRY(zinv_f64(A, sA, M_, batch, inv_, st_));
     return merge_info_kernel_launch(batch, inv_.info, status_dev, st_);
@@ -349,6 +357,14 @@ int Engine::invert(double2* A, long long sA, int batch, int* status_dev) {
 // Sancho-Rubio (Source/Contact_Self_Energy.F90:156-269), batched over problems
 // -------------------------------------------------------------------------------------
 int Engine::solve_sr(const std::vector<SrJob>& jobs, std::vector<int>& status, std::vector<int>& iters) {
+  cudaEvent_t ph;
+  timed_begin(st_, TK_PH_SR, 0.0, &ph);
+  const int rc = solve_sr_impl(jobs, status, iters);
+  timed_end(st_, TK_PH_SR, ph);
+  return rc;
+}
+
+int Engine::solve_sr_impl(const std::vector<SrJob>& jobs, std::vector<int>& status, std::vector<int>& iters) {
   const int S = (int)jobs.size();
   if (S == 0) return NEGF_OK;
   if (S > S_) return NEGF_EINVAL;
@@ -470,6 +486,14 @@ int Engine::solve_sr(const std::vector<SrJob>& jobs, std::vector<int>& status, s
 // RGF sweep with the Gn site blocks and the end-block traces, batched over items
 // -------------------------------------------------------------------------------------
 int Engine::solve_rgf(const std::vector<Item>& items, bool keep_columns) {
+  cudaEvent_t ph;
+  timed_begin(st_, TK_PH_RGF, 0.0, &ph);
+  const int rc = solve_rgf_impl(items, keep_columns);
+  timed_end(st_, TK_PH_RGF, ph);
+  return rc;
+}
+
+int Engine::solve_rgf_impl(const std::vector<Item>& items, bool keep_columns) {
   const int B = (int)items.size();
   if (B == 0) return NEGF_OK;
   if (B > B_) return NEGF_EINVAL;
@@ -564,6 +588,14 @@ int Engine::solve_rgf(const std::vector<Item>& items, bool keep_columns) {
 }
 
 int Engine::densities(const std::vector<Item>& items, std::vector<double>& edens, std::vector<double>& hdens) {
+  cudaEvent_t ph;
+  timed_begin(st_, TK_PH_DENS, 0.0, &ph);
+  const int rc = densities_impl(items, edens, hdens);
+  timed_end(st_, TK_PH_DENS, ph);
+  return rc;
+}
+
+int Engine::densities_impl(const std::vector<Item>& items, std::vector<double>& edens, std::vector<double>& hdens) {
   const int B = (int)items.size();
   NEGF_CUDA_TRY(cudaMemcpyAsync(dItems_, items.data(), sizeof(Item) * B, cudaMemcpyHostToDevice, st_));
   DensityArgs a{};
@@ -594,7 +626,7 @@ int Engine::densities(const std::vector<Item>& items, std::vector<double>& edens
 // Batched solve
 // -------------------------------------------------------------------------------------
 int Engine::batch_solve(const negf_request* req, int n, negf_result* res, double* RhoN, double* RhoP, double* SigX,
-                        double* SigY, double* SigZ) {
+                        double* SigY, double* SigZ, double* site_items) {
   if (n < 0 || (n > 0 && (!req || !res))) return NEGF_EINVAL;
   NEGF_CUDA_TRY(cudaSetDevice(p_.device));
   const long long total = nsite_total();
@@ -644,6 +676,9 @@ int Engine::batch_solve(const negf_request* req, int n, negf_result* res, double
     std::vector<double> ed, hd;
     NEGF_TRY(densities(items, ed, hd));
     NEGF_TRY(reduce_sites(nb, (int)total, nslots, dItems_, dSite_, dAcc_, st_));
+    if (site_items)
+      NEGF_CUDA_TRY(cudaMemcpyAsync(site_items + (size_t)c0 * 5 * total, dSite_, sizeof(double) * 5 * total * nb,
+                                    cudaMemcpyDeviceToHost, st_));
     std::vector<double> tr(4 * (size_t)nb);
     std::vector<int> rst(nb);
     NEGF_CUDA_TRY(cudaMemcpyAsync(tr.data(), dTr_, sizeof(double) * 4 * nb, cudaMemcpyDeviceToHost, st_));

@@ -30,8 +30,10 @@ class Engine {
   // densities/spin for the current batch (after solve_rgf) with the items' f1,f2,dE
   int densities(const std::vector<Item>& items, std::vector<double>& edens, std::vector<double>& hdens);
 
+  // site_items (optional): n x 5 x nsite_total per-request dE-weighted site arrays, so a
+  // caller can sum energies in its own fixed order
   int batch_solve(const negf_request* req, int n, negf_result* res, double* RhoN, double* RhoP, double* SigX,
-                  double* SigY, double* SigZ);
+                  double* SigY, double* SigZ, double* site_items = nullptr);
 
   // accessors used by the per-energy API
   int M() const { return M_; }
@@ -109,6 +111,10 @@ class Engine {
   long long fallbacks_ = 0;
   double last_rnorm_max_ = 0.0;
   int invert(double2* A, long long sA, int batch, int* status_dev);
+  int invert_impl(double2* A, long long sA, int batch, int* status_dev);
+  int solve_sr_impl(const std::vector<SrJob>& jobs, std::vector<int>& status, std::vector<int>& iters);
+  int solve_rgf_impl(const std::vector<Item>& items, bool keep_columns);
+  int densities_impl(const std::vector<Item>& items, std::vector<double>& edens, std::vector<double>& hdens);
   HopBD hop() const {
     HopBD h;
     h.hb = dHopBD_;

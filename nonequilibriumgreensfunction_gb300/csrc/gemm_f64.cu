@@ -167,8 +167,11 @@ namespace negf {
 int cgemm_f32(const GemmBatchT<float2>& g, cudaStream_t st) {
   if (g.m <= 0 || g.n <= 0 || g.batch <= 0) return NEGF_OK;
   if (g.batch > 65535 || g.opA != OP_N || g.opB != OP_N) return NEGF_EINVAL;
+  cudaEvent_t ev;
+  timed_begin(st, TK_F32, 8.0 * g.m * g.n * (double)g.k * g.batch, &ev);
   launch<OP_N, OP_N, float2>(g, st);
   NEGF_CUDA_TRY(cudaGetLastError());
+  timed_end(st, TK_F32, ev);
   count_launch();
   return NEGF_OK;
 }

@@ -95,16 +95,20 @@ const char* last_cuda_error_text();
 // instrumentation (process-wide, shared by all handles and server workers: counters are
 // atomic, the flop sums and the event bookkeeping are under `mu`)
 // ----------------------------------------------------------------------------------
-enum TimedKind { TK_GEMM = 0, TK_PANEL = 1, TK_TC = 2, TK_COUNT = 3 };
+// kinds timed per launch (kernels) or per phase (PH_*), only while profiling is on
+enum TimedKind {
+  TK_GEMM = 0, TK_PANEL = 1, TK_TC = 2, TK_F32 = 3, TK_SLICE = 4,
+  TK_PH_SR = 5, TK_PH_RGF = 6, TK_PH_INV = 7, TK_PH_DENS = 8, TK_COUNT = 9
+};
 struct Instrument {
   std::atomic<long long> launches{0};
   std::atomic<long long> kind_launches[TK_COUNT];
   std::mutex mu;
-  double kind_flops[TK_COUNT] = {0, 0, 0};
+  double kind_flops[TK_COUNT] = {};
   std::atomic<bool> timing{false};
   struct Rec { cudaEvent_t a, b; int kind; };
   std::vector<Rec> pending;
-  double kind_ms[TK_COUNT] = {0, 0, 0};
+  double kind_ms[TK_COUNT] = {};
   double tc_complex_flops = 0;
   std::vector<cudaEvent_t> pool;
   Instrument() { for (auto& k : kind_launches) k.store(0); }

@@ -516,29 +516,32 @@ __global__ void to_f64_kernel(int n, const float2* src, long long sS, double2* d
 }
 
 // R = I - T in place; rnorm[b] = max over rows of sum_j |R_ij| (the infinity norm, the
-// Newton-Schulz contraction factor); one thread per row, columns strided (coalesced)
+// Newton-Schulz contraction factor).  A CTA covers 32 rows; its 8 thread rows stride over
+// the columns (coalesced) and the row sums are reduced in shared memory in fixed order.
 __global__ void ns_residual_kernel(int n, double2* T, long long sT, unsigned long long* rnorm) {
+  __shared__ double part[8][32];
   const int b = blockIdx.y;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int i = blockIdx.x * 32 + tx;
   double s = 0.0;
   if (i < n) {
     double2* Tb = T + (long long)b * sT;
-    for (int j = 0; j < n; ++j) {
+    for (int j = ty; j < n; j += 8) {
       double2 v = Tb[(long long)j * n + i];
       v = make_double2((i == j ? 1.0 : 0.0) - v.x, -v.y);
       Tb[(long long)j * n + i] = v;
       s += fabs(v.x) + fabs(v.y);
     }
   }
-  // block max, then one atomicMax per block on the bit pattern (non-negative doubles order as integers)
-  __shared__ double red[128];
-  red[threadIdx.x] = isnan(s) ? 1e300 : s;
+  part[ty][tx] = s;
   __syncthreads();
-  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-    if (threadIdx.x < w) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + w]);
-    __syncthreads();
+  if (ty == 0) {
+    for (int q = 1; q < 8; ++q) s += part[q][tx];
+    if (isnan(s)) s = 1e300;
+    // warp max, then one atomicMax per CTA on the bit pattern (non-negative doubles order as integers)
+    for (int off = 16; off > 0; off >>= 1) s = fmax(s, __shfl_xor_sync(0xffffffffu, s, off));
+    if (tx == 0) atomicMax(rnorm + b, (unsigned long long)__double_as_longlong(s));
   }
-  if (threadIdx.x == 0) atomicMax(rnorm + b, (unsigned long long)__double_as_longlong(red[0]));
 }
 
 }  // namespace
@@ -558,8 +561,8 @@ int to_f64(int n, int batch, const float2* src, long long sS, double2* dst, long
 }
 
 int ns_residual(int n, int batch, double2* T, long long sT, unsigned long long* rnorm, cudaStream_t st) {
-  dim3 grid((n + 127) / 128, batch);
-  ns_residual_kernel<<<grid, 128, 0, st>>>(n, T, sT, rnorm);
+  dim3 grid((n + 31) / 32, batch);
+  ns_residual_kernel<<<grid, dim3(32, 8), 0, st>>>(n, T, sT, rnorm);
   NEGF_CUDA_TRY(cudaGetLastError());
   count_launch();
   return NEGF_OK;

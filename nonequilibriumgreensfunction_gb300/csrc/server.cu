@@ -195,7 +195,7 @@ struct negf_server {
     cudaSetDevice(p.device);
     negf::Engine& eng = *w->eng;
     const long long total = (long long)w->key.npx * w->key.npy * w->key.npz;
-    std::vector<double> acc(5 * total * p.slots_per_geometry);
+    std::vector<double> items(5 * total * (size_t)p.max_batch);
     std::unique_lock<std::mutex> lk(mu);
     for (;;) {
       work_cv.wait(lk, [&] {
@@ -241,13 +241,13 @@ struct negf_server {
       int rc = NEGF_OK;
       if (!batch.empty()) {
         lk.unlock();
-        std::fill(acc.begin(), acc.end(), 0.0);
-        double* a0 = acc.data();
-        const long long st = (long long)p.slots_per_geometry * total;
-        rc = eng.batch_solve(batch.data(), (int)batch.size(), res.data(), a0, a0 + st, nullptr, nullptr, nullptr);
+        rc = eng.batch_solve(batch.data(), (int)batch.size(), res.data(), nullptr, nullptr, nullptr, nullptr, nullptr,
+                             items.data());
         lk.lock();
       }
-      // scatter results; site sums belong to the slot's owner
+      // scatter results; each energy's densities are added to its request in energy order
+      // (the order a single batch over the whole request uses), so sums do not depend on
+      // how the request's energies were split into batches
       std::vector<Request*> touched;
       for (size_t i = 0; i < owner.size(); ++i) {
         Request* r = owner[i].first;
@@ -259,14 +259,14 @@ struct negf_server {
         const int stv = rc != NEGF_OK ? rc : o.status;
         if (stv != 0 && r->status == 0) r->status = stv;
         r->n_done++;
+        const double* si = items.data() + i * 5 * (size_t)total;
+        for (long long j = 0; j < total; ++j) {
+          r->rho[j] += si[j];
+          r->rho[total + j] += si[total + j];
+        }
         if (std::find(touched.begin(), touched.end(), r) == touched.end()) touched.push_back(r);
       }
-      const long long st = (long long)p.slots_per_geometry * total;
       for (Request* r : touched) {
-        for (long long i = 0; i < total; ++i) {
-          r->rho[i] += acc[(size_t)r->slot * total + i];
-          r->rho[total + i] += acc[st + (size_t)r->slot * total + i];
-        }
         if (r->n_done == (int)r->e.size()) {
           r->done = true;
           r->t_done = now();

@@ -149,18 +149,26 @@ __device__ __forceinline__ int scale_exponent(double m) {
   return e;
 }
 
-// row exponents of A (M x K complex, column-major): one thread per row
+// row exponents of A (M x K complex, column-major): a CTA covers 32 rows, its 8 thread
+// rows stride over the columns (coalesced 512-byte row segments), reduced in shared memory
 __global__ void row_exp_kernel(const double2* A, int lda, long long sA, int m, int k, int* ea) {
+  __shared__ double part[8][32];
   const int b = blockIdx.y;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= m) return;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int i = blockIdx.x * 32 + tx;
   const double2* Ab = A + (long long)b * sA;
   double mx = 0.0;
-  for (int kk = 0; kk < k; ++kk) {
-    const double2 v = Ab[(long long)kk * lda + i];
-    mx = fmax(mx, fmax(fabs(v.x), fabs(v.y)));
+  if (i < m)
+    for (int kk = ty; kk < k; kk += 8) {
+      const double2 v = Ab[(long long)kk * lda + i];
+      mx = fmax(mx, fmax(fabs(v.x), fabs(v.y)));
+    }
+  part[ty][tx] = mx;
+  __syncthreads();
+  if (ty == 0 && i < m) {
+    for (int q = 1; q < 8; ++q) mx = fmax(mx, part[q][tx]);
+    ea[(long long)b * m + i] = scale_exponent(mx);
   }
-  ea[(long long)b * m + i] = scale_exponent(mx);
 }
 
 // A slices, K-major: out[((b*S + p)*m + i)*kp + k] with kp = 2K: [Ar(i, :), Ai(i, :)].
@@ -455,12 +463,15 @@ template <int S>
 int slice_a_t(const double2* A, int lda, long long sA, int m, int k, int batch, SlicedOperand& out, cudaStream_t st) {
   if (out.k != k)   // padded K: the pad columns of every slice row must read as zero
     NEGF_CUDA_TRY(cudaMemsetAsync(out.data, 0, sliced_bytes(m, out.k, S, batch), st));
-  dim3 g1((m + 127) / 128, batch);
-  row_exp_kernel<<<g1, 128, 0, st>>>(A, lda, sA, m, k, out.exps);
+  cudaEvent_t ev;
+  timed_begin(st, TK_SLICE, 0.0, &ev);
+  dim3 g1((m + 31) / 32, batch);
+  row_exp_kernel<<<g1, dim3(32, 8), 0, st>>>(A, lda, sA, m, k, out.exps);
   NEGF_CUDA_TRY(cudaGetLastError());
   dim3 g2((m + 31) / 32, (k + 31) / 32, batch);
   slice_a_kernel<S><<<g2, dim3(32, 8), 0, st>>>(A, lda, sA, m, k, out.exps, out.data, out.k);
   NEGF_CUDA_TRY(cudaGetLastError());
+  timed_end(st, TK_SLICE, ev);
   count_launch(2);
   return NEGF_OK;
 }
@@ -469,8 +480,11 @@ template <int S>
 int slice_b_t(const double2* B, int ldb, long long sB, int k, int n, int batch, SlicedOperand& out, cudaStream_t st) {
   if (out.k != k) NEGF_CUDA_TRY(cudaMemsetAsync(out.data, 0, sliced_bytes(2 * n, out.k, S, batch), st));
   dim3 g((n + 7) / 8, batch);
+  cudaEvent_t ev;
+  timed_begin(st, TK_SLICE, 0.0, &ev);
   slice_b_kernel<S><<<g, 256, 0, st>>>(B, ldb, sB, k, n, out.exps, out.data, out.k);
   NEGF_CUDA_TRY(cudaGetLastError());
+  timed_end(st, TK_SLICE, ev);
   count_launch();
   return NEGF_OK;
 }
