@@ -87,6 +87,7 @@ Engine::~Engine() {
   dfree(dSrCmax_); dfree(dSrDos_); dfree(dSrActive_); dfree(dSrE_); dfree(dSrHend_); dfree(dSrStatus_);
   inv_work_free(inv_);
   dfree(dWinv_); dfree(dW32_); dfree(dT_); dfree(sa_.data); dfree(sb_.data); dfree(sa_.exps); dfree(sb_.exps);
+  dfree(sw_.data); dfree(sw_.exps);
   dfree(dRnorm_); dfree(dTcErr_);
   if (hPin_) cudaFreeHost(hPin_);
   if (own_st_) cudaStreamDestroy(own_st_);
@@ -165,6 +166,8 @@ int Engine::alloc() {
     const int kp = padded_k(M_);
     NEGF_TRY(dalloc(reinterpret_cast<char**>(&sa_.data), sliced_bytes(M_, kp, smax, cap), bytes_));
     NEGF_TRY(dalloc(reinterpret_cast<char**>(&sb_.data), sliced_bytes(2 * M_, kp, smax, cap), bytes_));
+    NEGF_TRY(dalloc(reinterpret_cast<char**>(&sw_.data), sliced_bytes(M_, kp, smax, cap), bytes_));
+    NEGF_TRY(dalloc(&sw_.exps, (size_t)cap * M_, bytes_));
     NEGF_TRY(dalloc(&sa_.exps, (size_t)cap * M_, bytes_));
     NEGF_TRY(dalloc(&sb_.exps, (size_t)cap * M_, bytes_));
     NEGF_TRY(dalloc(&dRnorm_, (size_t)cap, bytes_));
@@ -319,15 +322,12 @@ int Engine::invert_impl(double2* A, long long sA, int batch, int* status_dev) {
   std::vector<int> info32(batch);
   NEGF_CUDA_TRY(cudaMemcpyAsync(info32.data(), inv_.info, sizeof(int) * batch, cudaMemcpyDeviceToHost, st_));
   NEGF_CUDA_TRY(cudaMemsetAsync(dRnorm_, 0, sizeof(unsigned long long) * batch, st_));
-  NEGF_TRY(slice_a(dWinv_, M_, MM_, M_, M_, batch, s_res_, sa_, st_));
+  NEGF_TRY(slice_a(dWinv_, M_, MM_, M_, M_, batch, s_res_, sw_, st_));
   std::vector<unsigned long long> r0(batch);
   for (int step = 0; step < ns_steps_; ++step) {
-    if (step > 0) {
-      NEGF_CUDA_TRY(cudaMemsetAsync(dRnorm_, 0, sizeof(unsigned long long) * batch, st_));
-      NEGF_TRY(slice_a(dWinv_, M_, MM_, M_, M_, batch, s_res_, sa_, st_));
-    }
+    if (step > 0) NEGF_CUDA_TRY(cudaMemsetAsync(dRnorm_, 0, sizeof(unsigned long long) * batch, st_));
     NEGF_TRY(slice_b(A, M_, sA, M_, M_, batch, s_res_, sb_, st_));
-    NEGF_TRY(zgemm_tc(sa_, sb_, one, zero, dT_, M_, MM_, dTcErr_, st_));          // T = W X
+    NEGF_TRY(zgemm_tc(sw_, sb_, one, zero, dT_, M_, MM_, dTcErr_, st_));          // T = W X
     NEGF_TRY(ns_residual(M_, batch, dT_, MM_, dRnorm_, st_));                     // R = I - T
     if (step == 0)
       NEGF_CUDA_TRY(cudaMemcpyAsync(r0.data(), dRnorm_, sizeof(unsigned long long) * batch, cudaMemcpyDeviceToHost, st_));

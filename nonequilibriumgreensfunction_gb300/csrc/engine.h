@@ -105,7 +105,7 @@ class Engine {
   double2* dWinv_ = nullptr; // copy of the matrix being inverted (FP64)
   float2* dW32_ = nullptr;
   double2* dT_ = nullptr;
-  SlicedOperand sa_, sb_;
+  SlicedOperand sa_, sb_, sw_;   // sw_: slices of the matrix under inversion (kept across NS steps)
   unsigned long long* dRnorm_ = nullptr;
   int* dTcErr_ = nullptr;
   long long fallbacks_ = 0;

@@ -166,10 +166,12 @@ __global__ void gj_colswap_kernel(T* A, long long sA, int n, const int* ipiv) {
 }  // namespace
 
 int panel_width(int n, int elem_bytes) {
-  // the panel (n x nb complex) must fit the 227 KB opt-in shared memory of a CTA; the
-  // FP32 form takes twice as wide a panel (half as many rank-nb updates)
+  // the panel (n x nb complex) must fit the 227 KB opt-in shared memory of a CTA.  The
+  // panel's work grows with nb (n*nb^2 per panel, n^2*nb per inverse) while its rank-nb
+  // updates are cheap, so both forms use nb = 32.
   const long long limit = kPanelSmemMax;
-  int nb = elem_bytes == 16 ? 32 : 64;
+  int nb = 32;
+  (void)elem_bytes;
   while (nb > 4 && (long long)n * nb * (long long)elem_bytes > limit) nb >>= 1;
   return nb;
 }

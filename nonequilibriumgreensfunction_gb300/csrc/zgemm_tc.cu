@@ -116,6 +116,31 @@ __device__ __forceinline__ void tc_commit(uint64_t* bar) {
                : "memory");
 }
 
+// v * 2^scale as a double, rounded to nearest even, built from integer operations only
+// (results below the normal range flush to zero)
+__device__ __forceinline__ double scaled_int_to_double(long long v, int scale) {
+  if (v == 0) return 0.0;
+  const unsigned long long sign = v < 0 ? (1ULL << 63) : 0ULL;
+  unsigned long long u = v < 0 ? (unsigned long long)(-v) : (unsigned long long)v;
+  int top = 63 - __clzll((long long)u);
+  unsigned long long mant;
+  if (top <= 52) {
+    mant = u << (52 - top);
+  } else {
+    const int sh = top - 52;
+    const unsigned long long rem = u & ((1ULL << sh) - 1), halfu = 1ULL << (sh - 1);
+    mant = u >> sh;
+    if (rem > halfu || (rem == halfu && (mant & 1))) {
+      ++mant;
+      if (mant >> 53) { mant >>= 1; ++top; }
+    }
+  }
+  const int ex = top + scale + 1023;
+  if (ex <= 0) return __longlong_as_double((long long)sign);
+  if (ex >= 2047) return __longlong_as_double((long long)(sign | (0x7FFULL << 52)));
+  return __longlong_as_double((long long)(sign | ((unsigned long long)ex << 52) | (mant & ((1ULL << 52) - 1))));
+}
+
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
   uint32_t r[16];
   asm volatile(
@@ -131,15 +156,29 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
 // ---------------------------------------------------------------------------------
 // slicing
 // ---------------------------------------------------------------------------------
+// Slices of x at scale exponent e (|x| < 2^e): the fixed-point integer
+// F = round(x 2^(6 + 7(S-1) - e)), |F| <= 2^(6 + 7(S-1)) <= 2^48, built from the bits of x
+// with integer operations only (GB300's FP64 pipe is 1/64 of its FP32 rate), then written
+// as balanced base-128 digits: F = sum_p s_p 128^(S-1-p), lower digits in [-64, 63], the
+// top digit in [-64, 64].  Every digit is exact in BF16; the truncation is <= 2^-7S of 2^e.
 template <int S>
 __device__ __forceinline__ void slice_value(double x, int e, __nv_bfloat16 (&out)[S]) {
-  double v = ldexp(x, 6 - e);   // |x| < 2^e  ->  |v| < 64
-#pragma unroll
-  for (int p = 0; p < S; ++p) {
-    const double s = rint(v);
-    out[p] = __float2bfloat16_rn((float)s);
-    v = (v - s) * 128.0;
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+  const int ex = (int)((bits >> 52) & 0x7FF);
+  long long F = 0;
+  if (ex != 0 && ex != 0x7FF) {                      // zero and subnormals slice to 0
+    const unsigned long long m = (bits & ((1ULL << 52) - 1)) | (1ULL << 52);   // x = m 2^(ex - 1075)
+    const int r = e - (ex - 1075) - (6 + 7 * (S - 1));                          // F = m 2^-r, r >= 5
+    if (r < 64) F = (long long)((m + (1ULL << (r - 1))) >> r);
+    if (bits >> 63) F = -F;
   }
+#pragma unroll
+  for (int p = S - 1; p >= 1; --p) {
+    const long long d = ((F + 64) & 127) - 64;
+    out[p] = __float2bfloat16_rn((float)d);
+    F = (F - d) >> 7;
+  }
+  out[0] = __float2bfloat16_rn((float)F);
 }
 
 __device__ __forceinline__ int scale_exponent(double m) {
@@ -171,49 +210,60 @@ __global__ void row_exp_kernel(const double2* A, int lda, long long sA, int m, i
   }
 }
 
-// A slices, K-major: out[((b*S + p)*m + i)*kp + k] with kp = 2K: [Ar(i, :), Ai(i, :)].
-// Tiles of 32 rows x 32 k are transposed through shared memory so both sides coalesce.
+// A slices, K-major: out[((b*S + p)*m + i)*kp + k] with kp = 2*half: [Ar(i, :), Ai(i, :)],
+// zero in the padding k in [K, half).  A tile of 32 rows x 64 k is staged through shared
+// memory (coalesced column-major reads); each thread then slices one row x 8 consecutive
+// k and writes 16-byte vectors.
 template <int S>
-__global__ void slice_a_kernel(const double2* A, int lda, long long sA, int m, int k, const int* ea,
-                               __nv_bfloat16* out, int half) {
+__global__ void __launch_bounds__(256) slice_a_kernel(const double2* A, int lda, long long sA, int m, int k,
+                                                      const int* ea, __nv_bfloat16* out, int half) {
+  __shared__ double2 tile[64][33];
   const int kp = 2 * half;
-  __shared__ double2 tile[32][33];
   const int b = blockIdx.z;
-  const int i0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
+  const int i0 = blockIdx.x * 32, k0 = blockIdx.y * 64;
   const double2* Ab = A + (long long)b * sA;
-  const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
-  for (int r = ty; r < 32; r += 8) {
-    const int kk = k0 + r, i = i0 + tx;
-    tile[r][tx] = (i < m && kk < k) ? Ab[(long long)kk * lda + i] : make_double2(0.0, 0.0);
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;   // 32 x 8
+#pragma unroll
+  for (int r = 0; r < 8; ++r) {
+    const int kk = k0 + ty + 8 * r, i = i0 + tx;
+    tile[ty + 8 * r][tx] = (i < m && kk < k) ? Ab[(long long)kk * lda + i] : make_double2(0.0, 0.0);
   }
   __syncthreads();
-  for (int r = ty; r < 32; r += 8) {
-    const int i = i0 + r, kk = k0 + tx;
-    if (i >= m || kk >= k) continue;
-    const double2 v = tile[tx][r];
-    const int e = ea[(long long)b * m + i];
-    __nv_bfloat16 sr[S], si[S];
-    slice_value<S>(v.x, e, sr);
-    slice_value<S>(v.y, e, si);
+  const int row = threadIdx.x >> 3, kg = threadIdx.x & 7;
+  const int i = i0 + row, kb = k0 + 8 * kg;
+  if (i >= m || kb >= half) return;
+  const int e = ea[(long long)b * m + i];
+  __align__(16) __nv_bfloat16 sr[S][8], si[S][8];
 #pragma unroll
-    for (int p = 0; p < S; ++p) {
-      __nv_bfloat16* row = out + ((long long)(b * S + p) * m + i) * kp;
-      row[kk] = sr[p];
-      row[half + kk] = si[p];
-    }
+  for (int q = 0; q < 8; ++q) {
+    const double2 v = tile[8 * kg + q][row];
+    __nv_bfloat16 a[S], c[S];
+    slice_value<S>(v.x, e, a);
+    slice_value<S>(v.y, e, c);
+#pragma unroll
+    for (int p = 0; p < S; ++p) { sr[p][q] = a[p]; si[p][q] = c[p]; }
+  }
+#pragma unroll
+  for (int p = 0; p < S; ++p) {
+    __nv_bfloat16* rowp = out + ((long long)(b * S + p) * m + i) * kp;
+    *reinterpret_cast<uint4*>(rowp + kb) = *reinterpret_cast<const uint4*>(sr[p]);
+    *reinterpret_cast<uint4*>(rowp + half + kb) = *reinterpret_cast<const uint4*>(si[p]);
   }
 }
 
 // B slices: one warp per column j of B (K x N complex, column-major).  Rows of the
-// K-major operand (output columns): 2j -> [Br(:,j); -Bi(:,j)], 2j+1 -> [Bi(:,j); Br(:,j)].
+// K-major operand (output columns): 2j -> [Br(:,j); -Bi(:,j)], 2j+1 -> [Bi(:,j); Br(:,j)],
+// zero in the padding.  Chunks of 256 k are read coalesced into shared memory; each lane
+// then slices 8 consecutive k and writes 16-byte vectors.
 template <int S>
-__global__ void slice_b_kernel(const double2* B, int ldb, long long sB, int k, int n, int* fb, __nv_bfloat16* out,
-                               int half) {
+__global__ void __launch_bounds__(256) slice_b_kernel(const double2* B, int ldb, long long sB, int k, int n, int* fb,
+                                                      __nv_bfloat16* out, int half) {
+  __shared__ double2 chunk[8][256];
   const int kp = 2 * half;
   const int b = blockIdx.y;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int j = blockIdx.x * (blockDim.x >> 5) + warp;
-  if (j >= n) return;
+  const int j = blockIdx.x * 8 + warp;
+  if (j >= n) return;   // whole warps leave together; no block-wide barrier below
   const double2* col = B + (long long)b * sB + (long long)j * ldb;
   double mx = 0.0;
   for (int kk = lane; kk < k; kk += 32) mx = fmax(mx, fmax(fabs(col[kk].x), fabs(col[kk].y)));
@@ -222,20 +272,37 @@ __global__ void slice_b_kernel(const double2* B, int ldb, long long sB, int k, i
   const int e = scale_exponent(mx);
   if (lane == 0) fb[(long long)b * n + j] = e;
   const long long n2 = 2LL * n;
-  for (int kk = lane; kk < k; kk += 32) {
-    const double2 v = col[kk];
-    __nv_bfloat16 sr[S], si[S];
-    slice_value<S>(v.x, e, sr);
-    slice_value<S>(v.y, e, si);
+  double2* ch = chunk[warp];
+  for (int c0 = 0; c0 < half; c0 += 256) {
 #pragma unroll
-    for (int p = 0; p < S; ++p) {
-      __nv_bfloat16* re_row = out + ((long long)(b * S + p) * n2 + 2LL * j) * kp;
-      __nv_bfloat16* im_row = re_row + kp;
-      re_row[kk] = sr[p];
-      re_row[half + kk] = __hneg(si[p]);
-      im_row[kk] = si[p];
-      im_row[half + kk] = sr[p];
+    for (int q = 0; q < 8; ++q) {
+      const int kk = c0 + lane + 32 * q;
+      ch[lane + 32 * q] = kk < k ? col[kk] : make_double2(0.0, 0.0);
     }
+    __syncwarp();
+    const int kb = c0 + 8 * lane;
+    if (kb < half) {
+      __align__(16) __nv_bfloat16 rr[S][8], ri[S][8], nr[S][8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const double2 v = ch[8 * lane + q];
+        __nv_bfloat16 a[S], c[S];
+        slice_value<S>(v.x, e, a);
+        slice_value<S>(v.y, e, c);
+#pragma unroll
+        for (int p = 0; p < S; ++p) { rr[p][q] = a[p]; ri[p][q] = c[p]; nr[p][q] = __hneg(c[p]); }
+      }
+#pragma unroll
+      for (int p = 0; p < S; ++p) {
+        __nv_bfloat16* re_row = out + ((long long)(b * S + p) * n2 + 2LL * j) * kp;
+        __nv_bfloat16* im_row = re_row + kp;
+        *reinterpret_cast<uint4*>(re_row + kb) = *reinterpret_cast<const uint4*>(rr[p]);
+        *reinterpret_cast<uint4*>(re_row + half + kb) = *reinterpret_cast<const uint4*>(nr[p]);
+        *reinterpret_cast<uint4*>(im_row + kb) = *reinterpret_cast<const uint4*>(ri[p]);
+        *reinterpret_cast<uint4*>(im_row + half + kb) = *reinterpret_cast<const uint4*>(rr[p]);
+      }
+    }
+    __syncwarp();
   }
 }
 
@@ -266,6 +333,8 @@ struct TcArgs {
   const int* fb;           // [batch][n]
   double2* C; int ldc; long long sC;
   double2 alpha, beta;
+  int alpha_one;           // alpha == 1
+  int beta_kind;           // 0: beta == 0, 1: beta == 1, 2: general
   int* err;
 };
 
@@ -371,20 +440,25 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const bool aborted = !ok || *((volatile int*)abort_flag);
     const int e_row = (row < a.m) ? a.ea[(long long)b * a.m + row] : 0;
     double2* Cb = a.C + (long long)b * a.sC;
-    const bool beta0 = (a.beta.x == 0.0 && a.beta.y == 0.0);
 #pragma unroll 1
     for (int c0 = 0; c0 < NT; c0 += 16) {
-      double v[16];
+      // exact recombination of the diagonal accumulators (integer-valued FP32) in int64:
+      // hi = sum_{d<DH} acc_d 2^(7(DH-1-d)), lo = sum_{d>=DH} acc_d 2^(7(S-1-d))
+      constexpr int DH = S <= 5 ? S : 3;
+      long long hi[16], lo[16];
 #pragma unroll
-      for (int i = 0; i < 16; ++i) v[i] = 0.0;
+      for (int i = 0; i < 16; ++i) { hi[i] = 0; lo[i] = 0; }
       if (ok) {
 #pragma unroll
-        for (int d = S - 1; d >= 0; --d) {
+        for (int d = 0; d < S; ++d) {
           float f[16];
           tmem_ld16(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(d * NT + c0), f);
-          const double w = ldexp(1.0, -7 * d);
 #pragma unroll
-          for (int i = 0; i < 16; ++i) v[i] = fma((double)f[i], w, v[i]);
+          for (int i = 0; i < 16; ++i) {
+            const long long q = (long long)__float2ll_rn(f[i]);
+            if (d < DH) hi[i] += q * (1LL << (7 * (DH - 1 - d)));
+            else lo[i] += q * (1LL << (7 * (S - 1 - d)));
+          }
         }
       }
       if (row >= a.m || aborted) continue;
@@ -392,12 +466,18 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       for (int jj = 0; jj < 8; ++jj) {
         const int col = (tn * NT + c0) / 2 + jj;   // complex output column
         if (col >= a.n) continue;
-        const int f_col = a.fb[(long long)b * a.n + col];
-        const double sc = ldexp(1.0, e_row + f_col - 12);
-        const double2 prod = make_double2(v[2 * jj] * sc, v[2 * jj + 1] * sc);
+        const int sc = e_row + a.fb[(long long)b * a.n + col] - 12 - 7 * (S - 1);
+        double re = scaled_int_to_double(hi[2 * jj], sc + 7 * (S - DH));
+        double im = scaled_int_to_double(hi[2 * jj + 1], sc + 7 * (S - DH));
+        if (DH < S) {
+          re += scaled_int_to_double(lo[2 * jj], sc);
+          im += scaled_int_to_double(lo[2 * jj + 1], sc);
+        }
+        double2 out = make_double2(re, im);
+        if (!a.alpha_one) out = cmul(a.alpha, out);
         double2* cp = Cb + (long long)col * a.ldc + row;
-        double2 out = cmul(a.alpha, prod);
-        if (!beta0) out = cadd(out, cmul(a.beta, *cp));
+        if (a.beta_kind == 1) out = cadd(out, *cp);
+        else if (a.beta_kind == 2) out = cadd(out, cmul(a.beta, *cp));
         *cp = out;
       }
     }
@@ -461,15 +541,13 @@ int launch_mma(const SlicedOperand& A, const SlicedOperand& B, const TcArgs& arg
 
 template <int S>
 int slice_a_t(const double2* A, int lda, long long sA, int m, int k, int batch, SlicedOperand& out, cudaStream_t st) {
-  if (out.k != k)   // padded K: the pad columns of every slice row must read as zero
-    NEGF_CUDA_TRY(cudaMemsetAsync(out.data, 0, sliced_bytes(m, out.k, S, batch), st));
   cudaEvent_t ev;
   timed_begin(st, TK_SLICE, 0.0, &ev);
   dim3 g1((m + 31) / 32, batch);
   row_exp_kernel<<<g1, dim3(32, 8), 0, st>>>(A, lda, sA, m, k, out.exps);
   NEGF_CUDA_TRY(cudaGetLastError());
-  dim3 g2((m + 31) / 32, (k + 31) / 32, batch);
-  slice_a_kernel<S><<<g2, dim3(32, 8), 0, st>>>(A, lda, sA, m, k, out.exps, out.data, out.k);
+  dim3 g2((m + 31) / 32, (out.k + 63) / 64, batch);
+  slice_a_kernel<S><<<g2, 256, 0, st>>>(A, lda, sA, m, k, out.exps, out.data, out.k);
   NEGF_CUDA_TRY(cudaGetLastError());
   timed_end(st, TK_SLICE, ev);
   count_launch(2);
@@ -478,7 +556,6 @@ int slice_a_t(const double2* A, int lda, long long sA, int m, int k, int batch, 
 
 template <int S>
 int slice_b_t(const double2* B, int ldb, long long sB, int k, int n, int batch, SlicedOperand& out, cudaStream_t st) {
-  if (out.k != k) NEGF_CUDA_TRY(cudaMemsetAsync(out.data, 0, sliced_bytes(2 * n, out.k, S, batch), st));
   dim3 g((n + 7) / 8, batch);
   cudaEvent_t ev;
   timed_begin(st, TK_SLICE, 0.0, &ev);
@@ -497,7 +574,7 @@ size_t sliced_bytes(int rows, int k, int slices, int batch) {
   return sizeof(__nv_bfloat16) * (size_t)batch * slices * rows * 2 * (size_t)k;
 }
 
-int padded_k(int k) { return (k + 3) & ~3; }
+int padded_k(int k) { return (k + 7) & ~7; }   // 16-byte slice vectors and TMA rows
 
 int slice_a(const double2* A, int lda, long long sA, int m, int k, int batch, int slices, SlicedOperand& out,
             cudaStream_t st) {
@@ -535,6 +612,8 @@ int zgemm_tc(const SlicedOperand& A, const SlicedOperand& B, double2 alpha, doub
   args.ea = A.exps; args.fb = B.exps;
   args.C = C; args.ldc = ldc; args.sC = sC;
   args.alpha = alpha; args.beta = beta; args.err = err;
+  args.alpha_one = (alpha.x == 1.0 && alpha.y == 0.0) ? 1 : 0;
+  args.beta_kind = (beta.x == 0.0 && beta.y == 0.0) ? 0 : (beta.x == 1.0 && beta.y == 0.0) ? 1 : 2;
   switch (A.slices) {
     case 3: return launch_mma<3, 128>(A, B, args, st);
     case 4: return launch_mma<4, 128>(A, B, args, st);
