@@ -234,6 +234,7 @@ def main():
     ap.add_argument("--form", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--batch", type=int, default=16)
     ap.add_argument("--slices", type=int, default=0, help="mixed form: BF16 slices of the RGF products (0 = default)")
+    ap.add_argument("--residual-slices", type=int, default=0, help="mixed form: slices of the Newton-Schulz residual")
     ap.add_argument("--fp64-steps", type=int, default=1,
                     help="mixed form: timed FP64 steps on the same requests (T error and FP64 rate)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -259,7 +260,8 @@ def main():
     hams = build_hamiltonians()
     m = 4 * NPY * NPZ
     solver = Solver(NPX, NPY, NPZ, n_hamiltonians=SEEDS, max_batch=args.batch, eta=ETA, sr_tol=SR_TOL,
-                    calc_spin=True, precision=args.form, device=local_rank, mixed_slices=args.slices)
+                    calc_spin=True, precision=args.form, device=local_rank, mixed_slices=args.slices,
+                    residual_slices=args.residual_slices)
     stream = torch.cuda.Stream(dev)          # a real stream handle, so events bracket the work
     torch.cuda.set_stream(stream)
     solver.set_stream(stream.cuda_stream)

@@ -113,6 +113,10 @@ int Engine::init(const negf_params& p) {
   keep_columns_ = p.keep_g_columns != 0;
   mixed_ = p.precision == NEGF_PREC_MIXED;
   if (mixed_ && p.mixed_slices != 0) s_rgf_ = p.mixed_slices;
+  if (mixed_ && p.residual_slices != 0) {
+    if (p.residual_slices != 5 && p.residual_slices != 7 && p.residual_slices != 6) return NEGF_EINVAL;
+    s_res_ = p.residual_slices;
+  }
   NEGF_CUDA_TRY(cudaSetDevice(p.device));
   NEGF_CUDA_TRY(cudaStreamCreateWithFlags(&own_st_, cudaStreamNonBlocking));
   st_ = own_st_;

@@ -315,7 +315,7 @@ struct TcCfg {
   static constexpr int B_TILE = NT * ROW_BYTES;                // bytes of one B slice tile
   static constexpr int STAGE = S * (A_TILE + B_TILE);
   static constexpr int STAGES = (200 * 1024) / STAGE > 4 ? 4 : (200 * 1024) / STAGE;
-  static constexpr int SMEM = STAGES * STAGE + 1024 + 256;     // + alignment + barriers
+  static constexpr int SMEM = STAGES * STAGE + 1024 + 256 + 4 * (NT / 2);   // + alignment, barriers, exponents
   static constexpr int TMEM_COLS_USED = S * NT;
   static constexpr int TMEM_COLS = TMEM_COLS_USED <= 32 ? 32 : TMEM_COLS_USED <= 64 ? 64
                                  : TMEM_COLS_USED <= 128 ? 128 : TMEM_COLS_USED <= 256 ? 256 : 512;
@@ -349,6 +349,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   uint64_t* done = empty + Cfg::STAGES;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
   int* abort_flag = reinterpret_cast<int*>(tmem_slot + 1);
+  int* col_exp = abort_flag + 1;   // NT/2 column exponents of this tile
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int tm = blockIdx.x, tn = blockIdx.y, b = blockIdx.z;
@@ -372,6 +373,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 
   if (warp == 0) {
     if (lane == 0) {
+      asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&mapA)) : "memory");
+      asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&mapB)) : "memory");
       // ---- TMA producer
       const int a_row0 = tm * TILE_M;
       const int b_row0 = tn * NT;
@@ -431,8 +434,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       tc_commit(done);
     }
   } else {
-    // ---- epilogue: warps 2..5 -> TMEM lane quarter (warp % 4)
+    // ---- epilogue: warps 2..5 -> TMEM lane quarter (warp % 4).  While the MMAs run,
+    // stage this tile's column exponents in shared memory.
     const int quarter = warp & 3;
+    for (int c = threadIdx.x - 64; c < NT / 2; c += 128) {
+      const int col = tn * (NT / 2) + c;
+      col_exp[c] = col < a.n ? a.fb[(long long)b * a.n + col] : 0;
+    }
+    asm volatile("bar.sync 1, 128;" ::: "memory");   // the four epilogue warps only
     const bool ok = mbar_wait(done, 0);
     if (!ok && a.err) atomicCAS(a.err, 0, 3);
     tc_fence_after();
@@ -444,7 +453,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     for (int c0 = 0; c0 < NT; c0 += 16) {
       // exact recombination of the diagonal accumulators (integer-valued FP32) in int64:
       // hi = sum_{d<DH} acc_d 2^(7(DH-1-d)), lo = sum_{d>=DH} acc_d 2^(7(S-1-d))
-      constexpr int DH = S <= 5 ? S : 3;
+      constexpr int DH = S <= 6 ? S : 3;   // S <= 6 fits one int64; S = 7 splits
       long long hi[16], lo[16];
 #pragma unroll
       for (int i = 0; i < 16; ++i) { hi[i] = 0; lo[i] = 0; }
@@ -462,11 +471,18 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         }
       }
       if (row >= a.m || aborted) continue;
+      const int col0 = (tn * NT + c0) / 2;   // first complex output column of this chunk
+      double2 cin[8];
+      if (a.beta_kind != 0) {                // issue all loads of the chunk before any store
+#pragma unroll
+        for (int jj = 0; jj < 8; ++jj)
+          cin[jj] = (col0 + jj < a.n) ? Cb[(long long)(col0 + jj) * a.ldc + row] : make_double2(0.0, 0.0);
+      }
 #pragma unroll
       for (int jj = 0; jj < 8; ++jj) {
-        const int col = (tn * NT + c0) / 2 + jj;   // complex output column
+        const int col = col0 + jj;
         if (col >= a.n) continue;
-        const int sc = e_row + a.fb[(long long)b * a.n + col] - 12 - 7 * (S - 1);
+        const int sc = e_row + col_exp[c0 / 2 + jj] - 12 - 7 * (S - 1);
         double re = scaled_int_to_double(hi[2 * jj], sc + 7 * (S - DH));
         double im = scaled_int_to_double(hi[2 * jj + 1], sc + 7 * (S - DH));
         if (DH < S) {
@@ -475,10 +491,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         }
         double2 out = make_double2(re, im);
         if (!a.alpha_one) out = cmul(a.alpha, out);
-        double2* cp = Cb + (long long)col * a.ldc + row;
-        if (a.beta_kind == 1) out = cadd(out, *cp);
-        else if (a.beta_kind == 2) out = cadd(out, cmul(a.beta, *cp));
-        *cp = out;
+        if (a.beta_kind == 1) out = cadd(out, cin[jj]);
+        else if (a.beta_kind == 2) out = cadd(out, cmul(a.beta, cin[jj]));
+        Cb[(long long)col * a.ldc + row] = out;
       }
     }
   }
@@ -568,7 +583,7 @@ int slice_b_t(const double2* B, int ldb, long long sB, int k, int n, int batch, 
 
 }  // namespace
 
-bool tc_supported_slices(int s) { return s == 3 || s == 4 || s == 5 || s == 7; }
+bool tc_supported_slices(int s) { return s == 3 || s == 4 || s == 5 || s == 6 || s == 7; }
 
 size_t sliced_bytes(int rows, int k, int slices, int batch) {
   return sizeof(__nv_bfloat16) * (size_t)batch * slices * rows * 2 * (size_t)k;
@@ -583,6 +598,7 @@ int slice_a(const double2* A, int lda, long long sA, int m, int k, int batch, in
     case 3: return slice_a_t<3>(A, lda, sA, m, k, batch, out, st);
     case 4: return slice_a_t<4>(A, lda, sA, m, k, batch, out, st);
     case 5: return slice_a_t<5>(A, lda, sA, m, k, batch, out, st);
+    case 6: return slice_a_t<6>(A, lda, sA, m, k, batch, out, st);
     case 7: return slice_a_t<7>(A, lda, sA, m, k, batch, out, st);
   }
   return NEGF_EINVAL;
@@ -595,6 +611,7 @@ int slice_b(const double2* B, int ldb, long long sB, int k, int n, int batch, in
     case 3: return slice_b_t<3>(B, ldb, sB, k, n, batch, out, st);
     case 4: return slice_b_t<4>(B, ldb, sB, k, n, batch, out, st);
     case 5: return slice_b_t<5>(B, ldb, sB, k, n, batch, out, st);
+    case 6: return slice_b_t<6>(B, ldb, sB, k, n, batch, out, st);
     case 7: return slice_b_t<7>(B, ldb, sB, k, n, batch, out, st);
   }
   return NEGF_EINVAL;
@@ -618,6 +635,7 @@ int zgemm_tc(const SlicedOperand& A, const SlicedOperand& B, double2 alpha, doub
     case 3: return launch_mma<3, 128>(A, B, args, st);
     case 4: return launch_mma<4, 128>(A, B, args, st);
     case 5: return launch_mma<5, 64>(A, B, args, st);
+    case 6: return launch_mma<6, 64>(A, B, args, st);
     case 7: return launch_mma<7, 64>(A, B, args, st);
   }
   return NEGF_EINVAL;
