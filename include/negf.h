@@ -73,7 +73,7 @@ typedef struct negf_params {
     int32_t keep_g_columns;  /* 1: keep G(:,1), G(:,N) of the per-energy call for
                                 negf_copy_g_columns (2*Npx*M^2*16 extra device bytes)    */
     int32_t residual_slices; /* NEGF_PREC_MIXED: slices of the Newton-Schulz residual W X
-                                (0 = default 7; 5..7 allowed)                            */
+                                (0 = default 8; 5..8 allowed)                            */
     int32_t reserved[5];     /* must be zero                                             */
     double  spin_ops[3][4][4][2]; /* gMx, gMy, gMz (row-major [row][col][re,im]) used by
                                      the spin reduction, Source/Read_In_Allocate.F90:183-196;
@@ -260,9 +260,9 @@ NEGF_API int negf_server_destroy(negf_server* s);
 
 /* zgemm('N','N', m, n, k, alpha, A, lda, B, ldb, beta, C, ldc) as called throughout
  * Source/Recursive_Greens.F90 and Source/Contact_Self_Energy.F90.  slices = 0 runs the
- * FP64 DFMA kernel; slices in {3, 4, 5, 7} runs the tcgen05 tensor-core kernel on exact
+ * FP64 DFMA kernel; slices in 3..8 runs the tcgen05 tensor-core kernel on exact
  * 7-bit integer BF16 slices of row/column-scaled operands (truncation <= 2^(-7*slices)
- * of max|A_i.| max|B_.j| per term; 7 slices is FP64-class).  NEGF_ETIMEDOUT if a
+ * of max|A_i.| max|B_.j| per term; 7-8 slices is FP64-class).  NEGF_ETIMEDOUT if a
  * bounded device wait expired.                                                          */
 NEGF_API int negf_zgemm(int32_t slices, int32_t m, int32_t n, int32_t k, const double* alpha,
                         const double* A, int32_t lda, const double* B, int32_t ldb,

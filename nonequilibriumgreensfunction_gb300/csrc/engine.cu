@@ -114,7 +114,7 @@ int Engine::init(const negf_params& p) {
   mixed_ = p.precision == NEGF_PREC_MIXED;
   if (mixed_ && p.mixed_slices != 0) s_rgf_ = p.mixed_slices;
   if (mixed_ && p.residual_slices != 0) {
-    if (p.residual_slices != 5 && p.residual_slices != 7 && p.residual_slices != 6) return NEGF_EINVAL;
+    if (p.residual_slices < 5 || p.residual_slices > 8) return NEGF_EINVAL;
     s_res_ = p.residual_slices;
   }
   NEGF_CUDA_TRY(cudaSetDevice(p.device));
@@ -327,14 +327,31 @@ int Engine::invert_impl(double2* A, long long sA, int batch, int* status_dev) {
   NEGF_CUDA_TRY(cudaMemcpyAsync(info32.data(), inv_.info, sizeof(int) * batch, cudaMemcpyDeviceToHost, st_));
   NEGF_CUDA_TRY(cudaMemsetAsync(dRnorm_, 0, sizeof(unsigned long long) * batch, st_));
   NEGF_TRY(slice_a(dWinv_, M_, MM_, M_, M_, batch, s_res_, sw_, st_));
-  std::vector<unsigned long long> r0(batch);
-  for (int step = 0; step < ns_steps_; ++step) {
+  std::vector<unsigned long long> r0(batch), rk(batch);
+  for (int step = 0; step < ns_max_steps_; ++step) {
     if (step > 0) NEGF_CUDA_TRY(cudaMemsetAsync(dRnorm_, 0, sizeof(unsigned long long) * batch, st_));
     NEGF_TRY(slice_b(A, M_, sA, M_, M_, batch, s_res_, sb_, st_));
     NEGF_TRY(zgemm_tc(sw_, sb_, one, zero, dT_, M_, MM_, dTcErr_, st_));          // T = W X
     NEGF_TRY(ns_residual(M_, batch, dT_, MM_, dRnorm_, st_));                     // R = I - T
     if (step == 0)
       NEGF_CUDA_TRY(cudaMemcpyAsync(r0.data(), dRnorm_, sizeof(unsigned long long) * batch, cudaMemcpyDeviceToHost, st_));
+    if (step + 1 >= ns_steps_) {
+      // R_{k+1} = R_k^2: after this update the residual is at most |R_k|^2; stop if that is
+      // small for every matrix that is not going to be redone in FP64
+      NEGF_CUDA_TRY(cudaMemcpyAsync(rk.data(), dRnorm_, sizeof(unsigned long long) * batch, cudaMemcpyDeviceToHost, st_));
+      NEGF_CUDA_TRY(cudaStreamSynchronize(st_));
+      double worst_k = 0.0;
+      for (int b = 0; b < batch; ++b) {
+        const double r = __longlong_as_double_host(r0[b]);
+        if (info32[b] != 0 || !(r <= ns_accept_)) continue;
+        worst_k = std::max(worst_k, __longlong_as_double_host(rk[b]));
+      }
+      NEGF_TRY(slice_a(A, M_, sA, M_, M_, batch, s_upd_, sa_, st_));
+      NEGF_TRY(slice_b(dT_, M_, MM_, M_, M_, batch, s_upd_, sb_, st_));
+      NEGF_TRY(zgemm_tc(sa_, sb_, one, one, A, M_, sA, dTcErr_, st_));            // X += X R
+      if (worst_k <= ns_tol_) break;
+      continue;
+    }
     NEGF_TRY(slice_a(A, M_, sA, M_, M_, batch, s_upd_, sa_, st_));
     NEGF_TRY(slice_b(dT_, M_, MM_, M_, M_, batch, s_upd_, sb_, st_));
     NEGF_TRY(zgemm_tc(sa_, sb_, one, one, A, M_, sA, dTcErr_, st_));              // X += X R

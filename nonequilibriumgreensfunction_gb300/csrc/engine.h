@@ -97,9 +97,11 @@ class Engine {
   bool mixed_ = false;
   int s_rgf_ = 5;      // RGF block products
   int s_sr_ = 7;       // Sancho-Rubio products (FP64-class)
-  int s_res_ = 7;      // Newton-Schulz residual W X (FP64-class)
+  int s_res_ = 8;      // Newton-Schulz residual W X (2^-56, beyond FP64 rounding of the inputs)
   int s_upd_ = 4;      // Newton-Schulz update X R (R is small)
-  int ns_steps_ = 2;
+  int ns_steps_ = 2;        // Newton-Schulz steps always taken
+  int ns_max_steps_ = 4;    // more while the latest residual norm is above ns_tol_
+  double ns_tol_ = 1e-6;
   double ns_accept_ = 0.5;   // first residual norm above this -> FP64 inverse for that matrix
   int cur_slices_ = 4;       // slices for the GEMMs issued now (set per phase)
   double2* dWinv_ = nullptr; // copy of the matrix being inverted (FP64)

@@ -141,6 +141,16 @@ __device__ __forceinline__ double scaled_int_to_double(long long v, int scale) {
   return __longlong_as_double((long long)(sign | ((unsigned long long)ex << 52) | (mant & ((1ULL << 52) - 1))));
 }
 
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
+  uint32_t r[8];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+}
+
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
   uint32_t r[16];
   asm volatile(
@@ -449,21 +459,23 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const bool aborted = !ok || *((volatile int*)abort_flag);
     const int e_row = (row < a.m) ? a.ea[(long long)b * a.m + row] : 0;
     double2* Cb = a.C + (long long)b * a.sC;
+    constexpr int CW = S >= 7 ? 8 : 16;      // fp32 columns per chunk (register budget)
 #pragma unroll 1
-    for (int c0 = 0; c0 < NT; c0 += 16) {
+    for (int c0 = 0; c0 < NT; c0 += CW) {
       // exact recombination of the diagonal accumulators (integer-valued FP32) in int64:
       // hi = sum_{d<DH} acc_d 2^(7(DH-1-d)), lo = sum_{d>=DH} acc_d 2^(7(S-1-d))
-      constexpr int DH = S <= 6 ? S : 3;   // S <= 6 fits one int64; S = 7 splits
-      long long hi[16], lo[16];
+      constexpr int DH = S <= 6 ? S : 3;   // S <= 6 fits one int64; S >= 7 splits
+      long long hi[CW], lo[CW];
 #pragma unroll
-      for (int i = 0; i < 16; ++i) { hi[i] = 0; lo[i] = 0; }
+      for (int i = 0; i < CW; ++i) { hi[i] = 0; lo[i] = 0; }
       if (ok) {
 #pragma unroll
         for (int d = 0; d < S; ++d) {
-          float f[16];
-          tmem_ld16(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(d * NT + c0), f);
+          float f[CW];
+          const uint32_t ta = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(d * NT + c0);
+          if constexpr (CW == 16) tmem_ld16(ta, f); else tmem_ld8(ta, f);
 #pragma unroll
-          for (int i = 0; i < 16; ++i) {
+          for (int i = 0; i < CW; ++i) {
             const long long q = (long long)__float2ll_rn(f[i]);
             if (d < DH) hi[i] += q * (1LL << (7 * (DH - 1 - d)));
             else lo[i] += q * (1LL << (7 * (S - 1 - d)));
@@ -472,14 +484,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       }
       if (row >= a.m || aborted) continue;
       const int col0 = (tn * NT + c0) / 2;   // first complex output column of this chunk
-      double2 cin[8];
+      double2 cin[CW / 2];
       if (a.beta_kind != 0) {                // issue all loads of the chunk before any store
 #pragma unroll
-        for (int jj = 0; jj < 8; ++jj)
+        for (int jj = 0; jj < CW / 2; ++jj)
           cin[jj] = (col0 + jj < a.n) ? Cb[(long long)(col0 + jj) * a.ldc + row] : make_double2(0.0, 0.0);
       }
 #pragma unroll
-      for (int jj = 0; jj < 8; ++jj) {
+      for (int jj = 0; jj < CW / 2; ++jj) {
         const int col = col0 + jj;
         if (col >= a.n) continue;
         const int sc = e_row + col_exp[c0 / 2 + jj] - 12 - 7 * (S - 1);
@@ -583,7 +595,7 @@ int slice_b_t(const double2* B, int ldb, long long sB, int k, int n, int batch, 
 
 }  // namespace
 
-bool tc_supported_slices(int s) { return s == 3 || s == 4 || s == 5 || s == 6 || s == 7; }
+bool tc_supported_slices(int s) { return s >= 3 && s <= 8; }
 
 size_t sliced_bytes(int rows, int k, int slices, int batch) {
   return sizeof(__nv_bfloat16) * (size_t)batch * slices * rows * 2 * (size_t)k;
@@ -600,6 +612,7 @@ int slice_a(const double2* A, int lda, long long sA, int m, int k, int batch, in
     case 5: return slice_a_t<5>(A, lda, sA, m, k, batch, out, st);
     case 6: return slice_a_t<6>(A, lda, sA, m, k, batch, out, st);
     case 7: return slice_a_t<7>(A, lda, sA, m, k, batch, out, st);
+    case 8: return slice_a_t<8>(A, lda, sA, m, k, batch, out, st);
   }
   return NEGF_EINVAL;
 }
@@ -613,6 +626,7 @@ int slice_b(const double2* B, int ldb, long long sB, int k, int n, int batch, in
     case 5: return slice_b_t<5>(B, ldb, sB, k, n, batch, out, st);
     case 6: return slice_b_t<6>(B, ldb, sB, k, n, batch, out, st);
     case 7: return slice_b_t<7>(B, ldb, sB, k, n, batch, out, st);
+    case 8: return slice_b_t<8>(B, ldb, sB, k, n, batch, out, st);
   }
   return NEGF_EINVAL;
 }
@@ -637,6 +651,7 @@ int zgemm_tc(const SlicedOperand& A, const SlicedOperand& B, double2 alpha, doub
     case 5: return launch_mma<5, 64>(A, B, args, st);
     case 6: return launch_mma<6, 64>(A, B, args, st);
     case 7: return launch_mma<7, 64>(A, B, args, st);
+    case 8: return launch_mma<8, 64>(A, B, args, st);
   }
   return NEGF_EINVAL;
 }

@@ -27,7 +27,7 @@ def _bound(A, B, S):
 
 
 @pytest.mark.parametrize("shape", [(64, 64, 64), (37, 53, 12), (130, 200, 256), (400, 400, 400)])
-@pytest.mark.parametrize("S", [3, 4, 5, 6, 7])
+@pytest.mark.parametrize("S", [3, 4, 5, 6, 7, 8])
 def test_sliced_gemm_error_bound(need_gpu, shape, S):
     rng = np.random.default_rng(S * 1000 + shape[0])
     m, n, k = shape
