@@ -167,7 +167,7 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
 // slicing
 // ---------------------------------------------------------------------------------
 // Slices of x at scale exponent e (|x| < 2^e): the fixed-point integer
-// F = round(x 2^(6 + 7(S-1) - e)), |F| <= 2^(6 + 7(S-1)) <= 2^48, built from the bits of x
+// F = round(x 2^(6 + 7(S-1) - e)), |F| <= 2^(6 + 7(S-1)) <= 2^55, built from the bits of x
 // with integer operations only (GB300's FP64 pipe is 1/64 of its FP32 rate), then written
 // as balanced base-128 digits: F = sum_p s_p 128^(S-1-p), lower digits in [-64, 63], the
 // top digit in [-64, 64].  Every digit is exact in BF16; the truncation is <= 2^-7S of 2^e.
@@ -178,8 +178,9 @@ __device__ __forceinline__ void slice_value(double x, int e, __nv_bfloat16 (&out
   long long F = 0;
   if (ex != 0 && ex != 0x7FF) {                      // zero and subnormals slice to 0
     const unsigned long long m = (bits & ((1ULL << 52) - 1)) | (1ULL << 52);   // x = m 2^(ex - 1075)
-    const int r = e - (ex - 1075) - (6 + 7 * (S - 1));                          // F = m 2^-r, r >= 5
-    if (r < 64) F = (long long)((m + (1ULL << (r - 1))) >> r);
+    const int r = e - (ex - 1075) - (6 + 7 * (S - 1));                          // F = m 2^-r, r >= 46 - 7(S-1)
+    if (r <= 0) F = (long long)(m << (-r));                                      // S = 8: exact, |F| < 2^55
+    else if (r < 64) F = (long long)((m + (1ULL << (r - 1))) >> r);
     if (bits >> 63) F = -F;
   }
 #pragma unroll
