@@ -235,6 +235,7 @@ def main():
     ap.add_argument("--batch", type=int, default=16)
     ap.add_argument("--slices", type=int, default=0, help="mixed form: BF16 slices of the RGF products (0 = default)")
     ap.add_argument("--residual-slices", type=int, default=0, help="mixed form: slices of the Newton-Schulz residual")
+    ap.add_argument("--sr-slices", type=int, default=0, help="mixed form: slices of the Sancho-Rubio products")
     ap.add_argument("--fp64-steps", type=int, default=1,
                     help="mixed form: timed FP64 steps on the same requests (T error and FP64 rate)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -261,7 +262,7 @@ def main():
     m = 4 * NPY * NPZ
     solver = Solver(NPX, NPY, NPZ, n_hamiltonians=SEEDS, max_batch=args.batch, eta=ETA, sr_tol=SR_TOL,
                     calc_spin=True, precision=args.form, device=local_rank, mixed_slices=args.slices,
-                    residual_slices=args.residual_slices)
+                    residual_slices=args.residual_slices, sr_slices=args.sr_slices)
     stream = torch.cuda.Stream(dev)          # a real stream handle, so events bracket the work
     torch.cuda.set_stream(stream)
     solver.set_stream(stream.cuda_stream)
@@ -362,11 +363,18 @@ def main():
         torch.cuda.synchronize()
         el64 = ev4.elapsed_time(ev5) * 1e-3
         t_err = 0.0
-        for a, b in zip(timed_results[:n_fp], outs):
-            t_err = max(t_err, float(np.max(np.abs(a["T12"] - b["T12"]) / np.maximum(np.abs(b["T12"]), 1e-3))))
+        worst = []
+        for s_i, (a, b) in enumerate(zip(timed_results[:n_fp], outs)):
+            rel = np.abs(a["T12"] - b["T12"]) / np.maximum(np.abs(b["T12"]), 1e-3)
+            t_err = max(t_err, float(np.max(rel)))
+            e_s, _, _, sl_s = step_requests(args.warmup + s_i, args.batch, rank, world)
+            for i in np.argsort(rel)[-3:]:
+                worst.append((float(rel[i]), float(e_s[i]), int(sl_s[i]), float(b["T12"][i]), float(a["T12"][i])))
+        worst = sorted(worst)[-3:]
         fp64 = {"value": args.batch * n_fp / el64, "unit": "solves/s", "steps": n_fp,
                 "t_rel_err_max": t_err, "t_err_gate": 1e-6, "gate_ok": t_err <= 1e-6,
-                "t_err_floor": "denominator max(|T_fp64|, 1e-3)"}
+                "t_err_floor": "denominator max(|T_fp64|, 1e-3)",
+                "worst": [{"rel": w[0], "E": w[1], "seed": w[2], "T_fp64": w[3], "T_mixed": w[4]} for w in worst]}
         ref.close()
         solver = None
         st = st_mixed

@@ -47,7 +47,7 @@ class NegfParams(ctypes.Structure):
         ("eta", c_double), ("sr_tol", c_double),
         ("sr_max_iter", c_int32), ("calc_spin", c_int32), ("precision", c_int32),
         ("device", c_int32), ("mixed_slices", c_int32), ("keep_g_columns", c_int32),
-        ("residual_slices", c_int32), ("reserved", c_int32 * 5),
+        ("residual_slices", c_int32), ("sr_slices", c_int32), ("reserved", c_int32 * 4),
         ("spin_ops", c_double * (3 * 4 * 4 * 2)),
     ]
 

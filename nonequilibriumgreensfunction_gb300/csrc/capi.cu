@@ -99,7 +99,7 @@ extern "C" {
 int negf_create(const negf_params* p, negf_handle** out) {
   if (!p || !out) return NEGF_EINVAL;
   *out = nullptr;
-  for (int i = 0; i < 5; ++i)
+  for (int i = 0; i < 4; ++i)
     if (p->reserved[i] != 0) return NEGF_EINVAL;
   negf_handle* h = new (std::nothrow) negf_handle();
   if (!h) return NEGF_ENOMEM;

@@ -113,6 +113,10 @@ int Engine::init(const negf_params& p) {
   keep_columns_ = p.keep_g_columns != 0;
   mixed_ = p.precision == NEGF_PREC_MIXED;
   if (mixed_ && p.mixed_slices != 0) s_rgf_ = p.mixed_slices;
+  if (mixed_ && p.sr_slices != 0) {
+    if (p.sr_slices < 5 || p.sr_slices > 8) return NEGF_EINVAL;
+    s_sr_ = p.sr_slices;
+  }
   if (mixed_ && p.residual_slices != 0) {
     if (p.residual_slices < 5 || p.residual_slices > 8) return NEGF_EINVAL;
     s_res_ = p.residual_slices;

@@ -44,7 +44,7 @@ def _to_fortran_blocks(htotd):
 class Solver:
     def __init__(self, npx, npy, npz, norb=4, n_hamiltonians=1, max_batch=1, eta=1e-4, sr_tol=1e-8,
                  sr_max_iter=20000, calc_spin=False, precision="fp64", device=0, keep_g_columns=False,
-                 spin_ops=None, mixed_slices=0, residual_slices=0):
+                 spin_ops=None, mixed_slices=0, residual_slices=0, sr_slices=0):
         self.lib = capi.load()
         p = NegfParams()
         p.npx, p.npy, p.npz, p.norb = npx, npy, npz, norb
@@ -55,6 +55,7 @@ class Solver:
         p.device = device
         p.mixed_slices = mixed_slices
         p.residual_slices = residual_slices
+        p.sr_slices = sr_slices
         p.keep_g_columns = 1 if keep_g_columns else 0
         if spin_ops is not None:
             ops = np.asarray(spin_ops, dtype=np.complex128)
