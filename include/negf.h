@@ -73,9 +73,9 @@ typedef struct negf_params {
     int32_t keep_g_columns;  /* 1: keep G(:,1), G(:,N) of the per-energy call for
                                 negf_copy_g_columns (2*Npx*M^2*16 extra device bytes)    */
     int32_t residual_slices; /* NEGF_PREC_MIXED: slices of the Newton-Schulz residual W X
-                                (0 = default 8; 5..8 allowed)                            */
+                                (0 = default 7; 5..8 allowed)                            */
     int32_t sr_slices;       /* NEGF_PREC_MIXED: slices of the Sancho-Rubio products
-                                (0 = default; 5..8 allowed)                              */
+                                (0 = default 8; 5..8 allowed)                            */
     int32_t reserved[4];     /* must be zero                                             */
     double  spin_ops[3][4][4][2]; /* gMx, gMy, gMz (row-major [row][col][re,im]) used by
                                      the spin reduction, Source/Read_In_Allocate.F90:183-196;

@@ -96,8 +96,8 @@ class Engine {
   // FP32 Gauss-Jordan + Newton-Schulz steps with the residual at s_res_ slices
   bool mixed_ = false;
   int s_rgf_ = 5;      // RGF block products
-  int s_sr_ = 7;       // Sancho-Rubio products (FP64-class)
-  int s_res_ = 8;      // Newton-Schulz residual W X (2^-56, beyond FP64 rounding of the inputs)
+  int s_sr_ = 8;       // Sancho-Rubio products: 2^-56, the decimation is ill-conditioned near band edges
+  int s_res_ = 7;      // Newton-Schulz residual W X (2^-49, FP64-class)
   int s_upd_ = 4;      // Newton-Schulz update X R (R is small)
   int ns_steps_ = 2;        // Newton-Schulz steps always taken
   int ns_max_steps_ = 4;    // more while the latest residual norm is above ns_tol_
