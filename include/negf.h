@@ -53,6 +53,7 @@ extern "C" {
 #define NEGF_EREFINE      (-9)   /* mixed form: refinement residual above bound          */
 #define NEGF_ENODEV      (-10)   /* no CUDA device                                       */
 #define NEGF_ENOHAM      (-11)   /* Hamiltonian slot never set                           */
+#define NEGF_ESCRATCH    (-12)   /* negf_zgemm_noalloc: sizes exceed its static scratch  */
 
 /* ---- arithmetic form ------------------------------------------------------------- */
 #define NEGF_PREC_FP64     0     /* plain FP64 complex throughout                        */
@@ -273,6 +274,25 @@ NEGF_API int negf_zgemm(int32_t slices, int32_t m, int32_t n, int32_t k, const d
 /* Invert_Matrix(invG, G, N, errorFlag) (Source/MKL_Routines_Cluster.F90:2-33): returns
  * the LAPACK INFO of the first singular matrix, 0 if all are invertible.               */
 NEGF_API int negf_zinv(int32_t n, const double* G, double* invG, int32_t batch);
+
+/* negf_zgemm_noalloc: no counterpart in the reference.  The tensor-core sliced GEMM of
+ * negf_zgemm (C = alpha A B + beta C, one matrix, slices 3..8) on DEVICE arrays, for
+ * callers that must not allocate device memory: code whose device memory is owned by
+ * another allocator (a framework pool, a serving process with a fixed HBM budget) and
+ * latency-critical loops that cannot absorb the device-wide synchronisation of
+ * cudaMalloc/cudaFree.  It calls no allocating routine; its scratch is one static device
+ * array of NEGF_NOALLOC_SCRATCH_BYTES that every GPU loading the library holds until
+ * exit, which limits m, n, k to NEGF_NOALLOC_MAX_DIM (larger sizes: NEGF_ESCRATCH).
+ * The first call on each device looks up the array's device address (make it before any
+ * stream capture).  All calls share the scratch: calls that overlap on the GPU race, so
+ * the caller must order them.  Runs on `stream` (cudaStream_t, NULL = default stream) and
+ * returns after the product is complete.                                               */
+#define NEGF_NOALLOC_MAX_DIM      512
+#define NEGF_NOALLOC_MAX_SLICES   8
+#define NEGF_NOALLOC_SCRATCH_BYTES (26u * 1024u * 1024u)
+NEGF_API int negf_zgemm_noalloc(int32_t slices, int32_t m, int32_t n, int32_t k, const double* alpha,
+                                const double* A, int32_t lda, const double* B, int32_t ldb,
+                                const double* beta, double* C, int32_t ldc, void* stream);
 
 #ifdef __cplusplus
 }

@@ -24,6 +24,7 @@ NEGF_ETIMEDOUT = -8
 NEGF_EREFINE = -9
 NEGF_ENODEV = -10
 NEGF_ENOHAM = -11
+NEGF_ESCRATCH = -12
 
 NEGF_PREC_FP64 = 0
 NEGF_PREC_MIXED = 1
@@ -34,7 +35,7 @@ EXPORTED_SYMBOLS = (
     "negf_set_stream", "negf_profile", "negf_get_stats",
     "negf_set_hamiltonian", "negf_contact_self_energy", "negf_get_retarded_greens",
     "negf_copy_g_columns", "negf_calculate_gnp", "negf_calculate_observables",
-    "negf_solve_batch", "negf_zgemm", "negf_zinv",
+    "negf_solve_batch", "negf_zgemm", "negf_zinv", "negf_zgemm_noalloc",
     "negf_server_create", "negf_server_submit", "negf_server_poll", "negf_server_wait",
     "negf_server_clock", "negf_server_destroy",
 )
@@ -121,6 +122,8 @@ def _declare(lib):
         "negf_zgemm": (c_int, [c_int32, c_int32, c_int32, c_int32, _dp, _dp, c_int32, _dp, c_int32, _dp, _dp,
                                c_int32, c_int32]),
         "negf_zinv": (c_int, [c_int32, _dp, _dp, c_int32]),
+        "negf_zgemm_noalloc": (c_int, [c_int32, c_int32, c_int32, c_int32, _dp, c_void_p, c_int32, c_void_p, c_int32,
+                                       _dp, c_void_p, c_int32, c_void_p]),
         "negf_server_create": (c_int, [POINTER(NegfServeParams), POINTER(c_void_p)]),
         "negf_server_submit": (c_int, [h, POINTER(NegfWireRequest), POINTER(c_int64)]),
         "negf_server_poll": (c_int, [h, c_int64, POINTER(NegfWireStatus), _dp, _dp, c_int32]),

@@ -132,6 +132,7 @@ const char* negf_strerror(int code) {
     case NEGF_EREFINE: return "refinement residual above bound";
     case NEGF_ENODEV: return "no CUDA device";
     case NEGF_ENOHAM: return "Hamiltonian slot not set";
+    case NEGF_ESCRATCH: return "sizes exceed the static scratch of negf_zgemm_noalloc (m, n, k <= 512)";
     default: return "unknown error";
   }
 }
