@@ -323,8 +323,7 @@ int Engine::invert_impl(double2* A, long long sA, int batch, int* status_dev) {
     return merge_info_kernel_launch(batch, inv_.info, status_dev, st_);
   }
   const double2 one = make_double2(1, 0), zero = make_double2(0, 0);
-  NEGF_TRY(copy_blocks(M_, batch, A, sA, dWinv_, MM_, st_));
-  NEGF_TRY(to_f32(M_, batch, A, sA, dW32_, MM_, st_));
+  NEGF_TRY(split_copy(M_, batch, A, sA, dWinv_, MM_, dW32_, MM_, st_));
   NEGF_TRY(cinv_f32(dW32_, MM_, M_, batch, inv_, st_));
   NEGF_TRY(to_f64(M_, batch, dW32_, MM_, A, sA, st_));
   std::vector<int> info32(batch);

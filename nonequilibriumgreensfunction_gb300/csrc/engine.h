@@ -98,7 +98,7 @@ class Engine {
   int s_rgf_ = 5;      // RGF block products
   int s_sr_ = 8;       // Sancho-Rubio products: 2^-56, the decimation is ill-conditioned near band edges
   int s_res_ = 7;      // Newton-Schulz residual W X (2^-49, FP64-class)
-  int s_upd_ = 4;      // Newton-Schulz update X R (R is small)
+  int s_upd_ = 3;      // Newton-Schulz update X R (R is small: 2^-21 of it is below the target)
   int ns_steps_ = 2;        // Newton-Schulz steps always taken
   int ns_max_steps_ = 4;    // more while the latest residual norm is above ns_tol_
   double ns_tol_ = 1e-6;

@@ -259,6 +259,8 @@ int reduce_sites(int batch, int nsite_total, int nslots, const Item* items, cons
 // rnorm[b] = atomic max of the row-sum norm of R as the bit pattern of a double
 int to_f32(int n, int batch, const double2* src, long long sS, float2* dst, long long sD, cudaStream_t st);
 int to_f64(int n, int batch, const float2* src, long long sS, double2* dst, long long sD, cudaStream_t st);
+int split_copy(int n, int batch, const double2* src, long long sS, double2* d64, long long s64, float2* d32,
+               long long s32, cudaStream_t st);
 int ns_residual(int n, int batch, double2* T, long long sT, unsigned long long* rnorm, cudaStream_t st);
 
 }  // namespace negf

@@ -506,6 +506,21 @@ __global__ void to_f32_kernel(int n, const double2* src, long long sS, float2* d
     d[e] = make_float2((float)s[e].x, (float)s[e].y);
 }
 
+// one read of the matrix to invert: its FP64 copy (kept for the residual) and FP32 copy
+__global__ void split_copy_kernel(int n, const double2* src, long long sS, double2* d64, long long s64, float2* d32,
+                                  long long s32) {
+  const int b = blockIdx.y;
+  const long long nn = (long long)n * n;
+  const double2* s = src + (long long)b * sS;
+  double2* a = d64 + (long long)b * s64;
+  float2* c = d32 + (long long)b * s32;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nn; e += (long long)gridDim.x * blockDim.x) {
+    const double2 v = s[e];
+    a[e] = v;
+    c[e] = make_float2((float)v.x, (float)v.y);
+  }
+}
+
 __global__ void to_f64_kernel(int n, const float2* src, long long sS, double2* dst, long long sD) {
   const int b = blockIdx.y;
   const long long nn = (long long)n * n;
@@ -548,6 +563,14 @@ __global__ void ns_residual_kernel(int n, double2* T, long long sT, unsigned lon
 
 int to_f32(int n, int batch, const double2* src, long long sS, float2* dst, long long sD, cudaStream_t st) {
   to_f32_kernel<<<ew_grid((long long)n * n, batch), EW_THREADS, 0, st>>>(n, src, sS, dst, sD);
+  NEGF_CUDA_TRY(cudaGetLastError());
+  count_launch();
+  return NEGF_OK;
+}
+
+int split_copy(int n, int batch, const double2* src, long long sS, double2* d64, long long s64, float2* d32,
+               long long s32, cudaStream_t st) {
+  split_copy_kernel<<<ew_grid((long long)n * n, batch), EW_THREADS, 0, st>>>(n, src, sS, d64, s64, d32, s32);
   NEGF_CUDA_TRY(cudaGetLastError());
   count_launch();
   return NEGF_OK;

@@ -320,18 +320,22 @@ __global__ void __launch_bounds__(256) slice_b_kernel(const double2* B, int ldb,
 // ---------------------------------------------------------------------------------
 // the MMA kernel
 // ---------------------------------------------------------------------------------
-template <int S, int NT>
+// MINB = CTAs resident per SM: 1 (deep pipeline, up to 200 KB of stages) or 2 (two CTAs
+// share an SM, so one's prologue/epilogue overlaps the other's MMAs; <= 110 KB of stages
+// and <= 256 TMEM columns each)
+template <int S, int NT, int MINB = 1>
 struct TcCfg {
   static constexpr int A_TILE = TILE_M * ROW_BYTES;            // bytes of one A slice tile
   static constexpr int B_TILE = NT * ROW_BYTES;                // bytes of one B slice tile
   static constexpr int STAGE = S * (A_TILE + B_TILE);
-  static constexpr int STAGES = (200 * 1024) / STAGE > 4 ? 4 : (200 * 1024) / STAGE;
+  static constexpr int BUDGET = MINB == 2 ? 110 * 1024 : 200 * 1024;
+  static constexpr int STAGES = BUDGET / STAGE > 4 ? 4 : BUDGET / STAGE;
   static constexpr int SMEM = STAGES * STAGE + 1024 + 256 + 4 * (NT / 2);   // + alignment, barriers, exponents
   static constexpr int TMEM_COLS_USED = S * NT;
   static constexpr int TMEM_COLS = TMEM_COLS_USED <= 32 ? 32 : TMEM_COLS_USED <= 64 ? 64
                                  : TMEM_COLS_USED <= 128 ? 128 : TMEM_COLS_USED <= 256 ? 256 : 512;
   static_assert(STAGES >= 2, "at least two stages");
-  static_assert(TMEM_COLS_USED <= 512, "TMEM holds 512 columns");
+  static_assert(TMEM_COLS_USED <= 512 / MINB, "TMEM holds 512 columns per SM");
   static_assert(NT % 16 == 0 && NT >= 16 && NT <= 256, "UMMA N");
 };
 
@@ -349,10 +353,10 @@ struct TcArgs {
   int* err;
 };
 
-template <int S, int NT>
-__global__ void __launch_bounds__(TC_THREADS, 1)
+template <int S, int NT, int MINB>
+__global__ void __launch_bounds__(TC_THREADS, MINB)
     zgemm_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, TcArgs a) {
-  using Cfg = TcCfg<S, NT>;
+  using Cfg = TcCfg<S, NT, MINB>;
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + Cfg::STAGES * Cfg::STAGE);
@@ -460,7 +464,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const bool aborted = !ok || *((volatile int*)abort_flag);
     const int e_row = (row < a.m) ? a.ea[(long long)b * a.m + row] : 0;
     double2* Cb = a.C + (long long)b * a.sC;
-    constexpr int CW = S >= 7 ? 8 : 16;      // fp32 columns per chunk (register budget)
+    constexpr int CW = (S >= 7 || MINB == 2 || NT % 16 != 0) ? 8 : 16;   // fp32 columns per chunk
 #pragma unroll 1
     for (int c0 = 0; c0 < NT; c0 += CW) {
       // exact recombination of the diagonal accumulators (integer-valued FP32) in int64:
@@ -548,19 +552,19 @@ int make_map(CUtensorMap* map, const void* base, int kp, long long rows, int box
   return r == CUDA_SUCCESS ? NEGF_OK : NEGF_ECUDA;
 }
 
-template <int S, int NT>
+template <int S, int NT, int MINB>
 int launch_mma(const SlicedOperand& A, const SlicedOperand& B, const TcArgs& args, cudaStream_t st) {
-  using Cfg = TcCfg<S, NT>;
+  using Cfg = TcCfg<S, NT, MINB>;
   CUtensorMap ma, mb;
   NEGF_TRY(make_map(&ma, A.data, args.kp, (long long)args.batch * S * args.rowsA, TILE_M));
   NEGF_TRY(make_map(&mb, B.data, args.kp, (long long)args.batch * S * args.rowsB, NT));
-  NEGF_CUDA_TRY(cudaFuncSetAttribute(zgemm_tc_kernel<S, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM));
+  NEGF_CUDA_TRY(cudaFuncSetAttribute(zgemm_tc_kernel<S, NT, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM));
   dim3 grid((args.m + TILE_M - 1) / TILE_M, (unsigned)((2LL * args.n + NT - 1) / NT), args.batch);
   cudaEvent_t ev;
   const double cflops = 8.0 * args.m * (double)args.n * (args.kp / 2) * args.batch;
   add_tc_complex_flops(cflops);
   timed_begin(st, TK_TC, cflops * (S * (S + 1) / 2), &ev);
-  zgemm_tc_kernel<S, NT><<<grid, TC_THREADS, Cfg::SMEM, st>>>(ma, mb, args);
+  zgemm_tc_kernel<S, NT, MINB><<<grid, TC_THREADS, Cfg::SMEM, st>>>(ma, mb, args);
   NEGF_CUDA_TRY(cudaGetLastError());
   timed_end(st, TK_TC, ev);
   count_launch();
@@ -647,12 +651,12 @@ int zgemm_tc(const SlicedOperand& A, const SlicedOperand& B, double2 alpha, doub
   args.alpha_one = (alpha.x == 1.0 && alpha.y == 0.0) ? 1 : 0;
   args.beta_kind = (beta.x == 0.0 && beta.y == 0.0) ? 0 : (beta.x == 1.0 && beta.y == 0.0) ? 1 : 2;
   switch (A.slices) {
-    case 3: return launch_mma<3, 128>(A, B, args, st);
-    case 4: return launch_mma<4, 128>(A, B, args, st);
-    case 5: return launch_mma<5, 64>(A, B, args, st);
-    case 6: return launch_mma<6, 64>(A, B, args, st);
-    case 7: return launch_mma<7, 64>(A, B, args, st);
-    case 8: return launch_mma<8, 64>(A, B, args, st);
+    case 3: return launch_mma<3, 80, 2>(A, B, args, st);
+    case 4: return launch_mma<4, 64, 2>(A, B, args, st);
+    case 5: return launch_mma<5, 48, 2>(A, B, args, st);
+    case 6: return launch_mma<6, 64, 1>(A, B, args, st);
+    case 7: return launch_mma<7, 64, 1>(A, B, args, st);
+    case 8: return launch_mma<8, 64, 1>(A, B, args, st);
   }
   return NEGF_EINVAL;
 }
