@@ -238,10 +238,16 @@ def main():
     ap.add_argument("--sr-slices", type=int, default=0, help="mixed form: slices of the Sancho-Rubio products")
     ap.add_argument("--fp64-steps", type=int, default=1,
                     help="mixed form: timed FP64 steps on the same requests (T error and FP64 rate)")
+    ap.add_argument("--npx", type=int, default=NPX,
+                    help="slices of the wire; the benchmark workload is 100, shorter wires only for profiling")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
 
+    global NPX, WORKLOAD
+    if args.npx != NPX:
+        NPX = args.npx
+        WORKLOAD = "ti_wire_M400_Npx%d" % NPX
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))

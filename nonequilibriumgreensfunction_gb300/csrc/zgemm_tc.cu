@@ -141,6 +141,14 @@ __device__ __forceinline__ double scaled_int_to_double(long long v, int scale) {
   return __longlong_as_double((long long)(sign | ((unsigned long long)ex << 52) | (mant & ((1ULL << 52) - 1))));
 }
 
+// TMEM loads without the wait: issue several, then one tcgen05.wait::ld
+__device__ __forceinline__ void tmem_ld8_nowait(uint32_t taddr, uint32_t (&r)[8]) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
 __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
   uint32_t r[8];
   asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
@@ -474,14 +482,23 @@ __global__ void __launch_bounds__(TC_THREADS, MINB)
 #pragma unroll
       for (int i = 0; i < CW; ++i) { hi[i] = 0; lo[i] = 0; }
       if (ok) {
+        // all S accumulator reads of this chunk in flight together, one wait
+        uint32_t raw[S][CW];
 #pragma unroll
         for (int d = 0; d < S; ++d) {
-          float f[CW];
           const uint32_t ta = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(d * NT + c0);
-          if constexpr (CW == 16) tmem_ld16(ta, f); else tmem_ld8(ta, f);
+#pragma unroll
+          for (int h = 0; h < CW / 8; ++h) {
+            uint32_t (&r8)[8] = *reinterpret_cast<uint32_t(*)[8]>(&raw[d][8 * h]);
+            tmem_ld8_nowait(ta + 8 * h, r8);
+          }
+        }
+        tmem_wait_ld();
+#pragma unroll
+        for (int d = 0; d < S; ++d) {
 #pragma unroll
           for (int i = 0; i < CW; ++i) {
-            const long long q = (long long)__float2ll_rn(f[i]);
+            const long long q = (long long)__float2ll_rn(__uint_as_float(raw[d][i]));
             if (d < DH) hi[i] += q * (1LL << (7 * (DH - 1 - d)));
             else lo[i] += q * (1LL << (7 * (S - 1 - d)));
           }
