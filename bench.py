@@ -226,6 +226,7 @@ def run_reference(args, rank, world):
 
 
 def main():
+    global NPX, WORKLOAD
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
@@ -244,7 +245,6 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
 
-    global NPX, WORKLOAD
     if args.npx != NPX:
         NPX = args.npx
         WORKLOAD = "ti_wire_M400_Npx%d" % NPX
