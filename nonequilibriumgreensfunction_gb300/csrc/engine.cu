@@ -361,17 +361,25 @@ int Engine::invert_impl(double2* A, long long sA, int batch, int* status_dev) {
   }
   NEGF_CUDA_TRY(cudaStreamSynchronize(st_));
   double worst = 0.0;
+  std::vector<int> bad;
   for (int b = 0; b < batch; ++b) {
     const double r = __longlong_as_double_host(r0[b]);
-    if (info32[b] != 0 || !(r <= ns_accept_)) {
-      // FP64 inverse of the saved matrix
-      NEGF_TRY(copy_blocks(M_, 1, dWinv_ + (long long)b * MM_, MM_, A + (long long)b * sA, sA, st_));
-      NEGF_TRY(zinv_f64(A + (long long)b * sA, sA, M_, 1, inv_, st_));
-      NEGF_TRY(merge_info_kernel_launch(1, inv_.info, status_dev + b, st_));
-      ++fallbacks_;
-    } else if (r > worst) {
-      worst = r;
+    if (info32[b] != 0 || !(r <= ns_accept_)) bad.push_back(b);
+    else if (r > worst) worst = r;
+  }
+  if (!bad.empty()) {
+    // FP64 inverses of the saved matrices, all failures of this call in one batched call
+    const int nb = (int)bad.size();
+    for (int i = 0; i < nb; ++i)
+      NEGF_CUDA_TRY(cudaMemcpyAsync(dT_ + (long long)i * MM_, dWinv_ + (long long)bad[i] * MM_,
+                                    sizeof(double2) * MM_, cudaMemcpyDeviceToDevice, st_));
+    NEGF_TRY(zinv_f64(dT_, MM_, M_, nb, inv_, st_));
+    for (int i = 0; i < nb; ++i) {
+      NEGF_CUDA_TRY(cudaMemcpyAsync(A + (long long)bad[i] * sA, dT_ + (long long)i * MM_, sizeof(double2) * MM_,
+                                    cudaMemcpyDeviceToDevice, st_));
+      NEGF_TRY(merge_info_kernel_launch(1, inv_.info + i, status_dev + bad[i], st_));
     }
+    fallbacks_ += nb;
   }
   last_rnorm_max_ = std::max(last_rnorm_max_, worst);
   return NEGF_OK;

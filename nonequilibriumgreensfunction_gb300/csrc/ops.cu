@@ -2,6 +2,8 @@
 // invert, block-diagonal hopping products, the site blocks of Gn/Gp, traces and the
 // density / spin reductions.  All are O(n^2) per block; the O(n^3) work is in
 // gemm_f64.cu and inverse_f64.cu.
+#include <algorithm>
+
 #include "negf_internal.cuh"
 
 namespace negf {
@@ -192,35 +194,36 @@ __global__ void form_alpha_kernel(int n, const double* energies, const double2* 
   }
 }
 
-// T += change (if active); cmax = max |change| over the block (NaN propagates)
+// T += change (if active); cmax[b] = max |change| (as the bit pattern of a non-negative
+// double, combined with atomicMax across CTAs; a NaN is recorded as a positive NaN, whose
+// pattern exceeds every finite one).  cmax must be zeroed before the launch.
 __global__ void sr_accumulate_kernel(int n, const int* active, const double2* change, long long sC, double2* T,
-                                     long long sT, double* cmax) {
+                                     long long sT, unsigned long long* cmax) {
   __shared__ double red[EW_THREADS];
-  __shared__ int nan_seen;
-  const int b = blockIdx.x;
+  const int b = blockIdx.y;
   const long long nn = (long long)n * n;
   const double2* c = change + (long long)b * sC;
   double2* t = T + (long long)b * sT;
   const bool act = active[b] != 0;
-  if (threadIdx.x == 0) nan_seen = 0;
-  __syncthreads();
   double m = 0.0;
-  bool nan = false;
-  for (long long e = threadIdx.x; e < nn; e += EW_THREADS) {
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nn; e += (long long)gridDim.x * blockDim.x) {
     const double2 v = c[e];
-    const double a = hypot(v.x, v.y);
-    if (isnan(a)) nan = true;
-    m = fmax(m, a);
+    double a = hypot(v.x, v.y);
+    if (isnan(a)) a = __longlong_as_double(0x7FF8000000000000LL);
+    m = (isnan(a) || isnan(m)) ? a : fmax(m, a);
     if (act) t[e] = cadd(t[e], v);
   }
-  if (nan) atomicOr(&nan_seen, 1);
   red[threadIdx.x] = m;
   __syncthreads();
   for (int w = EW_THREADS / 2; w > 0; w >>= 1) {
-    if (threadIdx.x < w) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + w]);
+    if (threadIdx.x < w) {
+      const double o = red[threadIdx.x + w];
+      red[threadIdx.x] = (isnan(o) || isnan(red[threadIdx.x])) ? __longlong_as_double(0x7FF8000000000000LL)
+                                                                : fmax(red[threadIdx.x], o);
+    }
     __syncthreads();
   }
-  if (threadIdx.x == 0) cmax[b] = nan_seen ? (0.0 / 0.0) : red[0];
+  if (threadIdx.x == 0) atomicMax(cmax + b, (unsigned long long)__double_as_longlong(red[0]));
 }
 
 // W = alpha - L T with L = H^H (lead 0) or H (lead 1), H block diagonal
@@ -443,7 +446,11 @@ int form_alpha(int n, int nprob, const double* energies, const double2* const* h
 
 int sr_accumulate(int n, int nprob, const int* active, const double2* change, long long sC, double2* T, long long sT,
                   double* cmax, cudaStream_t st) {
-  sr_accumulate_kernel<<<nprob, EW_THREADS, 0, st>>>(n, active, change, sC, T, sT, cmax);
+  unsigned long long* bits = reinterpret_cast<unsigned long long*>(cmax);
+  NEGF_CUDA_TRY(cudaMemsetAsync(bits, 0, sizeof(unsigned long long) * nprob, st));
+  const long long nn = (long long)n * n;
+  const int per = (int)std::min<long long>((nn + EW_THREADS * 16 - 1) / (EW_THREADS * 16), 64);
+  sr_accumulate_kernel<<<dim3(per, nprob), EW_THREADS, 0, st>>>(n, active, change, sC, T, sT, bits);
   NEGF_CUDA_TRY(cudaGetLastError());
   count_launch();
   return NEGF_OK;
