@@ -77,7 +77,10 @@ typedef struct negf_params {
                                 (0 = default 7; 5..8 allowed)                            */
     int32_t sr_slices;       /* NEGF_PREC_MIXED: slices of the Sancho-Rubio products
                                 (0 = default 8; 5..8 allowed)                            */
-    int32_t reserved[4];     /* must be zero                                             */
+    int32_t calc_currents;   /* 1: bond currents Jx/Jy/Jz (Source/Calculate_Observables.F90:
+                                110-169); keeps the +x/+y/+z site blocks of Gn/Gp
+                                (6*npx*M*norb*16 bytes per batch entry)                  */
+    int32_t reserved[3];     /* must be zero                                             */
     double  spin_ops[3][4][4][2]; /* gMx, gMy, gMz (row-major [row][col][re,im]) used by
                                      the spin reduction, Source/Read_In_Allocate.F90:183-196;
                                      all zero = the reference's tau0 (x) sigma_j          */
@@ -131,6 +134,30 @@ NEGF_API int negf_get_stats(negf_handle* h, negf_stats* out);
  * applies it as a site-local operator instead of a dense product.                     */
 NEGF_API int negf_set_hamiltonian(negf_handle* h, int32_t slot, const double* Htotd, const double* HopX);
 
+/* ---- on-device Hamiltonian ----------------------------------------------------------
+ * Build_Hamiltonian (Source/Build_Hamiltonian.F90:1-303, model 0 with open boundaries) on
+ * the device: the slot's Htotd is generated in HBM from 4 x 4 site blocks instead of being
+ * copied from the host (npx*M^2*16 bytes, 256 MB at M = 400, npx = 100).  Every slice holds
+ * the on-site block on each site, hop_y between (y, z) and (y+1, z) times the Landau-gauge
+ * phase exp(i 2 pi z flux / ((npy-1)(npz-1))) (:186-207), hop_z between (y, z) and (y, z+1),
+ * their Hermitian conjugates below the diagonal, and the potential V(x, y, z) on the
+ * diagonal.  HopX is hop_x on every site (:59-64).  V is either the caller's array or
+ * Anderson disorder U[-W/2, W/2) on slices 2..npx-1 only (:279-296) from a counter-based
+ * stream: V = (u - 1/2) W with u = (s >> 11) 2^-53 and s the i-th output of SplitMix64
+ * seeded with `seed` (Steele, Lea, Flood 2014), i = x + npx (y + npy z) + 1.  The
+ * reference's RANDOM_NUMBER stream is compiler-specific (:230-241); this one is
+ * reproducible bit for bit on any host.  Requires norb = 4.  HopX is shared by all slots,
+ * as in negf_set_hamiltonian.                                                           */
+typedef struct negf_wire_model {
+    double   onsite[4][4][2];  /* row-major [row][col][re, im]                           */
+    double   hop[3][4][4][2];  /* hop_x, hop_y, hop_z = H(site, site + e_j)              */
+    double   flux;             /* Aharonov-Bohm flux through the cross-section, Phi_0    */
+    double   W;                /* disorder width (ignored when V != NULL)                */
+    uint64_t seed;             /* disorder stream                                        */
+    const double* V;           /* optional npx x npy x npz potential, column-major       */
+    int32_t  reserved[8];      /* must be zero                                           */
+} negf_wire_model;
+NEGF_API int negf_build_hamiltonian(negf_handle* h, int32_t slot, const negf_wire_model* model);
 /* ---- per-energy interface (one energy point, Hamiltonian slot 0) ---------------------
  * The four calls below are the drop-in for the reference's subroutines, in the order
  * Energy_Sweep makes them.  All device results stay in the handle between calls.       */
@@ -168,6 +195,14 @@ NEGF_API int negf_calculate_observables(negf_handle* h, double dE, double f1, do
                                double* modes, double* contact_current,
                                double* SigX, double* SigY, double* SigZ);
 
+/* Bond currents of Calculate_Observables (Source/Calculate_Observables.F90:110-169) for the
+ * energy of the last negf_calculate_gnp call (its f1, f2, dE): adds the dE/(2 pi)-weighted
+ * currents of every bond leaving site (x, y, z) towards +x, +y, +z into Jx, Jy, Jz
+ * (npx x npy x npz, any may be NULL).  Each orbital-pair term is rounded to REAL(4) before
+ * it is weighted and added, as the reference's dumVar (:7).  The x bonds use the site
+ * blocks of HopX (:150-156).  NEGF_ESTATE unless the handle was created with
+ * calc_currents = 1 and negf_calculate_gnp ran for this energy.                         */
+NEGF_API int negf_calculate_currents(negf_handle* h, double* Jx, double* Jy, double* Jz);
 /* ---- batched interface -------------------------------------------------------------
  * Many energy points (and Hamiltonian slots, e.g. disorder seeds) in one device pass:
  * the GB300 replacement for the round-robin energy loop of Source/NEGF_Main.F90:21-27
@@ -198,6 +233,18 @@ typedef struct negf_result {
 NEGF_API int negf_solve_batch(negf_handle* h, const negf_request* req, int32_t n, negf_result* res,
                      double* RhoN, double* RhoP, double* SigX, double* SigY, double* SigZ);
 
+/* negf_solve_batch with every accumulated site array of the reference: RhoN, RhoP
+ * (Calculate_Gnp), SigX/Y/Z (calc_spin) and Jx/Jy/Jz (calc_currents), each
+ * npx x npy x npz x n_hamiltonians or NULL, summed over requests as
+ * Source/MPI_Routines.F90:33-90 sums them over ranks.                                   */
+typedef struct negf_batch_outputs {
+    double* RhoN; double* RhoP;
+    double* SigX; double* SigY; double* SigZ;
+    double* Jx;   double* Jy;   double* Jz;
+    double* reserved[8];     /* must be NULL                                             */
+} negf_batch_outputs;
+NEGF_API int negf_solve_batch_ex(negf_handle* h, const negf_request* req, int32_t n, negf_result* res,
+                                 const negf_batch_outputs* out);
 /* ---- serving ----------------------------------------------------------------------
  * A device-resident request loop in place of the MPI energy sweep: wires of different
  * cross-sections arrive as requests (Hamiltonian + a list of energy points with their
@@ -225,14 +272,17 @@ typedef struct negf_serve_params {
 
 typedef struct negf_wire_request {
     int32_t npx, npy, npz, norb;
-    const double* Htotd;      /* M x M x npx complex, copied at submit                       */
-    const double* HopX;       /* M x M complex, copied at submit                             */
+    const double* Htotd;      /* M x M x npx complex, copied at submit (NULL with `model`)   */
+    const double* HopX;       /* M x M complex, copied at submit (NULL with `model`)         */
     int32_t n_energies;
     int32_t reserved0;
     const double* energies;   /* n_energies each, copied at submit                           */
     const double* f1;
     const double* f2;
     const double* dE;
+    const negf_wire_model* model; /* instead of Htotd/HopX: the wire is generated on the
+                                 device by negf_build_hamiltonian (norb = 4); the model and
+                                 its V array are copied at submit                          */
 } negf_wire_request;
 
 typedef struct negf_wire_status {

@@ -21,7 +21,8 @@ INCLUDE_DIR = os.path.join(REPO_DIR, "include")
 
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH_FLAGS + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
-                           "-Xcompiler", "-fvisibility=hidden", "--expt-relaxed-constexpr",
+                           "-Xcompiler", "-fvisibility=hidden", "-Xcompiler", "-ffp-contract=off",
+                           "--expt-relaxed-constexpr",
                            "-I" + INCLUDE_DIR]
 
 

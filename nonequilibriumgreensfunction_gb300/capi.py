@@ -8,7 +8,7 @@ from __future__ import annotations
 
 import ctypes
 import os
-from ctypes import POINTER, c_char_p, c_double, c_int, c_int32, c_int64, c_void_p
+from ctypes import POINTER, c_char_p, c_double, c_int, c_int32, c_int64, c_uint64, c_void_p
 
 from . import _build
 
@@ -33,9 +33,10 @@ NEGF_PREC_MIXED = 1
 EXPORTED_SYMBOLS = (
     "negf_create", "negf_destroy", "negf_strerror", "negf_device_bytes",
     "negf_set_stream", "negf_profile", "negf_get_stats",
-    "negf_set_hamiltonian", "negf_contact_self_energy", "negf_get_retarded_greens",
+    "negf_set_hamiltonian", "negf_build_hamiltonian", "negf_contact_self_energy", "negf_get_retarded_greens",
     "negf_copy_g_columns", "negf_calculate_gnp", "negf_calculate_observables",
-    "negf_solve_batch", "negf_zgemm", "negf_zinv", "negf_zgemm_noalloc",
+    "negf_calculate_currents", "negf_solve_batch", "negf_solve_batch_ex",
+    "negf_zgemm", "negf_zinv", "negf_zgemm_noalloc",
     "negf_server_create", "negf_server_submit", "negf_server_poll", "negf_server_wait",
     "negf_server_clock", "negf_server_destroy",
 )
@@ -48,7 +49,8 @@ class NegfParams(ctypes.Structure):
         ("eta", c_double), ("sr_tol", c_double),
         ("sr_max_iter", c_int32), ("calc_spin", c_int32), ("precision", c_int32),
         ("device", c_int32), ("mixed_slices", c_int32), ("keep_g_columns", c_int32),
-        ("residual_slices", c_int32), ("sr_slices", c_int32), ("reserved", c_int32 * 4),
+        ("residual_slices", c_int32), ("sr_slices", c_int32), ("calc_currents", c_int32),
+        ("reserved", c_int32 * 3),
         ("spin_ops", c_double * (3 * 4 * 4 * 2)),
     ]
 
@@ -62,6 +64,39 @@ class NegfResult(ctypes.Structure):
     _fields_ = [("T12", c_double), ("EDensity", c_double), ("HDensity", c_double),
                 ("modes", c_double * 2), ("dosc", c_double * 2),
                 ("status", c_int32), ("sr_iters", c_int32)]
+
+
+class NegfWireModel(ctypes.Structure):
+    _fields_ = [("onsite", c_double * 32), ("hop", c_double * 96), ("flux", c_double), ("W", c_double),
+                ("seed", c_uint64), ("V", c_void_p), ("reserved", c_int32 * 8)]
+
+
+def wire_model_struct(model, shape):
+    """NegfWireModel from a ``hamiltonian.wire_model`` dict; returns (struct, V array kept
+    alive by the caller for as long as the struct is used).  ``shape`` = (npx, npy, npz)."""
+    import numpy as np
+    m = NegfWireModel()
+    blocks = [np.asarray(model["onsite"], dtype=complex)] + [np.asarray(h, dtype=complex) for h in model["hops"]]
+    flat = [np.stack([b.real, b.imag], axis=-1).ravel() for b in blocks]
+    for i, v in enumerate(flat[0]):
+        m.onsite[i] = v
+    for j in range(3):
+        for i, v in enumerate(flat[1 + j]):
+            m.hop[32 * j + i] = v
+    m.flux, m.W, m.seed = float(model["flux"]), float(model["W"]), int(model["seed"]) & (2 ** 64 - 1)
+    keep = None
+    if model.get("V") is not None:
+        keep = np.asfortranarray(np.asarray(model["V"], dtype=np.float64))
+        if keep.shape != tuple(shape):
+            raise ValueError("V must be (npx, npy, npz) = %s" % (tuple(shape),))
+        m.V = keep.ctypes.data
+    return m, keep
+
+
+class NegfBatchOutputs(ctypes.Structure):
+    _fields_ = [("RhoN", c_void_p), ("RhoP", c_void_p), ("SigX", c_void_p), ("SigY", c_void_p),
+                ("SigZ", c_void_p), ("Jx", c_void_p), ("Jy", c_void_p), ("Jz", c_void_p),
+                ("reserved", c_void_p * 8)]
 
 
 class NegfStats(ctypes.Structure):
@@ -84,7 +119,8 @@ class NegfServeParams(ctypes.Structure):
 class NegfWireRequest(ctypes.Structure):
     _fields_ = [("npx", c_int32), ("npy", c_int32), ("npz", c_int32), ("norb", c_int32),
                 ("Htotd", c_void_p), ("HopX", c_void_p), ("n_energies", c_int32), ("reserved0", c_int32),
-                ("energies", c_void_p), ("f1", c_void_p), ("f2", c_void_p), ("dE", c_void_p)]
+                ("energies", c_void_p), ("f1", c_void_p), ("f2", c_void_p), ("dE", c_void_p),
+                ("model", c_void_p)]
 
 
 class NegfWireStatus(ctypes.Structure):
@@ -113,12 +149,14 @@ def _declare(lib):
         "negf_profile": (c_int, [h, c_int]),
         "negf_get_stats": (c_int, [h, POINTER(NegfStats)]),
         "negf_set_hamiltonian": (c_int, [h, c_int32, _dp, _dp]),
+        "negf_build_hamiltonian": (c_int, [h, c_int32, POINTER(NegfWireModel)]),
         "negf_contact_self_energy": (c_int, [h, c_double, _dp, _dp, _dp, _dp, _dp]),
         "negf_get_retarded_greens": (c_int, [h]),
         "negf_copy_g_columns": (c_int, [h, _dp, _dp]),
         "negf_calculate_gnp": (c_int, [h, c_double, c_double, c_double, _dp, _dp]),
         "negf_calculate_observables": (c_int, [h, c_double, c_double, c_double, _dp, _dp, _dp, _dp,
                                                _dp, _dp, _dp, _dp]),
+        "negf_calculate_currents": (c_int, [h, _dp, _dp, _dp]),
         "negf_zgemm": (c_int, [c_int32, c_int32, c_int32, c_int32, _dp, _dp, c_int32, _dp, c_int32, _dp, _dp,
                                c_int32, c_int32]),
         "negf_zinv": (c_int, [c_int32, _dp, _dp, c_int32]),
@@ -132,6 +170,8 @@ def _declare(lib):
         "negf_server_destroy": (c_int, [h]),
         "negf_solve_batch": (c_int, [h, POINTER(NegfRequest), c_int32, POINTER(NegfResult),
                                      _dp, _dp, _dp, _dp, _dp]),
+        "negf_solve_batch_ex": (c_int, [h, POINTER(NegfRequest), c_int32, POINTER(NegfResult),
+                                        POINTER(NegfBatchOutputs)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

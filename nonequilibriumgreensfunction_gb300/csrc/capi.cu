@@ -9,8 +9,6 @@ namespace negf {
 
 namespace {
 thread_local std::string g_last_cuda_error;
-constexpr double kQ = 1.602e-19;   // Source/Constants.F90:4
-constexpr double kH = 6.626e-34;   // Source/Constants.F90:6
 }  // namespace
 
 void record_cuda_error(cudaError_t e, const char* what, const char* file, int line) {
@@ -99,7 +97,7 @@ extern "C" {
 int negf_create(const negf_params* p, negf_handle** out) {
   if (!p || !out) return NEGF_EINVAL;
   *out = nullptr;
-  for (int i = 0; i < 4; ++i)
+  for (int i = 0; i < 3; ++i)
     if (p->reserved[i] != 0) return NEGF_EINVAL;
   negf_handle* h = new (std::nothrow) negf_handle();
   if (!h) return NEGF_ENOMEM;
@@ -201,6 +199,11 @@ int negf_set_hamiltonian(negf_handle* h, int32_t slot, const double* Htotd, cons
   return h->eng.set_hamiltonian(slot, Htotd, HopX);
 }
 
+int negf_build_hamiltonian(negf_handle* h, int32_t slot, const negf_wire_model* model) {
+  if (!h || !model) return NEGF_EINVAL;
+  return h->eng.build_hamiltonian(slot, *model);
+}
+
 int negf_contact_self_energy(negf_handle* h, double energy, double* SigmaL, double* SigmaR, double* GammaL,
                              double* GammaR, double* dosc) {
   if (!h) return NEGF_EINVAL;
@@ -288,8 +291,9 @@ int negf_calculate_gnp(negf_handle* h, double f1, double f2, double dE, double* 
   std::vector<double> ed, hd;
   NEGF_TRY(e.densities(items, ed, hd));
   const long long total = e.nsite_total();
-  e.last_site_.resize(5 * total);
-  NEGF_CUDA_TRY(cudaMemcpyAsync(e.last_site_.data(), e.dSite_, sizeof(double) * 5 * total, cudaMemcpyDeviceToHost, e.st_));
+  e.last_site_.resize((size_t)e.nf_ * total);
+  NEGF_CUDA_TRY(cudaMemcpyAsync(e.last_site_.data(), e.dSite_, sizeof(double) * e.nf_ * total,
+                                cudaMemcpyDeviceToHost, e.st_));
   NEGF_CUDA_TRY(cudaStreamSynchronize(e.st_));
   for (long long i = 0; i < total; ++i) {
     if (RhoN) RhoN[i] += e.last_site_[i];
@@ -330,10 +334,37 @@ int negf_calculate_observables(negf_handle* h, double dE, double f1, double f2, 
   return NEGF_OK;
 }
 
+int negf_calculate_currents(negf_handle* h, double* Jx, double* Jy, double* Jz) {
+  if (!h) return NEGF_EINVAL;
+  Engine& e = h->eng;
+  if (!e.currents_ || !e.dens_valid_) return NEGF_ESTATE;
+  const long long total = e.nsite_total();
+  double* outs[3] = {Jx, Jy, Jz};
+  for (int j = 0; j < 3; ++j)
+    if (outs[j])
+      for (long long i = 0; i < total; ++i) outs[j][i] += e.last_site_[(5 + j) * total + i];
+  return NEGF_OK;
+}
+
 int negf_solve_batch(negf_handle* h, const negf_request* req, int32_t n, negf_result* res, double* RhoN, double* RhoP,
                      double* SigX, double* SigY, double* SigZ) {
   if (!h) return NEGF_EINVAL;
-  return h->eng.batch_solve(req, n, res, RhoN, RhoP, SigX, SigY, SigZ);
+  double* outs[8] = {RhoN, RhoP, SigX, SigY, SigZ, nullptr, nullptr, nullptr};
+  return h->eng.batch_solve(req, n, res, outs);
+}
+
+int negf_solve_batch_ex(negf_handle* h, const negf_request* req, int32_t n, negf_result* res,
+                        const negf_batch_outputs* out) {
+  if (!h) return NEGF_EINVAL;
+  double* outs[8] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  if (out) {
+    for (int i = 0; i < 8; ++i)
+      if (out->reserved[i]) return NEGF_EINVAL;
+    if ((out->Jx || out->Jy || out->Jz) && !h->eng.currents_) return NEGF_ESTATE;
+    double* o[8] = {out->RhoN, out->RhoP, out->SigX, out->SigY, out->SigZ, out->Jx, out->Jy, out->Jz};
+    for (int i = 0; i < 8; ++i) outs[i] = o[i];
+  }
+  return h->eng.batch_solve(req, n, res, outs);
 }
 
 }  // extern "C"

@@ -78,17 +78,19 @@ int merge_info_kernel_launch(int batch, const int* info, int* status, cudaStream
 
 Engine::~Engine() {
   if (p_.npx > 0) cudaSetDevice(p_.device);
-  dfree(dH_); dfree(dHop_); dfree(dHopBD_); dfree(dSpin_);
+  dfree(dH_); dfree(dHop_); dfree(dHopBD_); dfree(dSpin_); dfree(dHtab_); dfree(dVext_);
   dfree(dG_); dfree(dC1_); dfree(dCN_); dfree(dZ_); dfree(dY_); dfree(dQ_);
   dfree(dSigL_); dfree(dSigR_); dfree(dGamL_); dfree(dGamR_);
   dfree(dP1_); dfree(dP2_); dfree(dCol1_); dfree(dColN_);
+  dfree(dPx1_); dfree(dPy1_); dfree(dPz1_); dfree(dPx2_); dfree(dPy2_); dfree(dPz2_);
+  if (currents_) { dfree(dYalt_); dfree(dCNalt_); }
   dfree(dSite_); dfree(dSums_); dfree(dTr_); dfree(dAcc_); dfree(dStatus_); dfree(dItems_);
   dfree(dSr_); dfree(dSrSigL_); dfree(dSrSigR_); dfree(dSrGamL_); dfree(dSrGamR_);
   dfree(dSrCmax_); dfree(dSrDos_); dfree(dSrActive_); dfree(dSrE_); dfree(dSrHend_); dfree(dSrStatus_);
   inv_work_free(inv_);
   dfree(dWinv_); dfree(dW32_); dfree(dT_); dfree(sa_.data); dfree(sb_.data); dfree(sa_.exps); dfree(sb_.exps);
   dfree(sw_.data); dfree(sw_.exps);
-  dfree(dRnorm_); dfree(dTcErr_);
+  dfree(dRnorm_); dfree(dNsActive_); dfree(dTcErr_);
   if (hPin_) cudaFreeHost(hPin_);
   if (own_st_) cudaStreamDestroy(own_st_);
 }
@@ -111,6 +113,8 @@ int Engine::init(const negf_params& p) {
   B_ = p.max_batch;
   S_ = 2 * p.max_batch;
   keep_columns_ = p.keep_g_columns != 0;
+  currents_ = p.calc_currents != 0;
+  nf_ = currents_ ? 8 : 5;
   mixed_ = p.precision == NEGF_PREC_MIXED;
   if (mixed_ && p.mixed_slices != 0) s_rgf_ = p.mixed_slices;
   if (mixed_ && p.sr_slices != 0) {
@@ -139,6 +143,8 @@ int Engine::alloc() {
   NEGF_TRY(dalloc(&dHop_, (size_t)MM_, bytes_));
   NEGF_TRY(dalloc(&dHopBD_, (size_t)nsite_ * p_.norb * p_.norb, bytes_));
   NEGF_TRY(dalloc(&dSpin_, (size_t)3 * p_.norb * p_.norb, bytes_));
+  NEGF_TRY(dalloc(&dHtab_, (size_t)16 * (2 + p_.npz), bytes_));
+  NEGF_TRY(dalloc(&dVext_, (size_t)total, bytes_));
   NEGF_TRY(dalloc(&dG_, (size_t)(B_ * N * MM_), bytes_));
   double2** bufs[] = {&dC1_, &dCN_, &dZ_, &dY_, &dQ_, &dSigL_, &dSigR_, &dGamL_, &dGamR_};
   for (double2** b : bufs) NEGF_TRY(dalloc(b, (size_t)(B_ * MM_), bytes_));
@@ -148,11 +154,23 @@ int Engine::alloc() {
     NEGF_TRY(dalloc(&dCol1_, (size_t)(N * MM_), bytes_));
     NEGF_TRY(dalloc(&dColN_, (size_t)(N * MM_), bytes_));
   }
+  if (currents_) {
+    double2** pb[] = {&dPx1_, &dPy1_, &dPz1_, &dPx2_, &dPy2_, &dPz2_};
+    for (double2** b : pb) NEGF_TRY(dalloc(b, (size_t)(B_ * N * M_ * p_.norb), bytes_));
+    NEGF_TRY(dalloc(&dYalt_, (size_t)(B_ * MM_), bytes_));
+    NEGF_TRY(dalloc(&dCNalt_, (size_t)(B_ * MM_), bytes_));
+    // the x bond of the last slice does not exist: its blocks stay zero
+    for (double2* b : {dPx1_, dPx2_})
+      NEGF_CUDA_TRY(cudaMemset(b, 0, sizeof(double2) * (size_t)(B_ * N * M_ * p_.norb)));
+  } else {
+    dYalt_ = dY_;
+    dCNalt_ = dCN_;
+  }
   sums_blocks_ = (int)((total + 255) / 256);
-  NEGF_TRY(dalloc(&dSite_, (size_t)(B_ * 5 * total), bytes_));
+  NEGF_TRY(dalloc(&dSite_, (size_t)(B_ * nf_ * total), bytes_));
   NEGF_TRY(dalloc(&dSums_, (size_t)B_ * sums_blocks_ * 2, bytes_));
   NEGF_TRY(dalloc(&dTr_, (size_t)B_ * 4, bytes_));
-  NEGF_TRY(dalloc(&dAcc_, (size_t)(p_.n_hamiltonians * 5 * total), bytes_));
+  NEGF_TRY(dalloc(&dAcc_, (size_t)(p_.n_hamiltonians * nf_ * total), bytes_));
   NEGF_TRY(dalloc(&dStatus_, (size_t)B_, bytes_));
   NEGF_TRY(dalloc(&dItems_, (size_t)B_, bytes_));
   NEGF_TRY(dalloc(&dSr_, (size_t)(kSrBlocks * S_ * MM_), bytes_));
@@ -179,12 +197,13 @@ int Engine::alloc() {
     NEGF_TRY(dalloc(&sa_.exps, (size_t)cap * M_, bytes_));
     NEGF_TRY(dalloc(&sb_.exps, (size_t)cap * M_, bytes_));
     NEGF_TRY(dalloc(&dRnorm_, (size_t)cap, bytes_));
+    NEGF_TRY(dalloc(&dNsActive_, (size_t)cap, bytes_));
     NEGF_TRY(dalloc(&dTcErr_, (size_t)1, bytes_));
     NEGF_CUDA_TRY(cudaMemset(dTcErr_, 0, sizeof(int)));
   }
   hPinBytes_ = sizeof(double) * (size_t)std::max<long long>(
                    {(long long)B_ * sums_blocks_ * 2, (long long)B_ * 4, 4LL * S_,
-                    (long long)p_.n_hamiltonians * 5 * total, 5LL * total, 64});
+                    (long long)p_.n_hamiltonians * nf_ * total, (long long)nf_ * total, 64});
   NEGF_CUDA_TRY(cudaMallocHost((void**)&hPin_, hPinBytes_));
   // spin operators (default: tau0 (x) sigma_j of Source/Read_In_Allocate.F90:183-196)
   std::vector<double2> spin(3 * p_.norb * p_.norb, make_double2(0.0, 0.0));
@@ -213,40 +232,42 @@ int Engine::alloc() {
   return NEGF_OK;
 }
 
+int Engine::set_hopx(const double2* hx) {
+  if (hop_set_) {
+    std::vector<double2> cur(MM_);
+    NEGF_CUDA_TRY(cudaMemcpy(cur.data(), dHop_, sizeof(double2) * MM_, cudaMemcpyDeviceToHost));
+    // a different HopX invalidates every slot uploaded with the old one
+    if (!blocks_equal(cur.data(), hx, MM_)) std::fill(slot_set_.begin(), slot_set_.end(), 0);
+  }
+  NEGF_CUDA_TRY(cudaMemcpy(dHop_, hx, sizeof(double2) * MM_, cudaMemcpyHostToDevice));
+  // block-diagonal detection (site blocks of norb x norb)
+  const int no = p_.norb;
+  bool bd = true;
+  for (int j = 0; j < M_ && bd; ++j)
+    for (int i = 0; i < M_; ++i) {
+      if (i / no == j / no) continue;
+      const double2 v = hx[(long long)j * M_ + i];
+      if (v.x != 0.0 || v.y != 0.0) { bd = false; break; }
+    }
+  hop_bd_ = bd;
+  if (bd) {
+    std::vector<double2> hb((size_t)nsite_ * no * no);
+    for (int s = 0; s < nsite_; ++s)
+      for (int a = 0; a < no; ++a)
+        for (int c = 0; c < no; ++c) hb[((size_t)s * no + a) * no + c] = hx[(long long)(s * no + c) * M_ + s * no + a];
+    NEGF_CUDA_TRY(cudaMemcpy(dHopBD_, hb.data(), sizeof(double2) * hb.size(), cudaMemcpyHostToDevice));
+  }
+  hop_set_ = true;
+  return NEGF_OK;
+}
+
 int Engine::set_hamiltonian(int slot, const double* Htotd, const double* HopX) {
   if (slot < 0 || slot >= p_.n_hamiltonians || !Htotd) return NEGF_EINVAL;
   if (!hop_set_ && !HopX) return NEGF_EINVAL;
   NEGF_CUDA_TRY(cudaSetDevice(p_.device));
   const double2* h = reinterpret_cast<const double2*>(Htotd);
   const long long N = p_.npx;
-  if (HopX) {
-    const double2* hx = reinterpret_cast<const double2*>(HopX);
-    if (hop_set_) {
-      std::vector<double2> cur(MM_);
-      NEGF_CUDA_TRY(cudaMemcpy(cur.data(), dHop_, sizeof(double2) * MM_, cudaMemcpyDeviceToHost));
-      // a different HopX invalidates every slot uploaded with the old one
-      if (!blocks_equal(cur.data(), hx, MM_)) std::fill(slot_set_.begin(), slot_set_.end(), 0);
-    }
-    NEGF_CUDA_TRY(cudaMemcpy(dHop_, hx, sizeof(double2) * MM_, cudaMemcpyHostToDevice));
-    // block-diagonal detection (site blocks of norb x norb)
-    const int no = p_.norb;
-    bool bd = true;
-    for (int j = 0; j < M_ && bd; ++j)
-      for (int i = 0; i < M_; ++i) {
-        if (i / no == j / no) continue;
-        const double2 v = hx[(long long)j * M_ + i];
-        if (v.x != 0.0 || v.y != 0.0) { bd = false; break; }
-      }
-    hop_bd_ = bd;
-    if (bd) {
-      std::vector<double2> hb((size_t)nsite_ * no * no);
-      for (int s = 0; s < nsite_; ++s)
-        for (int a = 0; a < no; ++a)
-          for (int c = 0; c < no; ++c) hb[((size_t)s * no + a) * no + c] = hx[(long long)(s * no + c) * M_ + s * no + a];
-      NEGF_CUDA_TRY(cudaMemcpy(dHopBD_, hb.data(), sizeof(double2) * hb.size(), cudaMemcpyHostToDevice));
-    }
-    hop_set_ = true;
-  }
+  if (HopX) NEGF_TRY(set_hopx(reinterpret_cast<const double2*>(HopX)));
   NEGF_CUDA_TRY(cudaMemcpy(dH_ + (long long)slot * N * MM_, h, sizeof(double2) * N * MM_, cudaMemcpyHostToDevice));
   end_h1_[slot].assign(h, h + MM_);
   end_hn_[slot].assign(h + (N - 1) * MM_, h + N * MM_);
@@ -331,6 +352,11 @@ int Engine::invert_impl(double2* A, long long sA, int batch, int* status_dev) {
   NEGF_CUDA_TRY(cudaMemsetAsync(dRnorm_, 0, sizeof(unsigned long long) * batch, st_));
   NEGF_TRY(slice_a(dWinv_, M_, MM_, M_, M_, batch, s_res_, sw_, st_));
   std::vector<unsigned long long> r0(batch), rk(batch);
+  // Steps after the first ns_steps_ - 1 are taken per matrix: a matrix stays active while its
+  // own residual norm before the update is above ns_tol_ (the update squares it).  Inactive
+  // matrices get R = 0, so X + X R leaves them bit for bit unchanged and each inverse depends
+  // only on its own matrix, never on the rest of the batch.
+  std::vector<int> active(batch, 1);
   for (int step = 0; step < ns_max_steps_; ++step) {
     if (step > 0) NEGF_CUDA_TRY(cudaMemsetAsync(dRnorm_, 0, sizeof(unsigned long long) * batch, st_));
     NEGF_TRY(slice_b(A, M_, sA, M_, M_, batch, s_res_, sb_, st_));
@@ -339,20 +365,25 @@ int Engine::invert_impl(double2* A, long long sA, int batch, int* status_dev) {
     if (step == 0)
       NEGF_CUDA_TRY(cudaMemcpyAsync(r0.data(), dRnorm_, sizeof(unsigned long long) * batch, cudaMemcpyDeviceToHost, st_));
     if (step + 1 >= ns_steps_) {
-      // R_{k+1} = R_k^2: after this update the residual is at most |R_k|^2; stop if that is
-      // small for every matrix that is not going to be redone in FP64
+      // R_{k+1} = R_k^2: after this update the residual is at most |R_k|^2
       NEGF_CUDA_TRY(cudaMemcpyAsync(rk.data(), dRnorm_, sizeof(unsigned long long) * batch, cudaMemcpyDeviceToHost, st_));
       NEGF_CUDA_TRY(cudaStreamSynchronize(st_));
-      double worst_k = 0.0;
+      if (step + 1 > ns_steps_) {
+        // R of matrices that finished earlier (or go to the FP64 fallback) is zeroed
+        NEGF_CUDA_TRY(cudaMemcpyAsync(dNsActive_, active.data(), sizeof(int) * batch, cudaMemcpyHostToDevice, st_));
+        NEGF_TRY(zero_unmasked(M_, batch, dNsActive_, dT_, MM_, st_));
+      }
+      bool more = false;
       for (int b = 0; b < batch; ++b) {
         const double r = __longlong_as_double_host(r0[b]);
-        if (info32[b] != 0 || !(r <= ns_accept_)) continue;
-        worst_k = std::max(worst_k, __longlong_as_double_host(rk[b]));
+        if (info32[b] != 0 || !(r <= ns_accept_)) { active[b] = 0; continue; }
+        if (active[b] && __longlong_as_double_host(rk[b]) <= ns_tol_) active[b] = 0;
+        more = more || active[b];
       }
       NEGF_TRY(slice_a(A, M_, sA, M_, M_, batch, s_upd_, sa_, st_));
       NEGF_TRY(slice_b(dT_, M_, MM_, M_, M_, batch, s_upd_, sb_, st_));
       NEGF_TRY(zgemm_tc(sa_, sb_, one, one, A, M_, sA, dTcErr_, st_));            // X += X R
-      if (worst_k <= ns_tol_) break;
+      if (!more) break;
       continue;
     }
     NEGF_TRY(slice_a(A, M_, sA, M_, M_, batch, s_upd_, sa_, st_));
@@ -571,49 +602,70 @@ int Engine::solve_rgf_impl(const std::vector<Item>& items, bool keep_columns) {
   // right-connected sweep gR_x = inv(A_x - H gR_{x+1} H^H), x = N..1 (Recursive_Greens.F90:67-86)
   for (int x = N - 1; x >= 0; --x) NEGF_TRY(form(x, 1, x < N - 1 ? dG_ + (long long)(x + 1) * MM_ : nullptr));
 
-  // forward: column 1 from gR, then the left-connected gL_x into the same slot
+  // forward: column 1 from gR, then the left-connected gL_x into the same slot.  With
+  // currents, Y alternates between two buffers so that Y(x-1) = G(x-1,1) Gamma_L is still
+  // there when G(x,1) is formed: P1(x-1, x) = Y(x-1) G(x,1)^H on the site blocks.
+  const long long sl = (long long)M_ * p_.norb;   // one slice of site blocks
   for (int x = 0; x < N; ++x) {
     double2* Gx = dG_ + (long long)x * MM_;
+    double2* Y = (x & 1) ? dYalt_ : dY_;
+    double2* Yprev = (x & 1) ? dY_ : dYalt_;
     if (x == 0) {
       NEGF_TRY(copy_blocks(M_, B, Gx, sG, dC1_, sM, st_));                     // G(1,1) = gR_1
     } else {
       NEGF_TRY(hop_mul(1, OP_C, dC1_, sM, dZ_, sM, B));                          // H^H G(x-1,1)
       NEGF_TRY(gemm(B, OP_N, Gx, sG, OP_N, dZ_, sM, dC1_, sM, one, zero));       // gR_x H^H G(x-1,1)
+      if (currents_)
+        NEGF_TRY(site_blocks(M_, p_.norb, B, Yprev, sM, dC1_, sM, dPx1_ + (x - 1) * sl, sP, st_));
     }
     if (keep_columns && dCol1_) NEGF_TRY(copy_blocks(M_, 1, dC1_, sM, dCol1_ + (long long)x * MM_, sM, st_));
-    NEGF_TRY(gemm(B, OP_N, dC1_, sM, OP_N, dGamL_, sM, dY_, sM, one, zero));      // G(x,1) Gamma_L
-    NEGF_TRY(site_blocks(M_, p_.norb, B, dY_, sM, dC1_, sM, dP1_ + (long long)x * M_ * p_.norb, sP, st_));
+    NEGF_TRY(gemm(B, OP_N, dC1_, sM, OP_N, dGamL_, sM, Y, sM, one, zero));        // G(x,1) Gamma_L
+    if (currents_)
+      NEGF_TRY(site_pairs(M_, p_.norb, p_.npy, p_.npz, B, Y, sM, dC1_, sM, dP1_ + x * sl, dPy1_ + x * sl,
+                          dPz1_ + x * sl, sP, st_));
+    else
+      NEGF_TRY(site_blocks(M_, p_.norb, B, Y, sM, dC1_, sM, dP1_ + x * sl, sP, st_));
     if (x == 0) {
-      NEGF_TRY(gemm(B, OP_N, dGamL_, sM, OP_N, dY_, sM, dQ_, sM, one, zero));
+      NEGF_TRY(gemm(B, OP_N, dGamL_, sM, OP_N, Y, sM, dQ_, sM, one, zero));
       NEGF_TRY(trace_dot(M_, B, dQ_, sM, dC1_, sM, dTr_ + 0, 4, st_));
     }
     if (x == N - 1) {
-      NEGF_TRY(gemm(B, OP_N, dGamR_, sM, OP_N, dY_, sM, dQ_, sM, one, zero));
+      NEGF_TRY(gemm(B, OP_N, dGamR_, sM, OP_N, Y, sM, dQ_, sM, one, zero));
       NEGF_TRY(trace_dot(M_, B, dQ_, sM, dC1_, sM, dTr_ + 2, 4, st_));
     }
     // gL_x = inv(A_x - H^H gL_{x-1} H) (Recursive_Greens.F90:16-34)
     NEGF_TRY(form(x, 0, x > 0 ? dG_ + (long long)(x - 1) * MM_ : nullptr));
   }
 
-  // backward: column N, G(x,N) = gL_x H G(x+1,N) (Recursive_Greens.F90:53-63)
+  // backward: column N, G(x,N) = gL_x H G(x+1,N) (Recursive_Greens.F90:53-63).  With
+  // currents, G(:,N) alternates between two buffers so that G(x+1,N) is still there for
+  // P2(x, x+1) = Y(x) G(x+1,N)^H on the site blocks.
   for (int x = N - 1; x >= 0; --x) {
     double2* Gx = dG_ + (long long)x * MM_;
+    double2* CN = ((N - 1 - x) & 1) ? dCNalt_ : dCN_;
+    double2* CNprev = ((N - 1 - x) & 1) ? dCN_ : dCNalt_;
     if (x == N - 1) {
-      NEGF_TRY(copy_blocks(M_, B, Gx, sG, dCN_, sM, st_));
+      NEGF_TRY(copy_blocks(M_, B, Gx, sG, CN, sM, st_));
     } else {
-      NEGF_TRY(hop_mul(1, OP_N, dCN_, sM, dZ_, sM, B));
-      NEGF_TRY(gemm(B, OP_N, Gx, sG, OP_N, dZ_, sM, dCN_, sM, one, zero));
+      NEGF_TRY(hop_mul(1, OP_N, CNprev, sM, dZ_, sM, B));
+      NEGF_TRY(gemm(B, OP_N, Gx, sG, OP_N, dZ_, sM, CN, sM, one, zero));
     }
-    if (keep_columns && dColN_) NEGF_TRY(copy_blocks(M_, 1, dCN_, sM, dColN_ + (long long)x * MM_, sM, st_));
-    NEGF_TRY(gemm(B, OP_N, dCN_, sM, OP_N, dGamR_, sM, dY_, sM, one, zero));      // G(x,N) Gamma_R
-    NEGF_TRY(site_blocks(M_, p_.norb, B, dY_, sM, dCN_, sM, dP2_ + (long long)x * M_ * p_.norb, sP, st_));
+    if (keep_columns && dColN_) NEGF_TRY(copy_blocks(M_, 1, CN, sM, dColN_ + (long long)x * MM_, sM, st_));
+    NEGF_TRY(gemm(B, OP_N, CN, sM, OP_N, dGamR_, sM, dY_, sM, one, zero));        // G(x,N) Gamma_R
+    if (currents_) {
+      NEGF_TRY(site_pairs(M_, p_.norb, p_.npy, p_.npz, B, dY_, sM, CN, sM, dP2_ + x * sl, dPy2_ + x * sl,
+                          dPz2_ + x * sl, sP, st_));
+      if (x < N - 1) NEGF_TRY(site_blocks(M_, p_.norb, B, dY_, sM, CNprev, sM, dPx2_ + x * sl, sP, st_));
+    } else {
+      NEGF_TRY(site_blocks(M_, p_.norb, B, dY_, sM, CN, sM, dP2_ + x * sl, sP, st_));
+    }
     if (x == 0) {   // T12 = Re Tr[Gamma_L G(1,N) Gamma_R G(1,N)^H] (Calculate_Observables.F90:85-100)
       NEGF_TRY(gemm(B, OP_N, dGamL_, sM, OP_N, dY_, sM, dQ_, sM, one, zero));
-      NEGF_TRY(trace_dot(M_, B, dQ_, sM, dCN_, sM, dTr_ + 1, 4, st_));
+      NEGF_TRY(trace_dot(M_, B, dQ_, sM, CN, sM, dTr_ + 1, 4, st_));
     }
     if (x == N - 1) {
       NEGF_TRY(gemm(B, OP_N, dGamR_, sM, OP_N, dY_, sM, dQ_, sM, one, zero));
-      NEGF_TRY(trace_dot(M_, B, dQ_, sM, dCN_, sM, dTr_ + 3, 4, st_));
+      NEGF_TRY(trace_dot(M_, B, dQ_, sM, CN, sM, dTr_ + 3, 4, st_));
     }
   }
   return NEGF_OK;
@@ -632,10 +684,20 @@ int Engine::densities_impl(const std::vector<Item>& items, std::vector<double>& 
   NEGF_CUDA_TRY(cudaMemcpyAsync(dItems_, items.data(), sizeof(Item) * B, cudaMemcpyHostToDevice, st_));
   DensityArgs a{};
   a.n = M_; a.norb = p_.norb; a.npx = p_.npx; a.npy = p_.npy; a.npz = p_.npz; a.batch = B;
-  a.calc_spin = p_.calc_spin; a.items = dItems_;
+  a.calc_spin = p_.calc_spin; a.nf = nf_; a.items = dItems_;
   a.P1 = dP1_; a.P2 = dP2_; a.sP = (long long)p_.npx * M_ * p_.norb;
   a.spin_ops = dSpin_; a.site_out = dSite_; a.sums = dSums_;
   NEGF_TRY(density_spin(a, st_));
+  if (currents_) {
+    CurrentArgs c{};
+    c.n = M_; c.norb = p_.norb; c.npx = p_.npx; c.npy = p_.npy; c.npz = p_.npz; c.batch = B; c.nf = nf_;
+    c.items = dItems_; c.Hall = dH_; c.Hop = dHop_;
+    c.Px1 = dPx1_; c.Py1 = dPy1_; c.Pz1 = dPz1_; c.Px2 = dPx2_; c.Py2 = dPy2_; c.Pz2 = dPz2_;
+    c.sP = a.sP;
+    c.q2_over_hbar = kQ * kQ / kHbar;
+    c.site_out = dSite_;
+    NEGF_TRY(bond_currents(c, st_));
+  }
   const size_t np = (size_t)B * sums_blocks_ * 2;
   NEGF_CUDA_TRY(cudaMemcpyAsync(hPin_, dSums_, sizeof(double) * np, cudaMemcpyDeviceToHost, st_));
   NEGF_CUDA_TRY(cudaStreamSynchronize(st_));
@@ -657,8 +719,8 @@ int Engine::densities_impl(const std::vector<Item>& items, std::vector<double>& 
 // -------------------------------------------------------------------------------------
 // Batched solve
 // -------------------------------------------------------------------------------------
-int Engine::batch_solve(const negf_request* req, int n, negf_result* res, double* RhoN, double* RhoP, double* SigX,
-                        double* SigY, double* SigZ, double* site_items) {
+int Engine::batch_solve(const negf_request* req, int n, negf_result* res, double* const* outs,
+                        double* site_items) {
   if (n < 0 || (n > 0 && (!req || !res))) return NEGF_EINVAL;
   NEGF_CUDA_TRY(cudaSetDevice(p_.device));
   const long long total = nsite_total();
@@ -668,7 +730,7 @@ int Engine::batch_solve(const negf_request* req, int n, negf_result* res, double
     if (s < 0 || s >= nslots) return NEGF_EINVAL;
     if (!slot_set_[s]) return NEGF_ENOHAM;
   }
-  NEGF_CUDA_TRY(cudaMemsetAsync(dAcc_, 0, sizeof(double) * nslots * 5 * total, st_));
+  NEGF_CUDA_TRY(cudaMemsetAsync(dAcc_, 0, sizeof(double) * nslots * nf_ * total, st_));
   for (int c0 = 0; c0 < n; c0 += B_) {
     const int nb = std::min(B_, n - c0);
     // Sancho-Rubio problems: one per (energy, lead class), two if H_1 != H_N
@@ -707,10 +769,10 @@ int Engine::batch_solve(const negf_request* req, int n, negf_result* res, double
     NEGF_TRY(solve_rgf(items, false));
     std::vector<double> ed, hd;
     NEGF_TRY(densities(items, ed, hd));
-    NEGF_TRY(reduce_sites(nb, (int)total, nslots, dItems_, dSite_, dAcc_, st_));
+    NEGF_TRY(reduce_sites(nb, (int)total, nf_, nslots, dItems_, dSite_, dAcc_, st_));
     if (site_items)
-      NEGF_CUDA_TRY(cudaMemcpyAsync(site_items + (size_t)c0 * 5 * total, dSite_, sizeof(double) * 5 * total * nb,
-                                    cudaMemcpyDeviceToHost, st_));
+      NEGF_CUDA_TRY(cudaMemcpyAsync(site_items + (size_t)c0 * nf_ * total, dSite_,
+                                    sizeof(double) * nf_ * total * nb, cudaMemcpyDeviceToHost, st_));
     std::vector<double> tr(4 * (size_t)nb);
     std::vector<int> rst(nb);
     NEGF_CUDA_TRY(cudaMemcpyAsync(tr.data(), dTr_, sizeof(double) * 4 * nb, cudaMemcpyDeviceToHost, st_));
@@ -733,15 +795,15 @@ int Engine::batch_solve(const negf_request* req, int n, negf_result* res, double
     }
   }
   // add the slot-resolved site sums into the caller's arrays
-  const size_t acc_n = (size_t)nslots * 5 * total;
+  const size_t acc_n = (size_t)nslots * nf_ * total;
   NEGF_CUDA_TRY(cudaMemcpyAsync(hPin_, dAcc_, sizeof(double) * acc_n, cudaMemcpyDeviceToHost, st_));
   NEGF_CUDA_TRY(cudaStreamSynchronize(st_));
-  double* outs[5] = {RhoN, RhoP, SigX, SigY, SigZ};
-  for (int f = 0; f < 5; ++f) {
-    if (!outs[f]) continue;
-    if (f >= 2 && !p_.calc_spin) continue;
+  for (int f = 0; f < nf_; ++f) {
+    if (!outs || !outs[f]) continue;
+    if (f >= 2 && f < 5 && !p_.calc_spin) continue;
     for (int s = 0; s < nslots; ++s)
-      for (long long i = 0; i < total; ++i) outs[f][(size_t)s * total + i] += hPin_[((size_t)s * 5 + f) * total + i];
+      for (long long i = 0; i < total; ++i)
+        outs[f][(size_t)s * total + i] += hPin_[((size_t)s * nf_ + f) * total + i];
   }
   return NEGF_OK;   // per-request failures are reported in res[i].status
 }

@@ -22,6 +22,8 @@ class Engine {
   ~Engine();
   int init(const negf_params& p);
   int set_hamiltonian(int slot, const double* Htotd, const double* HopX);
+  // Htotd of `slot` generated on the device from a wire model (Build_Hamiltonian)
+  int build_hamiltonian(int slot, const negf_wire_model& m);
 
   // Sancho-Rubio for a list of problems; outputs into sr_* buffers (index = problem)
   int solve_sr(const std::vector<SrJob>& jobs, std::vector<int>& status, std::vector<int>& iters);
@@ -30,10 +32,11 @@ class Engine {
   // densities/spin for the current batch (after solve_rgf) with the items' f1,f2,dE
   int densities(const std::vector<Item>& items, std::vector<double>& edens, std::vector<double>& hdens);
 
-  // site_items (optional): n x 5 x nsite_total per-request dE-weighted site arrays, so a
-  // caller can sum energies in its own fixed order
-  int batch_solve(const negf_request* req, int n, negf_result* res, double* RhoN, double* RhoP, double* SigX,
-                  double* SigY, double* SigZ, double* site_items = nullptr);
+  // outs[8] = RhoN, RhoP, SigX, SigY, SigZ, Jx, Jy, Jz (each may be null).  site_items
+  // (optional): n x nf_ x nsite_total per-request dE-weighted site arrays, so a caller can
+  // sum energies in its own fixed order
+  int batch_solve(const negf_request* req, int n, negf_result* res, double* const* outs,
+                  double* site_items = nullptr);
 
   // accessors used by the per-energy API
   int M() const { return M_; }
@@ -62,12 +65,21 @@ class Engine {
   std::vector<int> slot_rep_, slot_joint_;
   void recompute_lead_classes();
   double2* dSpin_ = nullptr;
+  double2* dHtab_ = nullptr;   // build_hamiltonian: site-block table (16 * (2 + npz))
+  double* dVext_ = nullptr;    // build_hamiltonian: caller's potential (npx*npy*npz)
 
   // batch workspace
   double2 *dG_ = nullptr, *dC1_ = nullptr, *dCN_ = nullptr, *dZ_ = nullptr, *dY_ = nullptr, *dQ_ = nullptr;
   double2 *dSigL_ = nullptr, *dSigR_ = nullptr, *dGamL_ = nullptr, *dGamR_ = nullptr;
   double2 *dP1_ = nullptr, *dP2_ = nullptr;
   double2 *dCol1_ = nullptr, *dColN_ = nullptr;  // optional full columns for item 0
+  // bond currents (calc_currents): +x/+y/+z neighbour site blocks of each lead, and second
+  // buffers for Y = G(:,1) Gamma_L and G(:,N) so that slices x and x+1 are both at hand
+  bool currents_ = false;
+  int nf_ = 5;   // site fields per item: RhoN, RhoP, SigX, SigY, SigZ (+ Jx, Jy, Jz)
+  double2 *dPx1_ = nullptr, *dPy1_ = nullptr, *dPz1_ = nullptr;
+  double2 *dPx2_ = nullptr, *dPy2_ = nullptr, *dPz2_ = nullptr;
+  double2 *dYalt_ = nullptr, *dCNalt_ = nullptr;
   double* dSite_ = nullptr;
   double* dSums_ = nullptr;
   double* dTr_ = nullptr;
@@ -109,6 +121,7 @@ class Engine {
   double2* dT_ = nullptr;
   SlicedOperand sa_, sb_, sw_;   // sw_: slices of the matrix under inversion (kept across NS steps)
   unsigned long long* dRnorm_ = nullptr;
+  int* dNsActive_ = nullptr;  // per-matrix flags of the Newton-Schulz steps beyond ns_steps_
   int* dTcErr_ = nullptr;
   long long fallbacks_ = 0;
   double last_rnorm_max_ = 0.0;
@@ -132,7 +145,7 @@ class Engine {
   int cur_sr_status_ = 0;
   int cur_sr_iters_ = 0;
   int cur_rgf_status_ = 0;
-  std::vector<double> last_site_;  // 5 * nsite_total for item 0
+  std::vector<double> last_site_;  // nf_ * nsite_total for item 0
   double last_edens_ = 0.0, last_hdens_ = 0.0;
   bool keep_columns_ = false;
 
@@ -145,6 +158,8 @@ class Engine {
   int gemm_tc_nn(int batch, const double2* A, long long sA, const double2* B, long long sB, double2* C, long long sC,
                  double2 alpha, double2 beta, int slices);
   int merge_info(int batch);
+  // upload HopX (M x M) and its site-block form; a changed HopX invalidates every slot
+  int set_hopx(const double2* hx);
 };
 
 int merge_info_kernel_launch(int batch, const int* info, int* status, cudaStream_t st);

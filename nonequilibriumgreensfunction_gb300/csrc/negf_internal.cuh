@@ -16,6 +16,11 @@
 
 namespace negf {
 
+// physical constants of Source/Constants.F90:4-6
+constexpr double kQ = 1.602e-19;
+constexpr double kH = 6.626e-34;
+constexpr double kHbar = kH / (2.0 * 3.14159265358979323846);
+
 // ----------------------------------------------------------------------------------
 // complex helpers (double2 = (re, im))
 // ----------------------------------------------------------------------------------
@@ -208,6 +213,12 @@ int hop_apply(const HopBD& h, int n, int batch, int left, Op op, const double2* 
 int site_blocks(int n, int norb, int batch, const double2* Y, long long sY, const double2* X, long long sX,
                 double2* P, long long sP, cudaStream_t st);
 
+// site_blocks for the site itself (P), its +y neighbour (Py) and its +z neighbour (Pz) in one
+// pass: Py[b][r][a] = sum_k Y[b](r,k) conj(X[b]((site(r)+1)*norb + a, k)), Pz with site + npy;
+// zero where the neighbour is outside the slice.  Same layout and stride as site_blocks.
+int site_pairs(int n, int norb, int npy, int npz, int batch, const double2* Y, long long sY, const double2* X,
+               long long sX, double2* P, double2* Py, double2* Pz, long long sP, cudaStream_t st);
+
 // out[b] = Re sum_ij Q[b](i,j) conj(X[b](i,j))   (trace of Q X^H), one value per item.
 int trace_dot(int n, int batch, const double2* Q, long long sQ, const double2* X, long long sX,
               double* out, int out_stride, cudaStream_t st);
@@ -239,10 +250,11 @@ int sr_sigma(const HopBD& h, int n, int nprob, int lead, const double2* g, long 
              long long sSig, double2* gam, long long sGam, double* dos, cudaStream_t st);
 
 // density / spin from the site blocks of both leads.  P1, P2: [item][x][n][norb].
-// site_out: [item][5][npx*npy*npz] = (RhoN, RhoP, SigX, SigY, SigZ) already weighted
-// by dE/(2 pi); sums: [item][2] = (EDensity, HDensity).
+// site_out: [item][nf][npx*npy*npz], fields 0..4 = (RhoN, RhoP, SigX, SigY, SigZ) already
+// weighted by dE/(2 pi) (fields 5..7 = Jx, Jy, Jz when nf = 8, bond_currents);
+// sums: [item][2] = (EDensity, HDensity).
 struct DensityArgs {
-  int n, norb, npx, npy, npz, batch, calc_spin;
+  int n, norb, npx, npy, npz, batch, calc_spin, nf;
   const Item* items;
   const double2* P1; const double2* P2; long long sP;
   const double2* spin_ops;  // 3 * norb*norb (row-major)
@@ -251,8 +263,24 @@ struct DensityArgs {
 };
 int density_spin(const DensityArgs& a, cudaStream_t st);
 
-// acc[slot][f][i] += sum over items b with items[b].slot == slot (in order) of site_out[b][f][i]
-int reduce_sites(int batch, int nsite_total, int nslots, const Item* items, const double* site_out,
+// bond currents into site_out fields 5..7 (Jx, Jy, Jz), dE/(2 pi)-weighted, from the
+// neighbour blocks of both leads: Px[item][x][n][norb] = P(x, x+1; r, site(r)*norb + a),
+// Py/Pz as site_pairs writes them; Hall as FormW, Hop = HopX (dense, column-major).
+struct CurrentArgs {
+  int n, norb, npx, npy, npz, batch, nf;
+  const Item* items;
+  const double2* Hall;
+  const double2* Hop;
+  const double2 *Px1, *Py1, *Pz1, *Px2, *Py2, *Pz2;
+  long long sP;
+  double q2_over_hbar;
+  double* site_out;
+};
+int bond_currents(const CurrentArgs& a, cudaStream_t st);
+
+// acc[slot][f][i] += sum over items b with items[b].slot == slot (in order) of
+// site_out[b][f][i], f < nf
+int reduce_sites(int batch, int nsite_total, int nf, int nslots, const Item* items, const double* site_out,
                  double* acc, cudaStream_t st);
 
 // mixed form: precision conversion and the Newton-Schulz residual R = I - T (in place),
@@ -262,5 +290,7 @@ int to_f64(int n, int batch, const float2* src, long long sS, double2* dst, long
 int split_copy(int n, int batch, const double2* src, long long sS, double2* d64, long long s64, float2* d32,
                long long s32, cudaStream_t st);
 int ns_residual(int n, int batch, double2* T, long long sT, unsigned long long* rnorm, cudaStream_t st);
+// A[b] = 0 for every b with keep[b] == 0 (device flags)
+int zero_unmasked(int n, int batch, const int* keep, double2* A, long long sA, cudaStream_t st);
 
 }  // namespace negf

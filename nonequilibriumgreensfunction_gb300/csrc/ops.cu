@@ -130,6 +130,59 @@ __global__ void __launch_bounds__(SB_ROWS* SB_KSPLIT) site_blocks_kernel(int n, 
   }
 }
 
+// ---- in-slice neighbour blocks ------------------------------------------------------
+// For the row r of site s = r / no (s = y + z*npy):
+//   P0[r][a] = sum_k Y(r,k) conj(X(s*no + a, k))            (the site itself)
+//   P1[r][a] = same with site s + 1    (next y; zero when y = npy - 1)
+//   P2[r][a] = same with site s + npy  (next z; zero when z = npz - 1)
+// One pass over Y serves all three; the k split is reduced in shared memory per output in a
+// fixed order, so P0 equals what site_blocks_kernel writes.
+__global__ void __launch_bounds__(SB_ROWS* SB_KSPLIT) site_pairs_kernel(int n, int no, int npy, int npz,
+                                                                        const double2* Y, long long sY,
+                                                                        const double2* X, long long sX, double2* P0,
+                                                                        double2* P1, double2* P2, long long sP) {
+  __shared__ double2 part[SB_KSPLIT][SB_ROWS][4];
+  const int b = blockIdx.y;
+  const int lr = threadIdx.x % SB_ROWS, kg = threadIdx.x / SB_ROWS;
+  const int r = blockIdx.x * SB_ROWS + lr;
+  const double2* Yb = Y + (long long)b * sY;
+  const double2* Xb = X + (long long)b * sX;
+  double2 acc[3][4];
+  for (int d = 0; d < 3; ++d)
+    for (int a = 0; a < 4; ++a) acc[d][a] = make_double2(0, 0);
+  int base[3] = {-1, -1, -1};
+  if (r < n) {
+    const int s = r / no;
+    const int y = s % npy, z = s / npy;
+    base[0] = s * no;
+    if (y < npy - 1) base[1] = (s + 1) * no;
+    if (z < npz - 1) base[2] = (s + npy) * no;
+    const int k_per = (n + SB_KSPLIT - 1) / SB_KSPLIT;
+    const int k_lo = kg * k_per, k_hi = min(n, k_lo + k_per);
+    for (int k = k_lo; k < k_hi; ++k) {
+      const double2 yv = Yb[(long long)k * n + r];
+      const double2* xk = Xb + (long long)k * n;
+      for (int d = 0; d < 3; ++d) {
+        if (base[d] < 0) continue;
+        for (int a = 0; a < no && a < 4; ++a) cfma(acc[d][a], yv, cconj(xk[base[d] + a]));
+      }
+    }
+  }
+  double2* outs[3] = {P0, P1, P2};
+  for (int d = 0; d < 3; ++d) {
+    for (int a = 0; a < 4; ++a) part[kg][lr][a] = acc[d][a];
+    __syncthreads();
+    if (kg == 0 && r < n) {
+      for (int a = 0; a < no && a < 4; ++a) {
+        double2 v = part[0][lr][a];
+        for (int q = 1; q < SB_KSPLIT; ++q) v = cadd(v, part[q][lr][a]);
+        outs[d][(long long)b * sP + (long long)r * no + a] = v;
+      }
+    }
+    __syncthreads();
+  }
+}
+
 // ---- Re sum Q .* conj(X) (one CTA per item, fixed reduction order) -------------------
 __global__ void trace_dot_kernel(int n, const double2* Q, long long sQ, const double2* X, long long sX, double* out,
                                  int out_stride) {
@@ -337,7 +390,7 @@ __global__ void density_spin_kernel(DensityArgs a) {
     }
     // site arrays are (x, y, z) column-major: x fastest
     const long long o = (long long)x + (long long)a.npx * (y + (long long)a.npy * z);
-    double* so = a.site_out + (long long)b * 5 * total;
+    double* so = a.site_out + (long long)b * a.nf * total;
     so[o] = rn * w;
     so[total + o] = rp * w;
     so[2 * total + o] = sp[0] * w;
@@ -365,10 +418,73 @@ __global__ void density_spin_kernel(DensityArgs a) {
   }
 }
 
-__global__ void reduce_sites_kernel(int batch, int total, int nslots, const Item* items, const double* site_out,
-                                    double* acc) {
+// ---- bond currents, Source/Calculate_Observables.F90:110-169 -----------------------------
+// One thread per site (x, y, z) of one item.  With Gn = f1 P1 + f2 P2, Gp = (1-f1) P1 +
+// (1-f2) P2 and the Hermitian symmetry Gn(b,a) = conj(Gn(a,b)), each orbital pair (i, j)
+// of a bond a -> b contributes
+//   dumVar = REAL(4)( Re( i q^2/hbar (H(a,b) Gn(b,a) - Gn(a,b) H(b,a) - H(a,b) Gp(b,a)
+//                                    + Gp(a,b) H(b,a)) ) )
+// and J += dumVar dE/(2 pi) in REAL(8), as the reference's dumVar (:7) is REAL(4).  The x
+// bond couples the same site of slices x and x+1 through HopX(a,a) and its conjugate
+// (:150-156).  Writes site_out fields 5, 6, 7 = Jx, Jy, Jz.
+__global__ void bond_currents_kernel(CurrentArgs a) {
+  const int b = blockIdx.y;
+  const int nsite = a.npy * a.npz;
+  const int total = a.npx * nsite;
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= total) return;
+  const int no = a.norb;
+  const Item it = a.items[b];
+  const double w = it.dE / (2.0 * 3.14159265358979323846);
+  const double pref = a.q2_over_hbar;
+  const int x = idx / nsite, s = idx % nsite;
+  const int y = s % a.npy, z = s / a.npy;
+  const long long n = a.n;
+  const double2* H = a.Hall + ((long long)it.slot * a.npx + x) * n * n;
+  const long long prow = (long long)b * a.sP + ((long long)x * n + (long long)s * no) * no;
+  const double f1 = it.f1, f2 = it.f2;
+  // one bond term given the two lead blocks of P(a_i, b_j) and H(a_i, b_j), H(b_j, a_i)
+  auto term = [&](double2 p1, double2 p2, double2 hab, double2 hba) -> double {
+    const double2 gn = make_double2(f1 * p1.x + f2 * p2.x, f1 * p1.y + f2 * p2.y);
+    const double2 gp = make_double2((1.0 - f1) * p1.x + (1.0 - f2) * p2.x, (1.0 - f1) * p1.y + (1.0 - f2) * p2.y);
+    double2 v = csub(cmul(hab, cconj(gn)), cmul(gn, hba));
+    v = csub(v, cmul(hab, cconj(gp)));
+    v = cadd(v, cmul(gp, hba));
+    const float dum = __double2float_rn(-pref * v.y);   // Re(i c v) = -c Im v
+    return (double)dum * w;
+  };
+  double j[3] = {0.0, 0.0, 0.0};
+  if (x < a.npx - 1) {
+    const double2* hop = a.Hop;
+    for (int ii = 0; ii < no; ++ii)
+      for (int jj = 0; jj < no; ++jj) {
+        const long long ri = (long long)s * no + ii, rj = (long long)s * no + jj;
+        const double2 hx = hop[rj * n + ri];
+        j[0] += term(a.Px1[prow + ii * no + jj], a.Px2[prow + ii * no + jj], hx, cconj(hx));
+      }
+  }
+  const double2* pb1[2] = {a.Py1, a.Pz1};
+  const double2* pb2[2] = {a.Py2, a.Pz2};
+  const int nb_site[2] = {y < a.npy - 1 ? s + 1 : -1, z < a.npz - 1 ? s + a.npy : -1};
+  for (int d = 0; d < 2; ++d) {
+    if (nb_site[d] < 0) continue;
+    for (int ii = 0; ii < no; ++ii)
+      for (int jj = 0; jj < no; ++jj) {
+        const long long ra = (long long)s * no + ii, rb = (long long)nb_site[d] * no + jj;
+        j[1 + d] += term(pb1[d][prow + ii * no + jj], pb2[d][prow + ii * no + jj], H[rb * n + ra], H[ra * n + rb]);
+      }
+  }
+  const long long o = (long long)x + (long long)a.npx * (y + (long long)a.npy * z);
+  double* so = a.site_out + (long long)b * a.nf * total;
+  so[5LL * total + o] = j[0];
+  so[6LL * total + o] = j[1];
+  so[7LL * total + o] = j[2];
+}
+
+__global__ void reduce_sites_kernel(int batch, int total, int nf, int nslots, const Item* items,
+                                    const double* site_out, double* acc) {
   const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  const long long per_slot = 5LL * total;
+  const long long per_slot = (long long)nf * total;
   if (i >= per_slot * nslots) return;
   const int slot = (int)(i / per_slot);
   const long long f = i % per_slot;
@@ -401,6 +517,26 @@ int site_blocks(int n, int norb, int batch, const double2* Y, long long sY, cons
   if (norb > 4) return NEGF_EINVAL;
   dim3 grid((n + SB_ROWS - 1) / SB_ROWS, batch);
   site_blocks_kernel<<<grid, SB_ROWS * SB_KSPLIT, 0, st>>>(n, norb, Y, sY, X, sX, P, sP);
+  NEGF_CUDA_TRY(cudaGetLastError());
+  count_launch();
+  return NEGF_OK;
+}
+
+int site_pairs(int n, int norb, int npy, int npz, int batch, const double2* Y, long long sY, const double2* X,
+               long long sX, double2* P, double2* Py, double2* Pz, long long sP, cudaStream_t st) {
+  if (norb > 4 || n != norb * npy * npz) return NEGF_EINVAL;
+  dim3 grid((n + SB_ROWS - 1) / SB_ROWS, batch);
+  site_pairs_kernel<<<grid, SB_ROWS * SB_KSPLIT, 0, st>>>(n, norb, npy, npz, Y, sY, X, sX, P, Py, Pz, sP);
+  NEGF_CUDA_TRY(cudaGetLastError());
+  count_launch();
+  return NEGF_OK;
+}
+
+int bond_currents(const CurrentArgs& a, cudaStream_t st) {
+  if (a.norb > 4 || a.nf < 8) return NEGF_EINVAL;
+  const int total = a.npx * a.npy * a.npz;
+  dim3 grid((total + 127) / 128, a.batch);
+  bond_currents_kernel<<<grid, 128, 0, st>>>(a);
   NEGF_CUDA_TRY(cudaGetLastError());
   count_launch();
   return NEGF_OK;
@@ -486,10 +622,11 @@ int density_spin(const DensityArgs& a, cudaStream_t st) {
   return NEGF_OK;
 }
 
-int reduce_sites(int batch, int nsite_total, int nslots, const Item* items, const double* site_out, double* acc,
-                 cudaStream_t st) {
-  const long long n = 5LL * nsite_total * nslots;
-  reduce_sites_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(batch, nsite_total, nslots, items, site_out, acc);
+int reduce_sites(int batch, int nsite_total, int nf, int nslots, const Item* items, const double* site_out,
+                 double* acc, cudaStream_t st) {
+  const long long n = (long long)nf * nsite_total * nslots;
+  reduce_sites_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(batch, nsite_total, nf, nslots, items, site_out,
+                                                                   acc);
   NEGF_CUDA_TRY(cudaGetLastError());
   count_launch();
   return NEGF_OK;
@@ -585,6 +722,24 @@ int split_copy(int n, int batch, const double2* src, long long sS, double2* d64,
 
 int to_f64(int n, int batch, const float2* src, long long sS, double2* dst, long long sD, cudaStream_t st) {
   to_f64_kernel<<<ew_grid((long long)n * n, batch), EW_THREADS, 0, st>>>(n, src, sS, dst, sD);
+  NEGF_CUDA_TRY(cudaGetLastError());
+  count_launch();
+  return NEGF_OK;
+}
+
+namespace {
+__global__ void zero_unmasked_kernel(int n, const int* keep, double2* A, long long sA) {
+  const int b = blockIdx.y;
+  if (keep[b]) return;
+  const long long nn = (long long)n * n;
+  double2* Ab = A + (long long)b * sA;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nn; e += (long long)gridDim.x * blockDim.x)
+    Ab[e] = make_double2(0.0, 0.0);
+}
+}  // namespace
+
+int zero_unmasked(int n, int batch, const int* keep, double2* A, long long sA, cudaStream_t st) {
+  zero_unmasked_kernel<<<dim3(64, batch), 256, 0, st>>>(n, keep, A, sA);
   NEGF_CUDA_TRY(cudaGetLastError());
   count_launch();
   return NEGF_OK;

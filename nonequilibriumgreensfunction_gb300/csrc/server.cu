@@ -44,6 +44,9 @@ struct Request {
   int64_t id = 0;
   GeomKey key{};
   std::vector<double2> H, hop;
+  bool has_model = false;       // generate H on the device from `model` (and V)
+  negf_wire_model model{};
+  std::vector<double> V;
   std::vector<double> e, f1, f2, dE;
   std::vector<double> res7;   // 7 per energy
   std::vector<double> rho;    // RhoN then RhoP, npx*npy*npz each
@@ -195,7 +198,8 @@ struct negf_server {
     cudaSetDevice(p.device);
     negf::Engine& eng = *w->eng;
     const long long total = (long long)w->key.npx * w->key.npy * w->key.npz;
-    std::vector<double> items(5 * total * (size_t)p.max_batch);
+    const int nf = eng.nf_;
+    std::vector<double> items((size_t)nf * total * (size_t)p.max_batch);
     std::unique_lock<std::mutex> lk(mu);
     for (;;) {
       work_cv.wait(lk, [&] {
@@ -213,9 +217,16 @@ struct negf_server {
       if (!up.empty()) {
         lk.unlock();
         std::vector<int> st(up.size());
-        for (size_t i = 0; i < up.size(); ++i)
-          st[i] = eng.set_hamiltonian(up[i]->slot, reinterpret_cast<const double*>(up[i]->H.data()),
-                                      reinterpret_cast<const double*>(up[i]->hop.data()));
+        for (size_t i = 0; i < up.size(); ++i) {
+          Request* r = up[i];
+          if (r->has_model) {
+            r->model.V = r->V.empty() ? nullptr : r->V.data();
+            st[i] = eng.build_hamiltonian(r->slot, r->model);
+          } else {
+            st[i] = eng.set_hamiltonian(r->slot, reinterpret_cast<const double*>(r->H.data()),
+                                        reinterpret_cast<const double*>(r->hop.data()));
+          }
+        }
         lk.lock();
         const double t = now();
         for (size_t i = 0; i < up.size(); ++i) {
@@ -241,8 +252,7 @@ struct negf_server {
       int rc = NEGF_OK;
       if (!batch.empty()) {
         lk.unlock();
-        rc = eng.batch_solve(batch.data(), (int)batch.size(), res.data(), nullptr, nullptr, nullptr, nullptr, nullptr,
-                             items.data());
+        rc = eng.batch_solve(batch.data(), (int)batch.size(), res.data(), nullptr, items.data());
         lk.lock();
       }
       // scatter results; each energy's densities are added to its request in energy order
@@ -259,7 +269,7 @@ struct negf_server {
         const int stv = rc != NEGF_OK ? rc : o.status;
         if (stv != 0 && r->status == 0) r->status = stv;
         r->n_done++;
-        const double* si = items.data() + i * 5 * (size_t)total;
+        const double* si = items.data() + i * nf * (size_t)total;
         for (long long j = 0; j < total; ++j) {
           r->rho[j] += si[j];
           r->rho[total + j] += si[total + j];
@@ -318,15 +328,32 @@ int negf_server_create(const negf_serve_params* p, negf_server** out) {
 }
 
 int negf_server_submit(negf_server* s, const negf_wire_request* r, int64_t* id) {
-  if (!s || !r || !id || !r->Htotd || !r->HopX || r->n_energies < 1 || !r->energies || !r->f1 || !r->f2 || !r->dE)
-    return NEGF_EINVAL;
+  if (!s || !r || !id || r->n_energies < 1 || !r->energies || !r->f1 || !r->f2 || !r->dE) return NEGF_EINVAL;
+  if (r->model ? (r->Htotd || r->HopX || r->norb != 4) : (!r->Htotd || !r->HopX)) return NEGF_EINVAL;
   if (r->npx < 2 || r->npy < 1 || r->npz < 1 || r->norb < 1 || r->norb > 4) return NEGF_EINVAL;
   auto q = std::make_unique<Request>();
   const long long m = (long long)r->norb * r->npy * r->npz, mm = m * m;
-  const double2* h = reinterpret_cast<const double2*>(r->Htotd);
   const double2* x = reinterpret_cast<const double2*>(r->HopX);
-  q->H.assign(h, h + r->npx * mm);
-  q->hop.assign(x, x + mm);
+  std::vector<double2> hop_model;
+  if (r->model) {
+    for (int i = 0; i < 8; ++i)
+      if (r->model->reserved[i] != 0) return NEGF_EINVAL;
+    q->has_model = true;
+    q->model = *r->model;
+    if (r->model->V) q->V.assign(r->model->V, r->model->V + (size_t)r->npx * r->npy * r->npz);
+    // the dense HopX the device build produces keys the geometry, so model and uploaded
+    // wires with the same HopX share a worker
+    hop_model.assign(mm, make_double2(0.0, 0.0));
+    for (long long st = 0; st < m / 4; ++st)
+      for (int a = 0; a < 4; ++a)
+        for (int b = 0; b < 4; ++b)
+          hop_model[(st * 4 + b) * m + st * 4 + a] = make_double2(r->model->hop[0][a][b][0], r->model->hop[0][a][b][1]);
+    x = hop_model.data();
+  } else {
+    const double2* h = reinterpret_cast<const double2*>(r->Htotd);
+    q->H.assign(h, h + r->npx * mm);
+    q->hop.assign(x, x + mm);
+  }
   q->e.assign(r->energies, r->energies + r->n_energies);
   q->f1.assign(r->f1, r->f1 + r->n_energies);
   q->f2.assign(r->f2, r->f2 + r->n_energies);

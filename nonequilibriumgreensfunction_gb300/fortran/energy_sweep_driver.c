@@ -10,7 +10,8 @@
  * Energies: n_e uniform points in [e_min, e_max]; T = 0 steps f_c = [E <= mu_c]
  * (Energy_Sweep.F90:11-21); dE from the energy spacing (Energy_Sweep.F90:7-9).
  * out.bin: per energy (T12, EDensity, HDensity, Modec1, Modec2, DOSc1, DOSc2) followed by
- * the energy-integrated RhoN and RhoP (npx*npy*npz each) and ContactCurrent[2].
+ * the energy-integrated RhoN and RhoP (npx*npy*npz each), ContactCurrent[2] and the bond
+ * currents Jx, Jy, Jz (npx*npy*npz each, Calculate_Observables.F90:110-169).
  */
 #include <stdio.h>
 #include <stdlib.h>
@@ -39,6 +40,7 @@ int main(int argc, char** argv) {
   p.n_hamiltonians = 1; p.max_batch = 1;
   p.eta = atof(argv[6]); p.sr_tol = atof(argv[7]); p.sr_max_iter = 20000;
   p.precision = NEGF_PREC_FP64;
+  p.calc_currents = 1;
   const double mu1 = atof(argv[8]), mu2 = atof(argv[9]);
   const int n_e = atoi(argv[10]);
   const double e_min = atof(argv[11]), e_max = atof(argv[12]);
@@ -54,10 +56,14 @@ int main(int argc, char** argv) {
   st = negf_set_hamiltonian(h, 0, htotd, hopx);
   if (st) { fprintf(stderr, "negf_set_hamiltonian: %s\n", negf_strerror(st)); return 1; }
 
-  double* out = (double*)calloc(7 * (size_t)n_e + 2 * nsites + 2, sizeof(double));
+  const size_t n_out = 7 * (size_t)n_e + 5 * nsites + 2;
+  double* out = (double*)calloc(n_out, sizeof(double));
   double* rhon = out + 7 * (size_t)n_e;
   double* rhop = rhon + nsites;
   double* cc = rhop + nsites;
+  double* jx = cc + 2;
+  double* jy = jx + nsites;
+  double* jz = jy + nsites;
   const double de0 = n_e > 1 ? (e_max - e_min) / (n_e - 1) : 0.0;
   double dE = de0;
   int failures = 0;
@@ -74,12 +80,14 @@ int main(int argc, char** argv) {
     if (st) { fprintf(stderr, "E=%g Calculate_Gnp: %s\n", energy, negf_strerror(st)); ++failures; }
     st = negf_calculate_observables(h, dE, f1, f2, &t12, &ed, &hd, modes, cc, NULL, NULL, NULL);
     if (st) { fprintf(stderr, "E=%g Calculate_Observables: %s\n", energy, negf_strerror(st)); ++failures; }
+    st = negf_calculate_currents(h, jx, jy, jz);
+    if (st) { fprintf(stderr, "E=%g bond currents: %s\n", energy, negf_strerror(st)); ++failures; }
     double* o = out + 7 * (size_t)k;
     o[0] = t12; o[1] = ed; o[2] = hd; o[3] = modes[0]; o[4] = modes[1]; o[5] = dosc[0]; o[6] = dosc[1];
   }
   FILE* f = fopen(argv[13], "wb");
   if (!f) return 2;
-  fwrite(out, sizeof(double), 7 * (size_t)n_e + 2 * nsites + 2, f);
+  fwrite(out, sizeof(double), n_out, f);
   fclose(f);
   negf_destroy(h);
   free(out); free(htotd); free(hopx);

@@ -27,7 +27,8 @@ MODULE negf_gpu_shim
         INTEGER(C_INT32_T) :: npx, npy, npz, norb, n_hamiltonians, max_batch
         REAL(C_DOUBLE)     :: eta, sr_tol
         INTEGER(C_INT32_T) :: sr_max_iter, calc_spin, precision, device, mixed_slices, keep_g_columns
-        INTEGER(C_INT32_T) :: reserved(6)
+        INTEGER(C_INT32_T) :: residual_slices, sr_slices, calc_currents
+        INTEGER(C_INT32_T) :: reserved(3)
         REAL(C_DOUBLE)     :: spin_ops(2, 4, 4, 3)   ! C order [3][4][4][2]
     END TYPE
 
@@ -72,6 +73,11 @@ MODULE negf_gpu_shim
             REAL(C_DOUBLE)        :: t12, eden, hden, modes(2), cc(2)
             TYPE(C_PTR), VALUE    :: sx, sy, sz
         END FUNCTION
+        INTEGER(C_INT) FUNCTION negf_calculate_currents(h, jx, jy, jz) BIND(C, NAME="negf_calculate_currents")
+            IMPORT :: C_INT, C_PTR, C_DOUBLE
+            TYPE(C_PTR), VALUE    :: h
+            REAL(C_DOUBLE)        :: jx(*), jy(*), jz(*)
+        END FUNCTION
     END INTERFACE
 
 CONTAINS
@@ -97,6 +103,7 @@ CONTAINS
             p%eta = eta_sigma; p%sr_tol = 1D-8; p%sr_max_iter = 20000
             p%calc_spin = calcSigExp; p%precision = 0; p%device = 0
             p%mixed_slices = 0; p%keep_g_columns = 0; p%reserved = 0
+            p%residual_slices = 0; p%sr_slices = 0; p%calc_currents = 1
             p%spin_ops = 0D0
             st = negf_create(p, negf_h)
             IF (st /= 0) STOP "negf_create failed"
@@ -161,4 +168,7 @@ SUBROUTINE Calculate_Observables
     HDensity(eCtr+1) = HDensity(eCtr+1) + hd
     Modec1(eCtr+1) = Modec1(eCtr+1) + modes(1)
     Modec2(eCtr+1) = Modec2(eCtr+1) + modes(2)
+    ! bond currents (Source/Calculate_Observables.F90:110-169)
+    st = negf_calculate_currents(negf_h, Jx, Jy, Jz)
+    CALL negf_shim_check(st, "Calculate_Observables (currents)")
 END SUBROUTINE Calculate_Observables

@@ -20,6 +20,8 @@ Arrays are returned slice-first: htotd[x, row, col], hopx[row, col].
 """
 from __future__ import annotations
 
+import math
+
 import numpy as np
 
 NORB = 4
@@ -111,4 +113,89 @@ def ti_wire(npx, npy, npz, M0=0.3, B=0.25, A=0.5, zeeman=0.0, flux=0.0, W=0.0, s
         diag = np.repeat(disorder.transpose(0, 2, 1).reshape(npx, nsite), NORB, axis=1)
         idx = np.arange(m)
         htotd[:, idx, idx] += diag
+    return htotd, hopx
+
+
+# ---------------------------------------------------------------------------------------
+# Counter-based wire model: the form negf_build_hamiltonian generates on the device
+# ---------------------------------------------------------------------------------------
+_GOLDEN_GAMMA = np.uint64(0x9E3779B97F4A7C15)
+_MIX1 = np.uint64(0xBF58476D1CE4E5B9)
+_MIX2 = np.uint64(0x94D049BB133111EB)
+
+
+def splitmix64(seed, i):
+    """Output ``i`` (array) of SplitMix64 seeded with ``seed`` (Steele, Lea, Flood 2014)."""
+    with np.errstate(over="ignore"):
+        z = np.uint64(seed) + np.asarray(i, dtype=np.uint64) * _GOLDEN_GAMMA
+        z = (z ^ (z >> np.uint64(30))) * _MIX1
+        z = (z ^ (z >> np.uint64(27))) * _MIX2
+        return z ^ (z >> np.uint64(31))
+
+
+def anderson_counter(npx, npy, npz, W, seed):
+    """Anderson potential (u - 1/2) W on slices 2..npx-1 with u = (s >> 11) 2^-53, s the
+    output x + npx (y + npy z) + 1 of SplitMix64(seed): the device's disorder stream."""
+    x, y, z = np.meshgrid(np.arange(npx), np.arange(npy), np.arange(npz), indexing="ij")
+    i = (x + npx * (y + npy * z)).astype(np.uint64) + np.uint64(1)
+    u = (splitmix64(seed, i) >> np.uint64(11)).astype(np.float64) * 2.0 ** -53
+    v = (u - 0.5) * W
+    v[0] = 0.0
+    v[npx - 1] = 0.0
+    return v
+
+
+def wire_model(M0=0.3, B=0.25, A=0.5, zeeman=0.0, flux=0.0, W=0.0, seed=0, basis="tau_sigma", V=None):
+    """Parameters of negf_build_hamiltonian: the 4x4 site blocks plus flux and disorder."""
+    onsite, hx, hy, hz = site_blocks(M0, B, A, zeeman, basis)
+    return dict(onsite=onsite, hops=(hx, hy, hz), flux=float(flux), W=float(W), seed=int(seed), V=V)
+
+
+def build_from_model(npx, npy, npz, model):
+    """Host twin of negf_build_hamiltonian: (htotd[npx, M, M], hopx[M, M]) with the same
+    arithmetic as the device path (the y-hop phase and its product with the block in plain
+    float operations, the potential added once to the on-site diagonal), so the two are
+    equal element for element."""
+    onsite = np.asarray(model["onsite"], dtype=complex)
+    hx, hy, hz = (np.asarray(h, dtype=complex) for h in model["hops"])
+    nsite = npy * npz
+    m = NORB * nsite
+    flux = model["flux"]
+    phased = flux != 0.0 and npy > 1 and npz > 1
+    hy_z = []
+    for z in range(npz):
+        if not phased:
+            hy_z.append(hy.copy())
+            continue
+        th = 2.0 * math.pi * z * flux / ((npy - 1) * (npz - 1))
+        c, s = math.cos(th), math.sin(th)
+        blk = np.empty((4, 4), dtype=complex)
+        for a in range(4):
+            for b in range(4):
+                hr, hi = float(hy[a, b].real), float(hy[a, b].imag)
+                blk[a, b] = complex(hr * c - hi * s, hr * s + hi * c)
+        hy_z.append(blk)
+    h = np.zeros((m, m), dtype=complex)
+    hopx = np.zeros((m, m), dtype=complex)
+    for z in range(npz):
+        for y in range(npy):
+            i = (y + z * npy) * NORB
+            s = slice(i, i + NORB)
+            h[s, s] = onsite
+            hopx[s, s] = hx
+            if y + 1 < npy:
+                t = slice(i + NORB, i + 2 * NORB)
+                h[s, t] = hy_z[z]
+                h[t, s] = hy_z[z].conj().T
+            if z + 1 < npz:
+                t = slice(i + NORB * npy, i + NORB * npy + NORB)
+                h[s, t] = hz
+                h[t, s] = hz.conj().T
+    v = model.get("V")
+    if v is None:
+        v = anderson_counter(npx, npy, npz, model["W"], model["seed"])
+    htotd = np.repeat(h[None], npx, axis=0)
+    diag = np.repeat(np.asarray(v).transpose(0, 2, 1).reshape(npx, nsite), NORB, axis=1)
+    idx = np.arange(m)
+    htotd[:, idx, idx] = (htotd[:, idx, idx].real + diag) + 1j * htotd[:, idx, idx].imag
     return htotd, hopx

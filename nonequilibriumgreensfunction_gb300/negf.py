@@ -44,7 +44,7 @@ def _to_fortran_blocks(htotd):
 class Solver:
     def __init__(self, npx, npy, npz, norb=4, n_hamiltonians=1, max_batch=1, eta=1e-4, sr_tol=1e-8,
                  sr_max_iter=20000, calc_spin=False, precision="fp64", device=0, keep_g_columns=False,
-                 spin_ops=None, mixed_slices=0, residual_slices=0, sr_slices=0):
+                 spin_ops=None, mixed_slices=0, residual_slices=0, sr_slices=0, calc_currents=False):
         self.lib = capi.load()
         p = NegfParams()
         p.npx, p.npy, p.npz, p.norb = npx, npy, npz, norb
@@ -57,6 +57,7 @@ class Solver:
         p.residual_slices = residual_slices
         p.sr_slices = sr_slices
         p.keep_g_columns = 1 if keep_g_columns else 0
+        p.calc_currents = 1 if calc_currents else 0
         if spin_ops is not None:
             ops = np.asarray(spin_ops, dtype=np.complex128)
             buf = np.zeros((3, 4, 4, 2))
@@ -70,6 +71,7 @@ class Solver:
         self.max_batch = max_batch
         self.n_hamiltonians = n_hamiltonians
         self.calc_spin = bool(calc_spin)
+        self.calc_currents = bool(calc_currents)
         h = ctypes.c_void_p()
         check(self.lib.negf_create(ctypes.byref(p), ctypes.byref(h)), "negf_create")
         self._h = h
@@ -134,6 +136,14 @@ class Solver:
                                             None if hopx_f is None else _ptr(hopx_f)),
               "negf_set_hamiltonian")
 
+    def build_hamiltonian(self, model, slot=0):
+        """Generate slot ``slot``'s Htotd (and HopX) on the device from a wire model
+        (``hamiltonian.wire_model``): Build_Hamiltonian.F90 without the host-to-device copy.
+        ``hamiltonian.build_from_model`` gives the identical arrays on the host."""
+        m, keep = capi.wire_model_struct(model, (self.npx, self.npy, self.npz))
+        check(self.lib.negf_build_hamiltonian(self._h, slot, ctypes.byref(m)), "negf_build_hamiltonian")
+        del keep
+
     # -- the reference's four subroutines --------------------------------------------
     def contact_self_energy(self, energy, want_matrices=True):
         m = self.M
@@ -182,21 +192,35 @@ class Solver:
             _ptr(modes), _ptr(cc), _ptr(sx), _ptr(sy), _ptr(sz)), "negf_calculate_observables")
         return dict(T12=t12.value, EDensity=ed.value, HDensity=hd.value, Modec1=modes[0], Modec2=modes[1])
 
-    def energy_sweep(self, energy, f1, f2, dE, rho_n=None, rho_p=None, contact_current=None, spin=None):
+    def calculate_currents(self, currents):
+        """Bond currents of Calculate_Observables.F90:110-169 for the energy of the last
+        calculate_gnp call, added into ``currents`` = (Jx, Jy, Jz), Fortran-ordered
+        (npx, npy, npz) float64 arrays (None entries are skipped)."""
+        jx, jy, jz = currents
+        for a in (jx, jy, jz):
+            if a is not None and not (a.flags.f_contiguous and a.dtype == np.float64):
+                raise ValueError("site arrays must be Fortran-ordered float64")
+        check(self.lib.negf_calculate_currents(self._h, _ptr(jx), _ptr(jy), _ptr(jz)), "negf_calculate_currents")
+
+    def energy_sweep(self, energy, f1, f2, dE, rho_n=None, rho_p=None, contact_current=None, spin=None,
+                     currents=None):
         """Energy_Sweep.F90:28-46 for one energy; returns the per-energy observables."""
         cse = self.contact_self_energy(energy, want_matrices=False)
         st = self.get_retarded_greens()
         self.calculate_gnp(f1, f2, dE, rho_n, rho_p)
         obs = self.calculate_observables(dE, f1, f2, contact_current, spin)
+        if currents is not None:
+            self.calculate_currents(currents)
         obs.update(dosc=cse["dosc"], sr_status=cse["status"], rgf_status=st)
         return obs
 
     # -- batched ---------------------------------------------------------------------
-    def solve_batch(self, energies, f1, f2, dE, slots=None, rho_n=None, rho_p=None, spin=None):
+    def solve_batch(self, energies, f1, f2, dE, slots=None, rho_n=None, rho_p=None, spin=None, currents=None):
         """Solve len(energies) energy points (chunked by max_batch on the device).
 
-        ``rho_n``/``rho_p``/``spin`` (if given) are (npx, npy, npz, n_hamiltonians)
-        Fortran-ordered arrays the dE-weighted densities are added to.
+        ``rho_n``/``rho_p``/``spin``/``currents`` (if given) are (npx, npy, npz,
+        n_hamiltonians) Fortran-ordered arrays the dE-weighted densities, spin densities
+        (SigX, SigY, SigZ) and bond currents (Jx, Jy, Jz) are added to.
         Returns a dict of per-request arrays."""
         energies = np.asarray(energies, dtype=np.float64)
         n = energies.size
@@ -213,8 +237,18 @@ class Solver:
         sx = sy = sz = None
         if spin is not None:
             sx, sy, sz = spin
-        rc = self.lib.negf_solve_batch(self._h, req, n, res, _ptr(rho_n), _ptr(rho_p), _ptr(sx), _ptr(sy), _ptr(sz))
-        check(rc, "negf_solve_batch")
+        if currents is None:
+            rc = self.lib.negf_solve_batch(self._h, req, n, res, _ptr(rho_n), _ptr(rho_p), _ptr(sx), _ptr(sy),
+                                           _ptr(sz))
+            check(rc, "negf_solve_batch")
+        else:
+            outs = capi.NegfBatchOutputs()
+            for name, a in zip(("RhoN", "RhoP", "SigX", "SigY", "SigZ", "Jx", "Jy", "Jz"),
+                               (rho_n, rho_p, sx, sy, sz) + tuple(currents)):
+                if a is not None and not (a.flags.f_contiguous and a.dtype == np.float64):
+                    raise ValueError("site arrays must be Fortran-ordered float64")
+                setattr(outs, name, None if a is None else a.ctypes.data)
+            check(self.lib.negf_solve_batch_ex(self._h, req, n, res, ctypes.byref(outs)), "negf_solve_batch_ex")
         out = dict(
             T12=np.array([r.T12 for r in res]),
             EDensity=np.array([r.EDensity for r in res]),

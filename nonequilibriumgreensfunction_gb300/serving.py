@@ -70,6 +70,24 @@ class Server:
         self._meta[rid.value] = (n, npx, r.npy, r.npz)
         return rid.value
 
+    def submit_model(self, npx, npy, npz, model, energies, f1, f2, dE):
+        """Queue one wire given as a model (``hamiltonian.wire_model``): the server
+        generates its Htotd on the device, so only the model crosses to the GPU."""
+        e = np.ascontiguousarray(energies, dtype=np.float64)
+        n = e.size
+        arrs = [np.ascontiguousarray(np.broadcast_to(np.asarray(v, dtype=np.float64), (n,))) for v in (f1, f2, dE)]
+        m, keep = capi.wire_model_struct(model, (npx, npy, npz))
+        r = NegfWireRequest()
+        r.npx, r.npy, r.npz, r.norb = npx, npy, npz, 4
+        r.n_energies = n
+        r.energies, r.f1, r.f2, r.dE = e.ctypes.data, arrs[0].ctypes.data, arrs[1].ctypes.data, arrs[2].ctypes.data
+        r.model = ctypes.addressof(m)
+        rid = ctypes.c_int64()
+        check(self.lib.negf_server_submit(self._h, ctypes.byref(r), ctypes.byref(rid)), "negf_server_submit")
+        del keep
+        self._meta[rid.value] = (n, npx, npy, npz)
+        return rid.value
+
     def _infer_npy(self, nsite):
         # wires here are square in cross-section unless set explicitly
         s = int(round(math.sqrt(nsite)))
@@ -112,8 +130,9 @@ class Server:
 
 def run_poisson_load(server, make_request, rate_hz, duration_s, rng, max_outstanding=64):
     """Submit requests as a Poisson stream of `rate_hz` for `duration_s`, then drain.
-    `make_request(rng)` returns (htotd, hopx, energies, f1, f2, dE).  Returns per-request
-    latency (s), solves, and wall time."""
+    `make_request(rng)` returns (htotd, hopx, energies, f1, f2, dE), or a dict with keys
+    shape=(npx, npy, npz), model, energies, f1, f2, dE for a wire generated on the device.
+    Returns per-request latency (s), solves, and wall time."""
     t0 = time.perf_counter()
     ids, solves = [], 0
     t_next = 0.0
@@ -124,8 +143,13 @@ def run_poisson_load(server, make_request, rate_hz, duration_s, rng, max_outstan
         if now < t_next:
             time.sleep(min(t_next - now, 0.05))
             continue
-        h, x, e, f1, f2, de = make_request(rng)
-        ids.append(server.submit(h, x, e, f1, f2, de))
+        req = make_request(rng)
+        if isinstance(req, dict):
+            e = req["energies"]
+            ids.append(server.submit_model(*req["shape"], req["model"], e, req["f1"], req["f2"], req["dE"]))
+        else:
+            h, x, e, f1, f2, de = req
+            ids.append(server.submit(h, x, e, f1, f2, de))
         solves += len(e)
         t_next += rng.exponential(1.0 / rate_hz)
     lat = []

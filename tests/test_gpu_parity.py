@@ -44,6 +44,13 @@ def assert_close(a, b, what, rtol=RTOL, floor=None):
     assert ok, "%s: max rel err %.3e > %.1e" % (what, err, rtol)
 
 
+def assert_currents_close(got, want, what, rtol=1e-6):
+    """Bond currents: each term is REAL(4) in the reference (Calculate_Observables.F90:7),
+    so they are compared against the largest |J| of the array."""
+    err = np.abs(got - want).max() / max(np.abs(want).max(), 1e-300)
+    assert err <= rtol, "%s: max err %.3e of max|J| > %.1e" % (what, err, rtol)
+
+
 def test_per_energy_interface_matches_oracle(need_gpu):
     """Contact_Self_Energy -> Get_Retarded_Greens -> Calculate_Gnp -> Calculate_Observables
     at the reference's default size (4x3x3, its Dirac basis, eta = 1e-4, T = 0)."""
@@ -272,15 +279,22 @@ def test_c_driver_energy_loop_matches_oracle(need_gpu, tmp_path):
     nsites = npx * npy * npz
     per_e = vals[:7 * n_e].reshape(n_e, 7)
     rhon = vals[7 * n_e:7 * n_e + nsites].reshape((npx, npy, npz), order="F")
+    j0 = 7 * n_e + 2 * nsites + 2
+    jgot = [vals[j0 + i * nsites:j0 + (i + 1) * nsites].reshape((npx, npy, npz), order="F") for i in range(3)]
     opt = O.SolveOptions(eta=1e-4, sr_tol=1e-8)
     eaxis = e_min + (e_max - e_min) / (n_e - 1) * np.arange(n_e)
     w = O.energy_weights(eaxis, (e_max - e_min) / (n_e - 1))
     want_rn = np.zeros((npx, npy, npz))
+    want_j = [np.zeros((npx, npy, npz)) for _ in range(3)]
     for k, e in enumerate(eaxis):
-        ref = O.energy_sweep(htotd, hopx, float(e), (mu1, mu2), w[k], npy, npz, opt)
+        ref = O.energy_sweep(htotd, hopx, float(e), (mu1, mu2), w[k], npy, npz, opt, calc_currents=True)
+        for i, key in enumerate(("Jx", "Jy", "Jz")):
+            want_j[i] += ref[key]
         got = dict(zip(["T12", "EDensity", "HDensity", "Modec1", "Modec2"], per_e[k, :5]))
         for key, v in got.items():
             assert_close(v, ref[key], "%s[%d]" % (key, k), floor=1e-6)
         assert_close(per_e[k, 5:7], ref["dosc"], "dosc[%d]" % k)
         want_rn += ref["RhoN"]
     assert_close(rhon, want_rn, "RhoN")
+    for i, key in enumerate(("Jx", "Jy", "Jz")):
+        assert_currents_close(jgot[i], want_j[i], key)

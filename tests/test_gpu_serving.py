@@ -66,3 +66,27 @@ def test_server_admission_under_small_budget(need_gpu):
             assert got["status"] == 0
             want, _ = _alone(h, x, npx, n, es, 1.0, 0.0, 1e-3, "fp64")
             assert np.array_equal(got["T12"], want["T12"])
+
+
+def test_server_model_requests_match_uploaded_wires(need_gpu):
+    """Wires submitted as models (generated on the device) mix with uploaded wires of the
+    same geometry and give the results of the uploaded host twin solved alone."""
+    rng = np.random.default_rng(5)
+    with Server(precision="mixed", max_batch=4, slots_per_geometry=2) as srv:
+        reqs = []
+        for i in range(4):
+            m = HB.wire_model(W=0.15, seed=100 + i, flux=0.25 * i, zeeman=0.01)
+            h, x = HB.build_from_model(6, 3, 3, m)
+            es = np.sort(rng.uniform(-0.25, 0.25, size=5))
+            if i % 2 == 0:
+                rid = srv.submit_model(6, 3, 3, m, es, 0.8, 0.1, 1e-3)
+            else:
+                rid = srv.submit(h, x, es, 0.8, 0.1, 1e-3)
+            reqs.append((rid, h, x, es))
+        for rid, h, x, es in reqs:
+            srv.wait(rid, timeout=300)
+            got = srv.result(rid)
+            assert got["status"] == 0
+            want, rn = _alone(h, x, 6, 3, es, 0.8, 0.1, 1e-3, "mixed")
+            assert np.array_equal(got["T12"], want["T12"])
+            assert np.array_equal(got["RhoN"], rn)

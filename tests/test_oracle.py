@@ -166,3 +166,28 @@ def test_golden_vectors_are_oracle_output(case):
         assert abs(r["EDensity"] - g["EDensity"][i]) <= 1e-12 * max(1.0, abs(g["EDensity"][i]))
     p = json.loads(str(g["params"]))
     assert p["npx"] == c["npx"]
+
+
+def test_bond_currents_obey_kirchhoff_and_landauer():
+    """Pins the restatement of Calculate_Observables.F90:110-169: with eta -> 0 the bond
+    currents are divergence-free at every interior site (x, y and z bonds together, so their
+    signs and orbital index order must agree), and the +x current through any cross-section
+    is 2 T12 (f1 - f2) q^2/h (the Gn - Gp difference counts both leads).  The reference's
+    REAL(4) terms bound the agreement at ~1e-7 of the largest current."""
+    htotd, hopx = HB.ti_wire(6, 3, 3, W=0.2, seed=1, flux=0.3, zeeman=0.01)
+    opt = O.SolveOptions(eta=1e-7, sr_tol=1e-10, kT=0.0)
+    unit = O.Q_E ** 2 / O.HBAR / (2.0 * O.PI)
+    for e in (-0.2, 0.21):
+        r = O.energy_sweep(htotd, hopx, e, (0.5, -0.5), 1.0, 3, 3, opt, calc_currents=True)
+        jx, jy, jz = r["Jx"] / unit, r["Jy"] / unit, r["Jz"] / unit
+        scale = max(np.abs(jx).max(), np.abs(jy).max(), np.abs(jz).max())
+        div = jx.copy()
+        div[1:] -= jx[:-1]
+        div += jy
+        div[:, 1:] -= jy[:, :-1]
+        div += jz
+        div[:, :, 1:] -= jz[:, :, :-1]
+        assert np.abs(div[1:-1]).max() <= 1e-6 * scale
+        through = jx[:-1].sum(axis=(1, 2))
+        assert np.ptp(through) <= 1e-6 * np.abs(through).max()
+        assert abs(through.mean() - 2.0 * r["T12"] * (r["f1"] - r["f2"])) <= 1e-3 * abs(through.mean())
