@@ -141,10 +141,11 @@ NEGF_API int negf_set_hamiltonian(negf_handle* h, int32_t slot, const double* Ht
  * the on-site block on each site, hop_y between (y, z) and (y+1, z) times the Landau-gauge
  * phase exp(i 2 pi z flux / ((npy-1)(npz-1))) (:186-207), hop_z between (y, z) and (y, z+1),
  * their Hermitian conjugates below the diagonal, and the potential V(x, y, z) on the
- * diagonal.  HopX is hop_x on every site (:59-64).  V is either the caller's array or
- * Anderson disorder U[-W/2, W/2) on slices 2..npx-1 only (:279-296) from a counter-based
- * stream: V = (u - 1/2) W with u = (s >> 11) 2^-53 and s the i-th output of SplitMix64
- * seeded with `seed` (Steele, Lea, Flood 2014), i = x + npx (y + npy z) + 1.  The
+ * diagonal.  HopX is hop_x on every site (:59-64).  V is the caller's array (an
+ * electrostatic potential, :104-112; NULL = 0) plus Anderson disorder U[-W/2, W/2) on
+ * slices 2..npx-1 only (:279-296) from a counter-based stream: (u - 1/2) W with
+ * u = (s >> 11) 2^-53 and s the i-th output of SplitMix64 seeded with `seed` (Steele, Lea,
+ * Flood 2014), i = x + npx (y + npy z) + 1; the site's potential is V + that.  The
  * reference's RANDOM_NUMBER stream is compiler-specific (:230-241); this one is
  * reproducible bit for bit on any host.  Requires norb = 4.  HopX is shared by all slots,
  * as in negf_set_hamiltonian.                                                           */
@@ -152,7 +153,7 @@ typedef struct negf_wire_model {
     double   onsite[4][4][2];  /* row-major [row][col][re, im]                           */
     double   hop[3][4][4][2];  /* hop_x, hop_y, hop_z = H(site, site + e_j)              */
     double   flux;             /* Aharonov-Bohm flux through the cross-section, Phi_0    */
-    double   W;                /* disorder width (ignored when V != NULL)                */
+    double   W;                /* disorder width (0 = no disorder)                       */
     uint64_t seed;             /* disorder stream                                        */
     const double* V;           /* optional npx x npy x npz potential, column-major       */
     int32_t  reserved[8];      /* must be zero                                           */
@@ -306,6 +307,24 @@ NEGF_API int negf_server_wait(negf_server* s, int64_t id, double timeout_s);
 NEGF_API double negf_server_clock(const negf_server* s);
 NEGF_API int negf_server_destroy(negf_server* s);
 
+/* ---- self-consistent bias point: Poisson ---------------------------------------------
+ * The electrostatic step of the Poisson <-> NEGF loop (SIP_Main / SIP_V1,
+ * Source/SIP_Solver.F90:35-231, called from Source/NEGF_Main.F90:10-12), on the current
+ * CUDA device.  For each of n_grids site grids (npx x npy x npz, column-major, grids
+ * consecutive) it solves for the electron potential energy U (eV)
+ *     6 U_i - sum_{in-grid neighbours j} U_j = kappa rho_i + sum of the boundary values
+ *                                              of i's neighbours outside the grid,
+ * a 7-point Laplacian with uniform eps_r (kappa = q / (eps0 eps_r a)) and Dirichlet values
+ * bc[0] on the plane x = -1 (left contact), bc[1] on x = npx (right contact) and bc[2] on
+ * every y and z face (the gate).  rho = RhoN - RhoP per site.  U holds the initial guess
+ * and receives the solution.  The reference iterates Stone's strongly implicit procedure;
+ * this solves the same symmetric positive definite system by conjugate gradients, one CTA
+ * per grid, until ||b - A U|| <= tol ||b||.  *iters (may be NULL) receives the largest
+ * iteration count; NEGF_EREFINE if a grid did not reach tol within max_iter, NEGF_ENAN if
+ * rho is not finite.                                                                    */
+NEGF_API int negf_poisson_solve(int32_t npx, int32_t npy, int32_t npz, int32_t n_grids, const double* rho,
+                                const double* bc, double kappa, double* U, double tol, int32_t max_iter,
+                                int32_t* iters);
 /* ---- stateless dense kernels -------------------------------------------------------
  * Drop-ins for the reference's dense calls on host arrays (column-major, interleaved
  * complex), run on the current CUDA device; `batch` matrices are consecutive in memory

@@ -36,7 +36,7 @@ EXPORTED_SYMBOLS = (
     "negf_set_hamiltonian", "negf_build_hamiltonian", "negf_contact_self_energy", "negf_get_retarded_greens",
     "negf_copy_g_columns", "negf_calculate_gnp", "negf_calculate_observables",
     "negf_calculate_currents", "negf_solve_batch", "negf_solve_batch_ex",
-    "negf_zgemm", "negf_zinv", "negf_zgemm_noalloc",
+    "negf_zgemm", "negf_zinv", "negf_zgemm_noalloc", "negf_poisson_solve",
     "negf_server_create", "negf_server_submit", "negf_server_poll", "negf_server_wait",
     "negf_server_clock", "negf_server_destroy",
 )
@@ -160,6 +160,8 @@ def _declare(lib):
         "negf_zgemm": (c_int, [c_int32, c_int32, c_int32, c_int32, _dp, _dp, c_int32, _dp, c_int32, _dp, _dp,
                                c_int32, c_int32]),
         "negf_zinv": (c_int, [c_int32, _dp, _dp, c_int32]),
+        "negf_poisson_solve": (c_int, [c_int32, c_int32, c_int32, c_int32, _dp, _dp, c_double, _dp, c_double,
+                                       c_int32, POINTER(c_int32)]),
         "negf_zgemm_noalloc": (c_int, [c_int32, c_int32, c_int32, c_int32, _dp, c_void_p, c_int32, c_void_p, c_int32,
                                        _dp, c_void_p, c_int32, c_void_p]),
         "negf_server_create": (c_int, [POINTER(NegfServeParams), POINTER(c_void_p)]),

@@ -185,7 +185,7 @@ int Engine::alloc() {
   NEGF_TRY(inv_work_alloc(inv_, M_, std::max(B_, S_)));
   if (mixed_) {
     const int cap = std::max(B_, S_);
-    const int smax = 7;
+    const int smax = 8;   // every slice count a phase may use (RGF, Sancho-Rubio, residual: <= 8)
     NEGF_TRY(dalloc(&dWinv_, (size_t)(cap * MM_), bytes_));
     NEGF_TRY(dalloc(&dW32_, (size_t)(cap * MM_), bytes_));
     NEGF_TRY(dalloc(&dT_, (size_t)(cap * MM_), bytes_));
@@ -196,6 +196,9 @@ int Engine::alloc() {
     NEGF_TRY(dalloc(&sw_.exps, (size_t)cap * M_, bytes_));
     NEGF_TRY(dalloc(&sa_.exps, (size_t)cap * M_, bytes_));
     NEGF_TRY(dalloc(&sb_.exps, (size_t)cap * M_, bytes_));
+    sa_.data_bytes = sw_.data_bytes = sliced_bytes(M_, kp, smax, cap);
+    sb_.data_bytes = sliced_bytes(2 * M_, kp, smax, cap);
+    sa_.exps_count = sb_.exps_count = sw_.exps_count = (size_t)cap * M_;
     NEGF_TRY(dalloc(&dRnorm_, (size_t)cap, bytes_));
     NEGF_TRY(dalloc(&dNsActive_, (size_t)cap, bytes_));
     NEGF_TRY(dalloc(&dTcErr_, (size_t)1, bytes_));

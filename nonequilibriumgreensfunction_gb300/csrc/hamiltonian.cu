@@ -39,8 +39,8 @@ __host__ __device__ __forceinline__ double anderson(unsigned long long seed, dou
 }
 
 // tab: [0..15] on-site block, [16..31] hop_z, [32 + 16 z ..] hop_y times the phase of layer z;
-// each block row-major [a][b].  V: explicit potential (npx*npy*npz, column-major) or null for
-// the counter-based Anderson potential.
+// each block row-major [a][b].  The on-site potential of a site is V (npx*npy*npz,
+// column-major, may be null) plus the counter-based Anderson potential.
 __global__ void build_h_kernel(int npx, int npy, int npz, const double2* __restrict__ tab,
                                const double* __restrict__ V, unsigned long long seed, double W, double2* H) {
   const int x = blockIdx.y;
@@ -56,7 +56,8 @@ __global__ void build_h_kernel(int npx, int npy, int npz, const double2* __restr
       v = tab[ra * 4 + ca];
       if (ra == ca) {
         const int y = rs % npy, z = rs / npy;
-        v.x += V ? V[x + (long long)npx * (y + (long long)npy * z)] : anderson(seed, W, npx, npy, x, y, z);
+        const double vext = V ? V[x + (long long)npx * (y + (long long)npy * z)] : 0.0;
+        v.x += vext + anderson(seed, W, npx, npy, x, y, z);
       }
     } else if (cs == rs + 1 && rs % npy + 1 < npy) {          // H(s, s + e_y)
       v = tab[32 + 16 * (rs / npy) + ra * 4 + ca];

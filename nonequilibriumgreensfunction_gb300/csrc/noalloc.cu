@@ -81,6 +81,8 @@ extern "C" int negf_zgemm_noalloc(int32_t slices, int32_t m, int32_t n, int32_t 
   ob.data = reinterpret_cast<__nv_bfloat16*>(base + kABytes);
   oa.exps = reinterpret_cast<int*>(base + kABytes + kBBytes);
   ob.exps = reinterpret_cast<int*>(base + kABytes + kBBytes + kEBytes);
+  oa.data_bytes = kABytes; ob.data_bytes = kBBytes;
+  oa.exps_count = ob.exps_count = (size_t)kMaxDim;
   const double2 al = make_double2(alpha[0], alpha[1]), be = make_double2(beta[0], beta[1]);
   NEGF_TRY(slice_a(reinterpret_cast<const double2*>(A), lda, 0, m, k, 1, slices, oa, st));
   NEGF_TRY(slice_b(reinterpret_cast<const double2*>(B), ldb, 0, k, n, 1, slices, ob, st));

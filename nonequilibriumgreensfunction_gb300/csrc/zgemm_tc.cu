@@ -627,6 +627,8 @@ int padded_k(int k) { return (k + 7) & ~7; }   // 16-byte slice vectors and TMA 
 
 int slice_a(const double2* A, int lda, long long sA, int m, int k, int batch, int slices, SlicedOperand& out,
             cudaStream_t st) {
+  if (sliced_bytes(m, padded_k(k), slices, batch) > out.data_bytes || (size_t)m * batch > out.exps_count)
+    return NEGF_EINVAL;
   out.rows = m; out.k = padded_k(k); out.slices = slices; out.batch = batch;
   switch (slices) {
     case 3: return slice_a_t<3>(A, lda, sA, m, k, batch, out, st);
@@ -641,6 +643,8 @@ int slice_a(const double2* A, int lda, long long sA, int m, int k, int batch, in
 
 int slice_b(const double2* B, int ldb, long long sB, int k, int n, int batch, int slices, SlicedOperand& out,
             cudaStream_t st) {
+  if (sliced_bytes(2 * n, padded_k(k), slices, batch) > out.data_bytes || (size_t)n * batch > out.exps_count)
+    return NEGF_EINVAL;
   out.rows = 2 * n; out.k = padded_k(k); out.slices = slices; out.batch = batch;
   switch (slices) {
     case 3: return slice_b_t<3>(B, ldb, sB, k, n, batch, out, st);

@@ -14,6 +14,8 @@ struct SlicedOperand {
   __nv_bfloat16* data = nullptr;
   int* exps = nullptr;
   int rows = 0, k = 0, slices = 0, batch = 0;
+  size_t data_bytes = 0;     // capacity of data; slice_a/slice_b refuse anything larger
+  size_t exps_count = 0;     // capacity of exps (ints)
 };
 
 bool tc_supported_slices(int s);

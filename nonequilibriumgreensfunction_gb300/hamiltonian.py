@@ -146,7 +146,8 @@ def anderson_counter(npx, npy, npz, W, seed):
 
 
 def wire_model(M0=0.3, B=0.25, A=0.5, zeeman=0.0, flux=0.0, W=0.0, seed=0, basis="tau_sigma", V=None):
-    """Parameters of negf_build_hamiltonian: the 4x4 site blocks plus flux and disorder."""
+    """Parameters of negf_build_hamiltonian: the 4x4 site blocks plus flux, disorder
+    (W, seed) and an optional site potential V (npx, npy, npz) added to the disorder."""
     onsite, hx, hy, hz = site_blocks(M0, B, A, zeeman, basis)
     return dict(onsite=onsite, hops=(hx, hy, hz), flux=float(flux), W=float(W), seed=int(seed), V=V)
 
@@ -191,9 +192,9 @@ def build_from_model(npx, npy, npz, model):
                 t = slice(i + NORB * npy, i + NORB * npy + NORB)
                 h[s, t] = hz
                 h[t, s] = hz.conj().T
-    v = model.get("V")
-    if v is None:
-        v = anderson_counter(npx, npy, npz, model["W"], model["seed"])
+    v = anderson_counter(npx, npy, npz, model["W"], model["seed"])
+    if model.get("V") is not None:
+        v = np.asarray(model["V"], dtype=np.float64) + v      # the device adds V + disorder
     htotd = np.repeat(h[None], npx, axis=0)
     diag = np.repeat(np.asarray(v).transpose(0, 2, 1).reshape(npx, nsite), NORB, axis=1)
     idx = np.arange(m)

@@ -35,8 +35,11 @@ def test_model_build_equals_reference_layout_builder():
         assert np.allclose(a, a.conj().transpose(0, 2, 1), rtol=0, atol=0)
 
 
-def test_explicit_potential_overrides_seed():
+def test_explicit_potential_adds_to_disorder():
     v = np.random.default_rng(0).random((5, 2, 3))
     a, _ = HB.build_from_model(5, 2, 3, HB.wire_model(W=0.3, seed=9, V=v))
-    b, _ = HB.ti_wire(5, 2, 3, disorder=v)
+    b, _ = HB.ti_wire(5, 2, 3, disorder=v + HB.anderson_counter(5, 2, 3, 0.3, 9))
     assert np.array_equal(a, b)
+    c, _ = HB.build_from_model(5, 2, 3, HB.wire_model(V=v))
+    d, _ = HB.ti_wire(5, 2, 3, disorder=v)
+    assert np.array_equal(c, d)
