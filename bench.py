@@ -184,6 +184,55 @@ def cpu_sample(n_energies=1):
                                       "NumPy/OpenBLAS on all host threads" % n_energies)
 
 
+SERVING_XS = (6, 8, 10)            # Npy = Npz of the served wires (M = 144, 256, 400)
+SERVING_NPX = (50, 75, 100)
+SERVING_E = (8, 64)                # energies per request, log-uniform
+
+
+def serving_request(rng):
+    """One request of the serving mix: a wire given as a model (its Hamiltonian is built on
+    the device), per-request disorder seed, W ~ U[0, 0.2] eV and flux ~ U[0, 1] Phi_0."""
+    from nonequilibriumgreensfunction_gb300 import hamiltonian as HB
+    n = int(rng.choice(SERVING_XS))
+    npx = int(rng.choice(SERVING_NPX))
+    ne = int(round(math.exp(rng.uniform(math.log(SERVING_E[0]), math.log(SERVING_E[1])))))
+    e = np.sort(rng.choice(energy_grid(), size=ne, replace=False))
+    model = HB.wire_model(W=float(rng.uniform(0.0, 0.2)), seed=int(rng.integers(1 << 62)),
+                          flux=float(rng.uniform(0.0, 1.0)), zeeman=ZEEMAN)
+    f1 = np.array([fermi(x, MU[0], KT) for x in e])
+    f2 = np.array([fermi(x, MU[1], KT) for x in e])
+    return dict(shape=(npx, n, n), model=model, energies=e, f1=f1, f2=f2, dE=0.6 / (N_E - 1))
+
+
+def serving_bench(seconds, device):
+    """p50/p99 latency under Poisson arrivals at 80% of the measured capacity (the serving
+    configuration, scaled to a bench run: cross-sections {6, 8, 10}, Npx in {50, 75, 100},
+    8-64 energies per request instead of {6..14}, [50, 200] and 64-1024)."""
+    from nonequilibriumgreensfunction_gb300.serving import Server, run_poisson_load
+    rng = np.random.default_rng(4)
+    with Server(precision="mixed", max_batch=32, slots_per_geometry=8, eta=ETA, sr_tol=SR_TOL,
+                device=device) as srv:
+        # capacity: a closed burst (also creates the engines of the geometries)
+        burst = [serving_request(rng) for _ in range(24)]
+        t0 = time.perf_counter()
+        ids = [srv.submit_model(*r["shape"], r["model"], r["energies"], r["f1"], r["f2"], r["dE"]) for r in burst]
+        for rid in ids:
+            srv.wait(rid, timeout=1800.0)
+            srv.result(rid)
+        cap_wall = time.perf_counter() - t0
+        cap_solves = sum(r["energies"].size for r in burst)
+        capacity = cap_solves / cap_wall
+        mean_e = float(np.mean([r["energies"].size for r in burst]))
+        rate = 0.8 * capacity / mean_e
+        lat, solves, wall = run_poisson_load(srv, serving_request, rate, seconds, rng)
+    return {"p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+            "solves_per_s": solves / wall, "capacity_solves_per_s": capacity, "arrival_rate_req_per_s": rate,
+            "requests": int(lat.size), "seconds": seconds, "form": "mixed",
+            "load": "Poisson arrivals at 0.8 x measured capacity; Npy=Npz in {6,8,10}, Npx in {50,75,100}, "
+                    "8-64 energies/request (log-uniform), W~U[0,0.2] eV, flux~U[0,1] Phi0, per-request seed; "
+                    "wires sent as models and built on the device"}
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -233,7 +282,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--form", default="mixed", choices=["fp64", "mixed"])
-    ap.add_argument("--batch", type=int, default=16)
+    ap.add_argument("--batch", type=int, default=128)
     ap.add_argument("--slices", type=int, default=0, help="mixed form: BF16 slices of the RGF products (0 = default)")
     ap.add_argument("--residual-slices", type=int, default=0, help="mixed form: slices of the Newton-Schulz residual")
     ap.add_argument("--sr-slices", type=int, default=0, help="mixed form: slices of the Sancho-Rubio products")
@@ -248,6 +297,8 @@ def main():
                          "--slices slices, twice) and exit")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--serving-seconds", type=float, default=30.0,
+                    help="length of the Poisson-arrival serving run (0 = skip); rank 0 of a 1-GPU run only")
     args = ap.parse_args()
 
     if args.npx != NPX:
@@ -436,6 +487,12 @@ def main():
         k: st[k] * 1e-3 / args.steps for k in ("phase_sr_ms", "phase_rgf_ms", "phase_inv_ms", "phase_dens_ms",
                                                "tc_ms", "gemm_ms", "panel_ms", "f32_gemm_ms", "slice_ms")}
     flops_solve = algorithmic_flops_per_solve(m, NPX, sr_iters)
+    serving = None
+    if args.serving_seconds > 0 and world == 1:
+        if solver is not None:
+            solver.close()
+            solver = None
+        serving = serving_bench(args.serving_seconds, local_rank)
     cpu = None
     if not args.no_cpu_baseline and world == 1:
         v, cores, sample = cpu_sample(1)
@@ -455,6 +512,7 @@ def main():
         "cpu_baseline": cpu,
         "fp64_form": fp64,
         "e2e": e2e,
+        "serving": serving,
         "gpu_launches": st["launches"],
         "clocks": clk.summary(local_rank),
         "peaks_file": {k: peaks.get(k) for k in ("hbm_gbs", "bf16_tflops", "bf16_tflops_sustained")},
