@@ -66,6 +66,15 @@ def step_requests(step, batch, rank, world):
     return e, f1, f2, slots
 
 
+def max_over_ranks(value, dist, device):
+    """The slowest rank's time (the job finishes when it does): an all-reduce MAX of one
+    scalar; `device` is the rank's GPU under NCCL, the CPU under gloo."""
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def algorithmic_flops_per_solve(m, npx, n_sr, n_seeds_sharing=SEEDS):
     """Work model of the solve (real flops), per energy point:
     RGF: per slice 2 inverses + 4 complex GEMMs (column 1, column N, G Gamma_L, G Gamma_R),
@@ -381,9 +390,7 @@ def main():
     solver.profile(False)
     elapsed = ev0.elapsed_time(ev1) * 1e-3
     if world > 1:
-        t = torch.tensor([elapsed], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed = float(t.item())
+        elapsed = max_over_ranks(elapsed, dist, dev)
         dist.barrier()
     solves = args.batch * args.steps * world
     value = solves / elapsed
@@ -404,9 +411,7 @@ def main():
         torch.cuda.synchronize()
         el2 = ev2.elapsed_time(ev3) * 1e-3
         if world > 1:
-            t = torch.tensor([el2], device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            el2 = float(t.item())
+            el2 = max_over_ranks(el2, dist, dev)
         h2d = sum(hf.nbytes + xf.nbytes for hf, xf in pinned) + args.batch * 40
         d2h = args.batch * 64 + 5 * nsites * SEEDS * 8
         e2e = {"value": args.batch * args.steps * world / el2, "unit": "solves/s",

@@ -13,9 +13,10 @@
 // accumulator; for d < 5 and K' <= 800 every partial sum stays below 2^24, so those
 // accumulators are EXACT (products of 7-bit integers and their sums are representable).
 // Higher diagonals carry weight <= 2^-35 and their rounding is far below FP64 epsilon of
-// the leading term.  The epilogue forms sum_d acc_d 2^-7d in FP64 and scales by
-// 2^(e_i + f_j - 12).  Accuracy is set by S: truncation <= 2^-7S of the row/column
-// maximum (S = 4: 4e-9, S = 5: 3e-11, S = 7: 2e-15).
+// the leading term.  The epilogue recombines sum_d acc_d 2^(7(S-1-d)) in int64 (two words
+// for S >= 7), converts once to FP64 and scales by 2^(e_i + f_j - 12 - 7(S-1)).  Accuracy
+// is set by S: truncation <= 2^-7S of the row/column maximum (S = 4: 4e-9, S = 5: 3e-11,
+// S = 7: 2e-15).
 //
 // Kernel structure (one 128 x NT output tile per CTA, 6 warps):
 //   warp 0      TMA producer: for each K block of 32, S A-slices (128 x 32) and S B-slices
