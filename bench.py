@@ -487,6 +487,7 @@ def main():
             "launches": st["tc_launches"], "share_of_step": st["tc_ms"] * 1e-3 / elapsed,
             "complex_equiv_tflops": (st["tc_complex_flops"] / (st["tc_ms"] * 1e-3) / 1e12) if st["tc_ms"] > 0 else None,
             "fallbacks": st["fallbacks"], "ns_residual_max": st["ns_residual_max"],
+            "ns_extra_steps": st["ns_extra_steps"],
         }
     roofline["breakdown_s_per_step"] = {
         k: st[k] * 1e-3 / args.steps for k in ("phase_sr_ms", "phase_rgf_ms", "phase_inv_ms", "phase_dens_ms",

@@ -121,6 +121,8 @@ typedef struct negf_stats {
     double  phase_rgf_ms;    /* whole RGF sweeps (including their inverses)                */
     double  phase_inv_ms;    /* all inverses (Sancho-Rubio and RGF)                        */
     double  phase_dens_ms;   /* density / spin reductions                                  */
+    int64_t ns_extra_steps;  /* mixed form: Newton-Schulz matrix-steps beyond the two fixed
+                                ones (matrices whose residual was still above 1e-6)        */
 } negf_stats;
 NEGF_API int negf_profile(negf_handle* h, int enable);
 NEGF_API int negf_get_stats(negf_handle* h, negf_stats* out);

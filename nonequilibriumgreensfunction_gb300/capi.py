@@ -106,7 +106,7 @@ class NegfStats(ctypes.Structure):
                 ("tc_complex_flops", c_double),
                 ("fallbacks", c_int64), ("ns_residual_max", c_double), ("f32_gemm_ms", c_double),
                 ("slice_ms", c_double), ("phase_sr_ms", c_double), ("phase_rgf_ms", c_double),
-                ("phase_inv_ms", c_double), ("phase_dens_ms", c_double)]
+                ("phase_inv_ms", c_double), ("phase_dens_ms", c_double), ("ns_extra_steps", c_int64)]
 
 
 class NegfServeParams(ctypes.Structure):

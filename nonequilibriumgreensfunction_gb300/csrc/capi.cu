@@ -163,6 +163,7 @@ int negf_profile(negf_handle* h, int enable) {
     I.timing.store(enable != 0);
   }
   h->eng.fallbacks_ = 0;
+  h->eng.ns_extra_ = 0;
   h->eng.last_rnorm_max_ = 0.0;
   return NEGF_OK;
 }
@@ -191,6 +192,7 @@ int negf_get_stats(negf_handle* h, negf_stats* out) {
   out->phase_dens_ms = I.kind_ms[negf::TK_PH_DENS];
   out->fallbacks = h->eng.fallbacks_;
   out->ns_residual_max = h->eng.last_rnorm_max_;
+  out->ns_extra_steps = h->eng.ns_extra_;
   return NEGF_OK;
 }
 

@@ -89,8 +89,8 @@ Engine::~Engine() {
   dfree(dSrCmax_); dfree(dSrDos_); dfree(dSrActive_); dfree(dSrE_); dfree(dSrHend_); dfree(dSrStatus_);
   inv_work_free(inv_);
   dfree(dWinv_); dfree(dW32_); dfree(dT_); dfree(sa_.data); dfree(sb_.data); dfree(sa_.exps); dfree(sb_.exps);
-  dfree(sw_.data); dfree(sw_.exps);
-  dfree(dRnorm_); dfree(dNsActive_); dfree(dTcErr_);
+  dfree(sw_.data); dfree(sw_.exps); dfree(sgl_.data); dfree(sgl_.exps); dfree(sgr_.data); dfree(sgr_.exps);
+  dfree(dRnorm_); dfree(dNsActive_); dfree(dNsIdx_); dfree(dNsX_); dfree(dNsW_); dfree(dTcErr_);
   if (hPin_) cudaFreeHost(hPin_);
   if (own_st_) cudaStreamDestroy(own_st_);
 }
@@ -196,11 +196,20 @@ int Engine::alloc() {
     NEGF_TRY(dalloc(&sw_.exps, (size_t)cap * M_, bytes_));
     NEGF_TRY(dalloc(&sa_.exps, (size_t)cap * M_, bytes_));
     NEGF_TRY(dalloc(&sb_.exps, (size_t)cap * M_, bytes_));
+    NEGF_TRY(dalloc(reinterpret_cast<char**>(&sgl_.data), sliced_bytes(2 * M_, kp, s_rgf_, B_), bytes_));
+    NEGF_TRY(dalloc(reinterpret_cast<char**>(&sgr_.data), sliced_bytes(2 * M_, kp, s_rgf_, B_), bytes_));
+    NEGF_TRY(dalloc(&sgl_.exps, (size_t)B_ * M_, bytes_));
+    NEGF_TRY(dalloc(&sgr_.exps, (size_t)B_ * M_, bytes_));
+    sgl_.data_bytes = sgr_.data_bytes = sliced_bytes(2 * M_, kp, s_rgf_, B_);
+    sgl_.exps_count = sgr_.exps_count = (size_t)B_ * M_;
     sa_.data_bytes = sw_.data_bytes = sliced_bytes(M_, kp, smax, cap);
     sb_.data_bytes = sliced_bytes(2 * M_, kp, smax, cap);
     sa_.exps_count = sb_.exps_count = sw_.exps_count = (size_t)cap * M_;
     NEGF_TRY(dalloc(&dRnorm_, (size_t)cap, bytes_));
     NEGF_TRY(dalloc(&dNsActive_, (size_t)cap, bytes_));
+    NEGF_TRY(dalloc(&dNsIdx_, (size_t)cap, bytes_));
+    NEGF_TRY(dalloc(&dNsX_, (size_t)cap * MM_, bytes_));
+    NEGF_TRY(dalloc(&dNsW_, (size_t)cap * MM_, bytes_));
     NEGF_TRY(dalloc(&dTcErr_, (size_t)1, bytes_));
     NEGF_CUDA_TRY(cudaMemset(dTcErr_, 0, sizeof(int)));
   }
@@ -305,6 +314,16 @@ int Engine::gemm_tc_nn(int batch, const double2* A, long long sA, const double2*
   return zgemm_tc(sa_, sb_, alpha, beta, C, M_, sC, dTcErr_, st_);
 }
 
+// C = A G with G's B-operand slicing made once per sweep (Gamma_L, Gamma_R); FP64 form:
+// a plain product with G itself
+int Engine::gemm_gamma(int batch, const double2* A, long long sA, const double2* G, const SlicedOperand& sg,
+                       double2* C, long long sC) {
+  const double2 one = make_double2(1, 0), zero = make_double2(0, 0);
+  if (!mixed_) return gemm(batch, OP_N, A, sA, OP_N, G, MM_, C, sC, one, zero);
+  NEGF_TRY(slice_a(A, M_, sA, M_, M_, batch, s_rgf_, sa_, st_));
+  return zgemm_tc(sa_, sg, one, zero, C, M_, sC, dTcErr_, st_);
+}
+
 int Engine::gemm(int batch, Op opA, const double2* A, long long sA, Op opB, const double2* B, long long sB, double2* C,
                  long long sC, double2 alpha, double2 beta) {
   if (mixed_ && opA == OP_N && opB == OP_N && sA != 0 && sB != 0)
@@ -355,43 +374,55 @@ int Engine::invert_impl(double2* A, long long sA, int batch, int* status_dev) {
   NEGF_CUDA_TRY(cudaMemsetAsync(dRnorm_, 0, sizeof(unsigned long long) * batch, st_));
   NEGF_TRY(slice_a(dWinv_, M_, MM_, M_, M_, batch, s_res_, sw_, st_));
   std::vector<unsigned long long> r0(batch), rk(batch);
-  // Steps after the first ns_steps_ - 1 are taken per matrix: a matrix stays active while its
-  // own residual norm before the update is above ns_tol_ (the update squares it).  Inactive
-  // matrices get R = 0, so X + X R leaves them bit for bit unchanged and each inverse depends
-  // only on its own matrix, never on the rest of the batch.
-  std::vector<int> active(batch, 1);
-  for (int step = 0; step < ns_max_steps_; ++step) {
+  // ns_steps_ steps for the whole batch
+  for (int step = 0; step < ns_steps_; ++step) {
     if (step > 0) NEGF_CUDA_TRY(cudaMemsetAsync(dRnorm_, 0, sizeof(unsigned long long) * batch, st_));
-    NEGF_TRY(slice_b(A, M_, sA, M_, M_, batch, s_res_, sb_, st_));
-    NEGF_TRY(zgemm_tc(sw_, sb_, one, zero, dT_, M_, MM_, dTcErr_, st_));          // T = W X
+    // the first residual only has to be good to the square root of the target (the next
+    // step squares the error), so it takes s_res0_ slices: the leading planes of W's slicing
+    const int sr = (step == 0 && ns_steps_ > 1) ? s_res0_ : s_res_;
+    NEGF_TRY(slice_b(A, M_, sA, M_, M_, batch, sr, sb_, st_));
+    NEGF_TRY(zgemm_tc(sw_, sb_, one, zero, dT_, M_, MM_, dTcErr_, st_, sr));    // T = W X
     NEGF_TRY(ns_residual(M_, batch, dT_, MM_, dRnorm_, st_));                     // R = I - T
     if (step == 0)
       NEGF_CUDA_TRY(cudaMemcpyAsync(r0.data(), dRnorm_, sizeof(unsigned long long) * batch, cudaMemcpyDeviceToHost, st_));
-    if (step + 1 >= ns_steps_) {
-      // R_{k+1} = R_k^2: after this update the residual is at most |R_k|^2
+    if (step == ns_steps_ - 1)
       NEGF_CUDA_TRY(cudaMemcpyAsync(rk.data(), dRnorm_, sizeof(unsigned long long) * batch, cudaMemcpyDeviceToHost, st_));
-      NEGF_CUDA_TRY(cudaStreamSynchronize(st_));
-      if (step + 1 > ns_steps_) {
-        // R of matrices that finished earlier (or go to the FP64 fallback) is zeroed
-        NEGF_CUDA_TRY(cudaMemcpyAsync(dNsActive_, active.data(), sizeof(int) * batch, cudaMemcpyHostToDevice, st_));
-        NEGF_TRY(zero_unmasked(M_, batch, dNsActive_, dT_, MM_, st_));
-      }
-      bool more = false;
-      for (int b = 0; b < batch; ++b) {
-        const double r = __longlong_as_double_host(r0[b]);
-        if (info32[b] != 0 || !(r <= ns_accept_)) { active[b] = 0; continue; }
-        if (active[b] && __longlong_as_double_host(rk[b]) <= ns_tol_) active[b] = 0;
-        more = more || active[b];
-      }
-      NEGF_TRY(slice_a(A, M_, sA, M_, M_, batch, s_upd_, sa_, st_));
-      NEGF_TRY(slice_b(dT_, M_, MM_, M_, M_, batch, s_upd_, sb_, st_));
-      NEGF_TRY(zgemm_tc(sa_, sb_, one, one, A, M_, sA, dTcErr_, st_));            // X += X R
-      if (!more) break;
-      continue;
-    }
     NEGF_TRY(slice_a(A, M_, sA, M_, M_, batch, s_upd_, sa_, st_));
     NEGF_TRY(slice_b(dT_, M_, MM_, M_, M_, batch, s_upd_, sb_, st_));
     NEGF_TRY(zgemm_tc(sa_, sb_, one, one, A, M_, sA, dTcErr_, st_));              // X += X R
+  }
+  NEGF_CUDA_TRY(cudaStreamSynchronize(st_));
+  // Further steps only for the matrices whose residual norm before the last update was
+  // above ns_tol_ (that update squared it), gathered into a compact batch: the work is
+  // proportional to the matrices that need it, and each matrix's result depends only on
+  // its own residuals, never on the rest of the batch.
+  std::vector<int> act;
+  for (int b = 0; b < batch; ++b) {
+    const double r = __longlong_as_double_host(r0[b]);
+    if (info32[b] != 0 || !(r <= ns_accept_)) continue;     // redone in FP64 below
+    if (__longlong_as_double_host(rk[b]) > ns_tol_) act.push_back(b);
+  }
+  for (int step = ns_steps_; step < ns_max_steps_ && !act.empty(); ++step) {
+    const int na = (int)act.size();
+    ns_extra_ += na;
+    NEGF_CUDA_TRY(cudaMemcpyAsync(dNsIdx_, act.data(), sizeof(int) * na, cudaMemcpyHostToDevice, st_));
+    NEGF_TRY(gather_strided(M_, na, A, sA, dNsIdx_, dNsX_, MM_, st_));
+    NEGF_TRY(gather_strided(M_, na, dWinv_, MM_, dNsIdx_, dNsW_, MM_, st_));
+    NEGF_CUDA_TRY(cudaMemsetAsync(dRnorm_, 0, sizeof(unsigned long long) * na, st_));
+    NEGF_TRY(slice_a(dNsW_, M_, MM_, M_, M_, na, s_res_, sa_, st_));
+    NEGF_TRY(slice_b(dNsX_, M_, MM_, M_, M_, na, s_res_, sb_, st_));
+    NEGF_TRY(zgemm_tc(sa_, sb_, one, zero, dT_, M_, MM_, dTcErr_, st_));            // T = W X
+    NEGF_TRY(ns_residual(M_, na, dT_, MM_, dRnorm_, st_));                           // R = I - T
+    NEGF_CUDA_TRY(cudaMemcpyAsync(rk.data(), dRnorm_, sizeof(unsigned long long) * na, cudaMemcpyDeviceToHost, st_));
+    NEGF_TRY(slice_a(dNsX_, M_, MM_, M_, M_, na, s_upd_, sa_, st_));
+    NEGF_TRY(slice_b(dT_, M_, MM_, M_, M_, na, s_upd_, sb_, st_));
+    NEGF_TRY(zgemm_tc(sa_, sb_, one, one, dNsX_, M_, MM_, dTcErr_, st_));          // X += X R
+    NEGF_TRY(scatter_strided(M_, na, dNsX_, MM_, dNsIdx_, A, sA, st_));
+    NEGF_CUDA_TRY(cudaStreamSynchronize(st_));
+    std::vector<int> next;
+    for (int i = 0; i < na; ++i)
+      if (__longlong_as_double_host(rk[i]) > ns_tol_) next.push_back(act[i]);
+    act.swap(next);
   }
   NEGF_CUDA_TRY(cudaStreamSynchronize(st_));
   double worst = 0.0;
@@ -578,6 +609,10 @@ int Engine::solve_rgf_impl(const std::vector<Item>& items, bool keep_columns) {
   NEGF_TRY(gather_blocks(M_, B, dSrSigR_, idx_r, istride, dSigR_, sM, st_));
   NEGF_TRY(gather_blocks(M_, B, dSrGamL_, idx_l, istride, dGamL_, sM, st_));
   NEGF_TRY(gather_blocks(M_, B, dSrGamR_, idx_r, istride, dGamR_, sM, st_));
+  if (mixed_) {   // Gamma is the right factor of every G(:,c) Gamma_c product of the sweep
+    NEGF_TRY(slice_b(dGamL_, M_, sM, M_, M_, B, s_rgf_, sgl_, st_));
+    NEGF_TRY(slice_b(dGamR_, M_, sM, M_, M_, B, s_rgf_, sgr_, st_));
+  }
 
   auto form = [&](int x, int side, const double2* gprev) -> int {
     FormW fw{};
@@ -622,7 +657,7 @@ int Engine::solve_rgf_impl(const std::vector<Item>& items, bool keep_columns) {
         NEGF_TRY(site_blocks(M_, p_.norb, B, Yprev, sM, dC1_, sM, dPx1_ + (x - 1) * sl, sP, st_));
     }
     if (keep_columns && dCol1_) NEGF_TRY(copy_blocks(M_, 1, dC1_, sM, dCol1_ + (long long)x * MM_, sM, st_));
-    NEGF_TRY(gemm(B, OP_N, dC1_, sM, OP_N, dGamL_, sM, Y, sM, one, zero));        // G(x,1) Gamma_L
+    NEGF_TRY(gemm_gamma(B, dC1_, sM, dGamL_, sgl_, Y, sM));                        // G(x,1) Gamma_L
     if (currents_)
       NEGF_TRY(site_pairs(M_, p_.norb, p_.npy, p_.npz, B, Y, sM, dC1_, sM, dP1_ + x * sl, dPy1_ + x * sl,
                           dPz1_ + x * sl, sP, st_));
@@ -654,7 +689,7 @@ int Engine::solve_rgf_impl(const std::vector<Item>& items, bool keep_columns) {
       NEGF_TRY(gemm(B, OP_N, Gx, sG, OP_N, dZ_, sM, CN, sM, one, zero));
     }
     if (keep_columns && dColN_) NEGF_TRY(copy_blocks(M_, 1, CN, sM, dColN_ + (long long)x * MM_, sM, st_));
-    NEGF_TRY(gemm(B, OP_N, CN, sM, OP_N, dGamR_, sM, dY_, sM, one, zero));        // G(x,N) Gamma_R
+    NEGF_TRY(gemm_gamma(B, CN, sM, dGamR_, sgr_, dY_, sM));                         // G(x,N) Gamma_R
     if (currents_) {
       NEGF_TRY(site_pairs(M_, p_.norb, p_.npy, p_.npz, B, dY_, sM, CN, sM, dP2_ + x * sl, dPy2_ + x * sl,
                           dPz2_ + x * sl, sP, st_));

@@ -110,18 +110,23 @@ class Engine {
   int s_rgf_ = 5;      // RGF block products
   int s_sr_ = 8;       // Sancho-Rubio products: 2^-56, the decimation is ill-conditioned near band edges
   int s_res_ = 7;      // Newton-Schulz residual W X (2^-49, FP64-class)
+  int s_res0_ = 5;     // the first residual (2^-35: the second step squares its error)
   int s_upd_ = 3;      // Newton-Schulz update X R (R is small: 2^-21 of it is below the target)
   int ns_steps_ = 2;        // Newton-Schulz steps always taken
   int ns_max_steps_ = 4;    // more while the latest residual norm is above ns_tol_
-  double ns_tol_ = 1e-6;
+  double ns_tol_ = 1e-5;     // residual norm before the last update; that update squares it
   double ns_accept_ = 0.5;   // first residual norm above this -> FP64 inverse for that matrix
   int cur_slices_ = 4;       // slices for the GEMMs issued now (set per phase)
   double2* dWinv_ = nullptr; // copy of the matrix being inverted (FP64)
   float2* dW32_ = nullptr;
   double2* dT_ = nullptr;
   SlicedOperand sa_, sb_, sw_;   // sw_: slices of the matrix under inversion (kept across NS steps)
+  SlicedOperand sgl_, sgr_;      // Gamma_L, Gamma_R as B operands, sliced once per sweep
   unsigned long long* dRnorm_ = nullptr;
-  int* dNsActive_ = nullptr;  // per-matrix flags of the Newton-Schulz steps beyond ns_steps_
+  int* dNsActive_ = nullptr;  // per-matrix flags (zero_unmasked)
+  int* dNsIdx_ = nullptr;     // matrices still taking Newton-Schulz steps beyond ns_steps_
+  double2 *dNsX_ = nullptr, *dNsW_ = nullptr;   // their X and W, gathered into a compact batch
+  long long ns_extra_ = 0;    // matrix-steps taken beyond ns_steps_ (statistics)
   int* dTcErr_ = nullptr;
   long long fallbacks_ = 0;
   double last_rnorm_max_ = 0.0;
@@ -157,6 +162,8 @@ class Engine {
            long long sC, double2 alpha, double2 beta);
   int gemm_tc_nn(int batch, const double2* A, long long sA, const double2* B, long long sB, double2* C, long long sC,
                  double2 alpha, double2 beta, int slices);
+  int gemm_gamma(int batch, const double2* A, long long sA, const double2* G, const SlicedOperand& sg, double2* C,
+                 long long sC);
   int merge_info(int batch);
   // upload HopX (M x M) and its site-block form; a changed HopX invalidates every slot
   int set_hopx(const double2* hx);

@@ -116,32 +116,62 @@ __global__ void __launch_bounds__(PANEL_THREADS) gj_panel_kernel(T* A, long long
   for (int e = t; e < n * kb; e += PANEL_THREADS) dst[e] = Ps[e];
 }
 
-// One thread per column j outside the panel: apply the nb row interchanges in order, copy
-// rows K to R (kb x n, column-major) and zero them in A.  Panel columns get R = 0.
+// Row interchanges of one panel for the columns outside it, and the copy of rows K into R.
+// The kb interchanges (r, ip[r]) of the panel touch at most 2 kb rows.  Thread 0 of each
+// CTA composes them once into a gather list over the touched rows (row trow[t] receives the
+// value of row torig[t]); then one warp per column loads its touched values (all loads
+// before any store, so the gather is a simultaneous permutation), writes rows K to R
+// (kb x n, column-major) with zeros in A, and the other touched rows back in place.
+// Panel columns get R = 0.
+constexpr int SWAP_WARPS = 8;
 template <typename T>
-__global__ void gj_swap_kernel(T* A, long long sA, int n, int k0, int kb, const int* ipiv, T* R, long long sR) {
+__global__ void __launch_bounds__(SWAP_WARPS * 32) gj_swap_kernel(T* A, long long sA, int n, int k0, int kb,
+                                                                  const int* ipiv, T* R, long long sR) {
+  __shared__ int trow[64], torig[64];
+  __shared__ int s_nt;
   const int b = blockIdx.y;
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= n) return;
   T* Ab = A + (long long)b * sA;
   const int* ip = ipiv + (long long)b * n;
   T* Rb = R + (long long)b * sR;
+  if (threadIdx.x == 0) {
+    int nt = kb;
+    for (int c = 0; c < kb; ++c) { trow[c] = k0 + c; torig[c] = k0 + c; }
+    for (int c = 0; c < kb; ++c) {
+      const int r = k0 + c, p = ip[r];
+      if (p == r) continue;
+      int ip_ = -1;
+      for (int t = 0; t < nt; ++t)
+        if (trow[t] == p) { ip_ = t; break; }
+      if (ip_ < 0) { ip_ = nt; trow[nt] = p; torig[nt] = p; ++nt; }
+      const int tmp = torig[c];   // row r sits at index c
+      torig[c] = torig[ip_];
+      torig[ip_] = tmp;
+    }
+    s_nt = nt;
+  }
+  __syncthreads();
+  const int nt = s_nt;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int j = blockIdx.x * SWAP_WARPS + warp;
+  if (j >= n) return;
   if (j >= k0 && j < k0 + kb) {
-    for (int c = 0; c < kb; ++c) Rb[(long long)j * kb + c] = CplxTraits<T>::make(0, 0);
+    for (int c = lane; c < kb; c += 32) Rb[(long long)j * kb + c] = CplxTraits<T>::make(0, 0);
     return;
   }
   T* colj = Ab + (long long)j * n;
-  for (int c = 0; c < kb; ++c) {
-    const int r = k0 + c, p = ip[r];
-    if (p != r) {
-      T tmp = colj[r];
-      colj[r] = colj[p];
-      colj[p] = tmp;
-    }
+  T v0 = CplxTraits<T>::make(0, 0), v1 = CplxTraits<T>::make(0, 0);
+  if (lane < nt) v0 = colj[torig[lane]];
+  if (lane + 32 < nt) v1 = colj[torig[lane + 32]];
+  __syncwarp();
+  if (lane < nt) {
+    const int r = trow[lane];
+    if (r >= k0 && r < k0 + kb) { Rb[(long long)j * kb + (r - k0)] = v0; colj[r] = CplxTraits<T>::make(0, 0); }
+    else colj[r] = v0;
   }
-  for (int c = 0; c < kb; ++c) {
-    Rb[(long long)j * kb + c] = colj[k0 + c];
-    colj[k0 + c] = CplxTraits<T>::make(0, 0);
+  if (lane + 32 < nt) {
+    const int r = trow[lane + 32];
+    if (r >= k0 && r < k0 + kb) { Rb[(long long)j * kb + (r - k0)] = v1; colj[r] = CplxTraits<T>::make(0, 0); }
+    else colj[r] = v1;
   }
 }
 
@@ -223,8 +253,8 @@ int gj_invert(T* A, long long sA, int n, int batch, InvWork& w, cudaStream_t st)
     gj_panel_kernel<T><<<batch, PANEL_THREADS, smem, st>>>(A, sA, n, k0, kb, w.ipiv, w.info);
     NEGF_CUDA_TRY(cudaGetLastError());
     timed_end(st, TK_PANEL, ev);
-    dim3 g2((n + 127) / 128, batch);
-    gj_swap_kernel<T><<<g2, 128, 0, st>>>(A, sA, n, k0, kb, w.ipiv, rbuf, sR);
+    dim3 g2((n + SWAP_WARPS - 1) / SWAP_WARPS, batch);
+    gj_swap_kernel<T><<<g2, SWAP_WARPS * 32, 0, st>>>(A, sA, n, k0, kb, w.ipiv, rbuf, sR);
     NEGF_CUDA_TRY(cudaGetLastError());
     count_launch(2);
     // A(:, 0:k0) += P R(:, 0:k0);  A(:, k0+kb:n) += P R(:, k0+kb:n)

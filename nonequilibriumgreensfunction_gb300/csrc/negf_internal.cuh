@@ -290,6 +290,12 @@ int to_f64(int n, int batch, const float2* src, long long sS, double2* dst, long
 int split_copy(int n, int batch, const double2* src, long long sS, double2* d64, long long s64, float2* d32,
                long long s32, cudaStream_t st);
 int ns_residual(int n, int batch, double2* T, long long sT, unsigned long long* rnorm, cudaStream_t st);
+// dst[i] = src[idx[i]] (gather) / dst[idx[i]] = src[i] (scatter) for i < count, n x n
+// blocks at the given strides, idx on the device
+int gather_strided(int n, int count, const double2* src, long long sSrc, const int* idx, double2* dst, long long sDst,
+                   cudaStream_t st);
+int scatter_strided(int n, int count, const double2* src, long long sSrc, const int* idx, double2* dst,
+                    long long sDst, cudaStream_t st);
 // A[b] = 0 for every b with keep[b] == 0 (device flags)
 int zero_unmasked(int n, int batch, const int* keep, double2* A, long long sA, cudaStream_t st);
 

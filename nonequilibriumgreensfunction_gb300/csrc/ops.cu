@@ -66,6 +66,67 @@ __global__ void form_w_kernel(FormW a) {
   }
 }
 
+// The same W when HopX is block diagonal with 4 x 4 site blocks: one thread per 4 x 4 site
+// block (si, sj) of W.  The coupling term of the block is L_si G(si, sj) R_sj (side 0:
+// L = H^H, R = H; side 1: L = H, R = H^H), formed as T = G R and then L T: 8 complex FMAs
+// per element instead of the 20 of the element-wise form.  GB300's FP64 pipe runs at 1/64
+// of its FP32 rate, so this FP64 arithmetic, not memory, bounds the kernel.  Each thread
+// reads and writes its block as four 64-byte column pieces; consecutive threads take
+// consecutive row blocks, so a warp's accesses to a column are contiguous.
+__global__ void form_w_blocks_kernel(FormW a) {
+  const int b = blockIdx.y;
+  const int n = a.n, ns = n / 4;
+  const long long nblk = (long long)ns * ns;
+  const Item it = a.items[b];
+  const double2* Hx = a.Hall + ((long long)it.slot * a.npx + a.x) * ((long long)n * n);
+  const double2* gp = a.gprev + (long long)b * a.sG;
+  const double2* sl = (a.x == 0 && a.sigL) ? a.sigL + (long long)b * a.sSig : nullptr;
+  const double2* sr = (a.x == a.npx - 1 && a.sigR) ? a.sigR + (long long)b * a.sSig : nullptr;
+  double2* W = a.W + (long long)b * a.sW;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nblk; t += (long long)gridDim.x * blockDim.x) {
+    const int si = (int)(t % ns), sj = (int)(t / ns);
+    double2 g[4][4];                       // g[r][c] = G(4 si + r, 4 sj + c)
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const double2* col = gp + (long long)(4 * sj + c) * n + 4 * si;
+#pragma unroll
+      for (int r = 0; r < 4; ++r) g[r][c] = col[r];
+    }
+    // T = G R, one column of R(q, j) at a time (side 0: R = H, side 1: R = H^H)
+    double2 tm[4][4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      double2 rc[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) rc[q] = a.side == 0 ? hbe(a.hop, sj, q, c) : cconj(hbe(a.hop, sj, c, q));
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        double2 acc = make_double2(0.0, 0.0);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) cfma(acc, g[r][q], rc[q]);
+        tm[r][c] = acc;
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const long long e0 = (long long)(4 * sj + c) * n + 4 * si;
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        double2 acc = make_double2(0.0, 0.0);
+#pragma unroll
+        for (int p = 0; p < 4; ++p)   // L(r, p): side 0: L = H^H, side 1: L = H
+          cfma(acc, a.side == 0 ? cconj(hbe(a.hop, si, p, r)) : hbe(a.hop, si, r, p), tm[p][c]);
+        const long long e = e0 + r;
+        double2 v = make_double2(-Hx[e].x, -Hx[e].y);
+        if (si == sj && r == c) { v.x += it.energy; v.y += a.eta; }
+        if (sl) v = csub(v, sl[e]);
+        if (sr) v = csub(v, sr[e]);
+        W[e] = csub(v, acc);
+      }
+    }
+  }
+}
+
 // ---- Y = op(H) X  or  X op(H), H block diagonal ------------------------------------
 __global__ void hop_apply_kernel(HopBD h, int n, int left, int op, const double2* X, long long sX, double2* Y,
                                  long long sY) {
@@ -498,6 +559,13 @@ __global__ void reduce_sites_kernel(int batch, int total, int nf, int nslots, co
 
 // =====================================================================================
 int form_w(const FormW& a, cudaStream_t st) {
+  if (a.gprev && a.hop.hb && a.hop.norb == 4 && !a.zsub && a.n % 4 == 0) {
+    const long long nblk = (long long)(a.n / 4) * (a.n / 4);
+    form_w_blocks_kernel<<<ew_grid(nblk, a.batch), 128, 0, st>>>(a);
+    NEGF_CUDA_TRY(cudaGetLastError());
+    count_launch();
+    return NEGF_OK;
+  }
   form_w_kernel<<<ew_grid((long long)a.n * a.n, a.batch), EW_THREADS, 0, st>>>(a);
   NEGF_CUDA_TRY(cudaGetLastError());
   count_launch();
@@ -737,6 +805,36 @@ __global__ void zero_unmasked_kernel(int n, const int* keep, double2* A, long lo
     Ab[e] = make_double2(0.0, 0.0);
 }
 }  // namespace
+
+namespace {
+__global__ void gather_strided_kernel(int n, const double2* src, long long sSrc, const int* idx, double2* dst,
+                                      long long sDst, int scatter) {
+  const int i = blockIdx.y;
+  const long long nn = (long long)n * n;
+  const double2* s_ = scatter ? src + (long long)i * sSrc : src + (long long)idx[i] * sSrc;
+  double2* d = scatter ? dst + (long long)idx[i] * sDst : dst + (long long)i * sDst;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nn; e += (long long)gridDim.x * blockDim.x)
+    d[e] = s_[e];
+}
+}  // namespace
+
+int gather_strided(int n, int count, const double2* src, long long sSrc, const int* idx, double2* dst, long long sDst,
+                   cudaStream_t st) {
+  if (count <= 0) return NEGF_OK;
+  gather_strided_kernel<<<ew_grid((long long)n * n, count), EW_THREADS, 0, st>>>(n, src, sSrc, idx, dst, sDst, 0);
+  NEGF_CUDA_TRY(cudaGetLastError());
+  count_launch();
+  return NEGF_OK;
+}
+
+int scatter_strided(int n, int count, const double2* src, long long sSrc, const int* idx, double2* dst,
+                    long long sDst, cudaStream_t st) {
+  if (count <= 0) return NEGF_OK;
+  gather_strided_kernel<<<ew_grid((long long)n * n, count), EW_THREADS, 0, st>>>(n, src, sSrc, idx, dst, sDst, 1);
+  NEGF_CUDA_TRY(cudaGetLastError());
+  count_launch();
+  return NEGF_OK;
+}
 
 int zero_unmasked(int n, int batch, const int* keep, double2* A, long long sA, cudaStream_t st) {
   zero_unmasked_kernel<<<dim3(64, batch), 256, 0, st>>>(n, keep, A, sA);

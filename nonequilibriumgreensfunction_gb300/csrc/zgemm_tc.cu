@@ -192,13 +192,31 @@ __device__ __forceinline__ void slice_value(double x, int e, __nv_bfloat16 (&out
     else if (r < 64) F = (long long)((m + (1ULL << (r - 1))) >> r);
     if (bits >> 63) F = -F;
   }
+  // Balanced digits from the bottom, d_p = F_p - 128 floor((F_p + 64) / 128), in 32-bit
+  // arithmetic: the low 28 bits give up to four digits and a carry into F >> 28 (|F| < 2^55,
+  // so that part fits an int).  The digits are unique, so this equals the 64-bit recurrence.
+  int hi = (int)(F >> 28);
+  int lo = (int)(F & ((1LL << 28) - 1));
+  constexpr int NL = S - 1 < 4 ? S - 1 : 4;   // digits taken from the low word
 #pragma unroll
-  for (int p = S - 1; p >= 1; --p) {
-    const long long d = ((F + 64) & 127) - 64;
-    out[p] = __float2bfloat16_rn((float)d);
-    F = (F - d) >> 7;
+  for (int t = 0; t < NL; ++t) {
+    const int nx = (lo + 64) >> 7;
+    out[S - 1 - t] = __float2bfloat16_rn((float)(lo - nx * 128));
+    lo = nx;
   }
-  out[0] = __float2bfloat16_rn((float)F);
+  if constexpr (S - 1 < 4) {
+    // S <= 4: what is left of the low word and the high word form the top digit
+    out[0] = __float2bfloat16_rn((float)(lo + hi * (1 << (28 - 7 * NL))));
+  } else {
+    hi += lo;   // carry out of the low 28 bits
+#pragma unroll
+    for (int p = S - 1 - NL; p >= 1; --p) {
+      const int nx = (hi + 64) >> 7;
+      out[p] = __float2bfloat16_rn((float)(hi - nx * 128));
+      hi = nx;
+    }
+    out[0] = __float2bfloat16_rn((float)hi);
+  }
 }
 
 __device__ __forceinline__ int scale_exponent(double m) {
@@ -353,6 +371,7 @@ struct TcArgs {
   int batch;
   long long rowsA;         // rows of one (item, slice) plane in the A map (= m)
   long long rowsB;         // rows of one (item, slice) plane in the B map (= 2n)
+  int planesA, planesB;    // slice planes stored per item (>= S: the leading S are used)
   const int* ea;           // [batch][m]
   const int* fb;           // [batch][n]
   double2* C; int ldc; long long sC;
@@ -416,8 +435,10 @@ __global__ void __launch_bounds__(TC_THREADS, MINB)
         mbar_expect_tx(&full[st], (uint32_t)Cfg::STAGE);
 #pragma unroll
         for (int p = 0; p < S; ++p) {
-          tma_load_2d(sa + p * Cfg::A_TILE, &mapA, kb * BK, (int)((long long)(b * S + p) * a.rowsA + a_row0), &full[st]);
-          tma_load_2d(sb + p * Cfg::B_TILE, &mapB, kb * BK, (int)((long long)(b * S + p) * a.rowsB + b_row0), &full[st]);
+          tma_load_2d(sa + p * Cfg::A_TILE, &mapA, kb * BK,
+                      (int)((long long)(b * a.planesA + p) * a.rowsA + a_row0), &full[st]);
+          tma_load_2d(sb + p * Cfg::B_TILE, &mapB, kb * BK,
+                      (int)((long long)(b * a.planesB + p) * a.rowsB + b_row0), &full[st]);
         }
         ++issued;
       }
@@ -574,8 +595,8 @@ template <int S, int NT, int MINB>
 int launch_mma(const SlicedOperand& A, const SlicedOperand& B, const TcArgs& args, cudaStream_t st) {
   using Cfg = TcCfg<S, NT, MINB>;
   CUtensorMap ma, mb;
-  NEGF_TRY(make_map(&ma, A.data, args.kp, (long long)args.batch * S * args.rowsA, TILE_M));
-  NEGF_TRY(make_map(&mb, B.data, args.kp, (long long)args.batch * S * args.rowsB, NT));
+  NEGF_TRY(make_map(&ma, A.data, args.kp, (long long)args.batch * args.planesA * args.rowsA, TILE_M));
+  NEGF_TRY(make_map(&mb, B.data, args.kp, (long long)args.batch * args.planesB * args.rowsB, NT));
   NEGF_CUDA_TRY(cudaFuncSetAttribute(zgemm_tc_kernel<S, NT, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM));
   dim3 grid((args.m + TILE_M - 1) / TILE_M, (unsigned)((2LL * args.n + NT - 1) / NT), args.batch);
   cudaEvent_t ev;
@@ -659,20 +680,25 @@ int slice_b(const double2* B, int ldb, long long sB, int k, int n, int batch, in
 }
 
 int zgemm_tc(const SlicedOperand& A, const SlicedOperand& B, double2 alpha, double2 beta, double2* C, int ldc,
-             long long sC, int* err, cudaStream_t st) {
-  if (A.slices != B.slices || A.k != B.k || A.batch != B.batch) return NEGF_EINVAL;
+             long long sC, int* err, cudaStream_t st, int slices) {
+  // the leading `slices` digit planes of each operand (its own count by default); the
+  // leading planes of a finer slicing are a coarser slicing of the same values
+  const int S = slices ? slices : A.slices;
+  if (S > A.slices || S > B.slices || (!slices && A.slices != B.slices)) return NEGF_EINVAL;
+  if (A.k != B.k || A.batch != B.batch) return NEGF_EINVAL;
   // the leading accumulator (one pair) is exact for K' * 2^12 < 2^24; larger K would
   // round it and lose the FP64-class tail
   if (2 * A.k >= 4096) return NEGF_EINVAL;
   TcArgs args{};
   args.m = A.rows; args.n = B.rows / 2; args.kp = 2 * A.k; args.batch = A.batch;
   args.rowsA = A.rows; args.rowsB = B.rows;
+  args.planesA = A.slices; args.planesB = B.slices;
   args.ea = A.exps; args.fb = B.exps;
   args.C = C; args.ldc = ldc; args.sC = sC;
   args.alpha = alpha; args.beta = beta; args.err = err;
   args.alpha_one = (alpha.x == 1.0 && alpha.y == 0.0) ? 1 : 0;
   args.beta_kind = (beta.x == 0.0 && beta.y == 0.0) ? 0 : (beta.x == 1.0 && beta.y == 0.0) ? 1 : 2;
-  switch (A.slices) {
+  switch (S) {
     case 3: return launch_mma<3, 80, 2>(A, B, args, st);
     case 4: return launch_mma<4, 64, 2>(A, B, args, st);
     case 5: return launch_mma<5, 48, 2>(A, B, args, st);

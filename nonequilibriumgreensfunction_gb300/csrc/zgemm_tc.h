@@ -30,8 +30,10 @@ int slice_a(const double2* A, int lda, long long sA, int m, int k, int batch, in
 // B operand: K x N complex, column-major
 int slice_b(const double2* B, int ldb, long long sB, int k, int n, int batch, int slices, SlicedOperand& out,
             cudaStream_t st);
-// C = alpha A B + beta C (C column-major, ldc, batch stride sC); err: optional device flag
+// C = alpha A B + beta C (C column-major, ldc, batch stride sC); err: optional device flag.
+// slices = 0 uses every plane (A and B must have the same count); slices > 0 uses the
+// leading `slices` planes of each operand, which may have been sliced finer.
 int zgemm_tc(const SlicedOperand& A, const SlicedOperand& B, double2 alpha, double2 beta, double2* C, int ldc,
-             long long sC, int* err, cudaStream_t st);
+             long long sC, int* err, cudaStream_t st, int slices = 0);
 
 }  // namespace negf

@@ -42,9 +42,10 @@ def test_struct_layout_matches_header():
 #include <stddef.h>
 #include "negf.h"
 int main(void) {
-  printf("%zu %zu %zu %zu %zu %zu %zu\n", sizeof(negf_params), offsetof(negf_params, eta),
+  printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(negf_params), offsetof(negf_params, eta),
          offsetof(negf_params, spin_ops), offsetof(negf_params, keep_g_columns), sizeof(negf_request),
-         sizeof(negf_result), offsetof(negf_result, status));
+         sizeof(negf_result), offsetof(negf_result, status), sizeof(negf_stats), sizeof(negf_wire_model),
+         sizeof(negf_batch_outputs), sizeof(negf_wire_request));
   return 0;
 }
 """
@@ -56,7 +57,8 @@ int main(void) {
         vals = [int(v) for v in subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()]
     want = [ctypes.sizeof(capi.NegfParams), capi.NegfParams.eta.offset, capi.NegfParams.spin_ops.offset,
             capi.NegfParams.keep_g_columns.offset, ctypes.sizeof(capi.NegfRequest), ctypes.sizeof(capi.NegfResult),
-            capi.NegfResult.status.offset]
+            capi.NegfResult.status.offset, ctypes.sizeof(capi.NegfStats), ctypes.sizeof(capi.NegfWireModel),
+            ctypes.sizeof(capi.NegfBatchOutputs), ctypes.sizeof(capi.NegfWireRequest)]
     assert vals == want
 
 
