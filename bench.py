@@ -291,7 +291,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--form", default="mixed", choices=["fp64", "mixed"])
-    ap.add_argument("--batch", type=int, default=128)
+    ap.add_argument("--batch", type=int, default=256)
     ap.add_argument("--slices", type=int, default=0, help="mixed form: BF16 slices of the RGF products (0 = default)")
     ap.add_argument("--residual-slices", type=int, default=0, help="mixed form: slices of the Newton-Schulz residual")
     ap.add_argument("--sr-slices", type=int, default=0, help="mixed form: slices of the Sancho-Rubio products")

@@ -41,8 +41,14 @@ namespace negf {
 namespace {
 
 constexpr int TC_THREADS = 192;
-constexpr int BK = 32;              // K elements (bf16) per stage row: 64 bytes, SWIZZLE_64B
-constexpr int ROW_BYTES = BK * 2;   // 64
+#ifndef TC_BK
+#define TC_BK 32
+#endif
+constexpr int BK = TC_BK;           // K elements (bf16) per stage row: 64 bytes with SWIZZLE_64B
+constexpr int ROW_BYTES = BK * 2;   // (32 bytes with SWIZZLE_32B when BK = 16)
+static_assert(BK == 32 || BK == 16, "stage rows of 64 or 32 bytes");
+// tcgen05 shared-memory descriptor swizzle field: 4 = 64-byte, 6 = 32-byte swizzling
+constexpr uint64_t DESC_SWIZZLE = BK == 32 ? 4 : 6;
 constexpr int TILE_M = 128;
 constexpr uint32_t kWaitLimit = 1u << 22;   // ~1 s of polling
 
@@ -95,7 +101,7 @@ __device__ __forceinline__ uint64_t make_desc(uint32_t saddr) {
   d |= (uint64_t)(16 >> 4) << 16;
   d |= (uint64_t)((8 * ROW_BYTES) >> 4) << 32;
   d |= (uint64_t)1 << 46;
-  d |= (uint64_t)4 << 61;
+  d |= DESC_SWIZZLE << 61;
   return d;
 }
 
@@ -356,7 +362,10 @@ struct TcCfg {
   static constexpr int B_TILE = NT * ROW_BYTES;                // bytes of one B slice tile
   static constexpr int STAGE = S * (A_TILE + B_TILE);
   static constexpr int BUDGET = MINB == 2 ? 110 * 1024 : 200 * 1024;
-  static constexpr int STAGES = BUDGET / STAGE > 4 ? 4 : BUDGET / STAGE;
+#ifndef TC_MAX_STAGES
+#define TC_MAX_STAGES 4
+#endif
+  static constexpr int STAGES = BUDGET / STAGE > TC_MAX_STAGES ? TC_MAX_STAGES : BUDGET / STAGE;
   static constexpr int SMEM = STAGES * STAGE + 1024 + 256 + 4 * (NT / 2);   // + alignment, barriers, exponents
   static constexpr int TMEM_COLS_USED = S * NT;
   static constexpr int TMEM_COLS = TMEM_COLS_USED <= 32 ? 32 : TMEM_COLS_USED <= 64 ? 64
@@ -460,6 +469,10 @@ __global__ void __launch_bounds__(TC_THREADS, MINB)
         tc_fence_after();
         const uint32_t sa = smem_u32(smem + st * Cfg::STAGE);
         const uint32_t sb = sa + S * Cfg::A_TILE;
+        // descriptors of the stage's first tiles; the others differ only in the start
+        // address field (bits 0-13, address >> 4), and shared addresses stay below 2^18,
+        // so a tile's descriptor is the base plus its byte offset >> 4
+        const uint64_t da0 = make_desc(sa), db0 = make_desc(sb);
 #pragma unroll
         for (int d = 0; d < S; ++d) {
 #pragma unroll
@@ -467,8 +480,8 @@ __global__ void __launch_bounds__(TC_THREADS, MINB)
             const int q = d - p;
 #pragma unroll
             for (int kk = 0; kk < BK / 16; ++kk) {
-              const uint64_t da = make_desc(sa + p * Cfg::A_TILE + kk * 32);
-              const uint64_t db = make_desc(sb + q * Cfg::B_TILE + kk * 32);
+              const uint64_t da = da0 + (uint64_t)((p * Cfg::A_TILE + kk * 32) >> 4);
+              const uint64_t db = db0 + (uint64_t)((q * Cfg::B_TILE + kk * 32) >> 4);
               const uint32_t acc = (kb > 0 || p > 0 || kk > 0) ? 1u : 0u;
               tc_mma(tmem + d * NT, da, db, idesc, acc);
             }
@@ -586,10 +599,31 @@ int make_map(CUtensorMap* map, const void* base, int kp, long long rows, int box
   cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)box_rows};
   cuuint32_t estr[2] = {1, 1};
   CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
-                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, BK == 32 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_32B,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS ? NEGF_OK : NEGF_ECUDA;
 }
+
+// Tile configuration <slices, N tile, CTAs per SM> of the slice counts below 6 (the others
+// use N = 64 and one CTA per SM: S x N TMEM columns must fit 512 / CTAs).  Compile-time
+// defaults; a build may override them to compare variants.
+#ifndef TC_NT3
+#define TC_NT3 80
+#define TC_MINB3 2
+#endif
+#ifndef TC_NT4
+#define TC_NT4 64
+#define TC_MINB4 2
+#endif
+#ifndef TC_NT5
+#define TC_NT5 48
+#define TC_MINB5 2
+#endif
+#ifndef TC_NT7
+#define TC_NT7 64
+#define TC_MINB7 1
+#endif
 
 template <int S, int NT, int MINB>
 int launch_mma(const SlicedOperand& A, const SlicedOperand& B, const TcArgs& args, cudaStream_t st) {
@@ -699,11 +733,11 @@ int zgemm_tc(const SlicedOperand& A, const SlicedOperand& B, double2 alpha, doub
   args.alpha_one = (alpha.x == 1.0 && alpha.y == 0.0) ? 1 : 0;
   args.beta_kind = (beta.x == 0.0 && beta.y == 0.0) ? 0 : (beta.x == 1.0 && beta.y == 0.0) ? 1 : 2;
   switch (S) {
-    case 3: return launch_mma<3, 80, 2>(A, B, args, st);
-    case 4: return launch_mma<4, 64, 2>(A, B, args, st);
-    case 5: return launch_mma<5, 48, 2>(A, B, args, st);
+    case 3: return launch_mma<3, TC_NT3, TC_MINB3>(A, B, args, st);
+    case 4: return launch_mma<4, TC_NT4, TC_MINB4>(A, B, args, st);
+    case 5: return launch_mma<5, TC_NT5, TC_MINB5>(A, B, args, st);
     case 6: return launch_mma<6, 64, 1>(A, B, args, st);
-    case 7: return launch_mma<7, 64, 1>(A, B, args, st);
+    case 7: return launch_mma<7, TC_NT7, TC_MINB7>(A, B, args, st);
     case 8: return launch_mma<8, 64, 1>(A, B, args, st);
   }
   return NEGF_EINVAL;
