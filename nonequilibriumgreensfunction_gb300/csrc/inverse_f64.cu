@@ -11,7 +11,7 @@
 //                  (pivot = first max of |re|+|im| over rows >= k, as LAPACK izamax).
 //   2. gj_swap:    applies the panel's row interchanges to the other columns, copies
 //                  their rows K into R (nb x n) and zeroes them.
-//   3. zgemm:      A(:, not K) += P * R(:, not K), P = A(:, K) (the factorised panel).
+//   3. gj_update:  A(:, not K) += P * R(:, not K), P = A(:, K) (the factorised panel).
 // After the last panel, gj_colswap undoes the row pivoting as column interchanges.
 // INFO follows ZGETRF: the 1-based index of the first exactly-zero pivot (0 if none).
 #include "negf_internal.cuh"
@@ -175,6 +175,63 @@ __global__ void __launch_bounds__(SWAP_WARPS * 32) gj_swap_kernel(T* A, long lon
   }
 }
 
+// The rank-kb update of one panel step: A(:, j) += P R(:, j) for every column j outside the
+// panel [k0, k0 + kb), P = A(:, k0:k0+kb) (n x kb), R (kb x n) from gj_swap.  K = kb <= 32,
+// so each CTA stages its whole P and R slabs in shared memory with one barrier and then
+// runs the kb rank-1 steps from there: 80 x 80 output tiles, 256 threads of 5 x 5 complex
+// accumulators (25 FMAs per 10 shared loads).  The k order and the final A + sum equal
+// those of the general GEMM kernel, so results are bitwise the same.
+constexpr int UPD_T = 80, UPD_R = 5;
+template <typename T>
+__global__ void __launch_bounds__(256) gj_update_kernel(T* A, long long sA, int n, int k0, int kb, const T* R,
+                                                        long long sR) {
+  extern __shared__ __align__(16) unsigned char upd_raw[];
+  T* Ps = reinterpret_cast<T*>(upd_raw);              // [kb][UPD_T]
+  T* Rs = Ps + 32 * UPD_T;                              // [kb][UPD_T]
+  const int b = blockIdx.z;
+  const int m0 = blockIdx.x * UPD_T, n0 = blockIdx.y * UPD_T;
+  if (n0 >= k0 && n0 + UPD_T <= k0 + kb) return;        // tile inside the panel columns
+  T* Ab = A + (long long)b * sA;
+  const T* Rb = R + (long long)b * sR;
+  const int t = threadIdx.x;
+  for (int e = t; e < kb * UPD_T; e += 256) {
+    const int k = e / UPD_T, i = e % UPD_T;
+    Ps[k * UPD_T + i] = (m0 + i < n) ? Ab[(long long)(k0 + k) * n + m0 + i] : CplxTraits<T>::make(0, 0);
+    const int j = e / kb, kk = e % kb;                  // R slab: contiguous kb x UPD_T
+    Rs[kk * UPD_T + j] = (n0 + j < n) ? Rb[(long long)(n0 + j) * kb + kk] : CplxTraits<T>::make(0, 0);
+  }
+  __syncthreads();
+  const int tx = t & 15, ty = t >> 4;
+  T acc[UPD_R][UPD_R];
+#pragma unroll
+  for (int i = 0; i < UPD_R; ++i)
+#pragma unroll
+    for (int j = 0; j < UPD_R; ++j) acc[i][j] = CplxTraits<T>::make(0, 0);
+  for (int k = 0; k < kb; ++k) {
+    T av[UPD_R], bv[UPD_R];
+#pragma unroll
+    for (int i = 0; i < UPD_R; ++i) av[i] = Ps[k * UPD_T + tx + 16 * i];
+#pragma unroll
+    for (int j = 0; j < UPD_R; ++j) bv[j] = Rs[k * UPD_T + ty + 16 * j];
+#pragma unroll
+    for (int i = 0; i < UPD_R; ++i)
+#pragma unroll
+      for (int j = 0; j < UPD_R; ++j) cfma(acc[i][j], av[i], bv[j]);
+  }
+#pragma unroll
+  for (int j = 0; j < UPD_R; ++j) {
+    const int col = n0 + ty + 16 * j;
+    if (col >= n || (col >= k0 && col < k0 + kb)) continue;
+#pragma unroll
+    for (int i = 0; i < UPD_R; ++i) {
+      const int row = m0 + tx + 16 * i;
+      if (row >= n) continue;
+      T* cp = Ab + (long long)col * n + row;
+      *cp = cadd(acc[i][j], *cp);
+    }
+  }
+}
+
 // One thread per row: column interchanges in reverse pivot order.
 template <typename T>
 __global__ void gj_colswap_kernel(T* A, long long sA, int n, const int* ipiv) {
@@ -228,12 +285,6 @@ void inv_work_free(InvWork& w) {
 
 namespace {
 
-template <typename T>
-int gemm_update(const GemmBatchT<T>& g, cudaStream_t st);
-template <>
-int gemm_update<double2>(const GemmBatchT<double2>& g, cudaStream_t st) { return zgemm_f64(g, st); }
-template <>
-int gemm_update<float2>(const GemmBatchT<float2>& g, cudaStream_t st) { return cgemm_f32(g, st); }
 
 template <typename T>
 int gj_invert(T* A, long long sA, int n, int batch, InvWork& w, cudaStream_t st) {
@@ -243,6 +294,9 @@ int gj_invert(T* A, long long sA, int n, int batch, InvWork& w, cudaStream_t st)
   const size_t smem = sizeof(T) * (size_t)n * nb;
   if (smem > kPanelSmemMax) return NEGF_EINVAL;
   NEGF_CUDA_TRY(cudaFuncSetAttribute(gj_panel_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPanelSmemMax));
+  const size_t upd_smem = sizeof(T) * 2 * 32 * UPD_T;
+  NEGF_CUDA_TRY(cudaFuncSetAttribute(gj_update_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)upd_smem));
+  if (nb > 32 || batch > 65535) return NEGF_EINVAL;
   NEGF_CUDA_TRY(cudaMemsetAsync(w.info, 0, sizeof(int) * batch, st));
   T* rbuf = reinterpret_cast<T*>(w.rbuf);
   const long long sR = (long long)nb * n;
@@ -257,20 +311,15 @@ int gj_invert(T* A, long long sA, int n, int batch, InvWork& w, cudaStream_t st)
     gj_swap_kernel<T><<<g2, SWAP_WARPS * 32, 0, st>>>(A, sA, n, k0, kb, w.ipiv, rbuf, sR);
     NEGF_CUDA_TRY(cudaGetLastError());
     count_launch(2);
-    // A(:, 0:k0) += P R(:, 0:k0);  A(:, k0+kb:n) += P R(:, k0+kb:n)
-    GemmBatchT<T> g{};
-    g.m = n; g.k = kb;
-    g.alpha = CplxTraits<T>::make(1, 0); g.beta = CplxTraits<T>::make(1, 0);
-    g.A = A + (long long)k0 * n; g.lda = n; g.sA = sA; g.opA = OP_N;
-    g.ldb = kb; g.sB = sR; g.opB = OP_N;
-    g.ldc = n; g.sC = sA; g.batch = batch;
-    if (k0 > 0) {
-      g.n = k0; g.B = rbuf; g.C = A;
-      NEGF_TRY(gemm_update<T>(g, st));
-    }
-    if (k0 + kb < n) {
-      g.n = n - k0 - kb; g.B = rbuf + (long long)(k0 + kb) * kb; g.C = A + (long long)(k0 + kb) * n;
-      NEGF_TRY(gemm_update<T>(g, st));
+    // A(:, j) += P R(:, j) for the columns outside the panel
+    {
+      cudaEvent_t eu;
+      timed_begin(st, sizeof(T) == 8 ? TK_F32 : TK_GEMM, 8.0 * n * (double)(n - kb) * kb * batch, &eu);
+      dim3 gu((n + UPD_T - 1) / UPD_T, (n + UPD_T - 1) / UPD_T, batch);
+      gj_update_kernel<T><<<gu, 256, upd_smem, st>>>(A, sA, n, k0, kb, rbuf, sR);
+      NEGF_CUDA_TRY(cudaGetLastError());
+      timed_end(st, sizeof(T) == 8 ? TK_F32 : TK_GEMM, eu);
+      count_launch();
     }
   }
   dim3 g3((n + 127) / 128, batch);

@@ -29,6 +29,7 @@
 //
 // Replaces, in the mixed form, the ZGEMM calls of Source/Recursive_Greens.F90 and the
 // G Gamma products of Source/Calculate_Gnp.F90.
+#include <algorithm>
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
@@ -577,6 +578,263 @@ __global__ void __launch_bounds__(TC_THREADS, MINB)
 // ---------------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------------
+// ---------------------------------------------------------------------------------
+// Persistent form: one CTA per SM walks the output tiles (tn fastest, so the CTAs running
+// at the same time share their A tiles in L2).  A ring of STAGES shared-memory stages runs
+// across tile boundaries, and TMEM holds two accumulator sets, so the epilogue of one tile
+// overlaps the MMAs of the next and the producer keeps STAGES - 1 stages in flight.
+//   warp 0     TMA producer over (tile, K block)
+//   warp 1     TMEM allocation; MMA issue into accumulator set (tile count & 1)
+//   warps 2-5  epilogue of each tile from its accumulator set, then release the set
+// Barriers: full/empty per stage (as the per-tile kernel), tfull[2] (MMA commit -> epilogue)
+// and tempty[2] (128 epilogue arrivals -> MMA).  Every wait is bounded; a timeout sets the
+// abort flag and the error code, every role leaves its loop, and the MMA warp waits for
+// its issued MMAs to complete before TMEM is freed.
+// ---------------------------------------------------------------------------------
+template <int S, int NT>
+struct TcPCfg {
+  static constexpr int A_TILE = TILE_M * ROW_BYTES;
+  static constexpr int B_TILE = NT * ROW_BYTES;
+  static constexpr int STAGE = S * (A_TILE + B_TILE);
+  static constexpr int BUDGET = 220 * 1024;
+  static constexpr int STAGES = BUDGET / STAGE > 6 ? 6 : BUDGET / STAGE;
+  static constexpr int ACC = S * NT;   // TMEM columns of one accumulator set
+  static constexpr int SMEM = STAGES * STAGE + 1024 + 256 + 4 * NT;   // + alignment, barriers, exponents
+  static_assert(STAGES >= 2, "at least two stages");
+  static_assert(2 * ACC <= 512, "two accumulator sets in TMEM");
+  static_assert(SMEM <= 227 * 1024, "shared memory of one CTA");
+  static_assert(NT % 16 == 0 && NT >= 16 && NT <= 256, "UMMA N");
+};
+
+// named barrier 1 over the 128 epilogue threads that also ORs a predicate: every thread
+// gets the same answer, so the four warps always take the same branch out of a loop
+__device__ __forceinline__ bool epi_barrier_any(bool v) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\t"
+      "setp.ne.u32 p, %1, 0;\n\t"
+      "bar.red.or.pred q, 1, 128, p;\n\t"
+      "selp.u32 %0, 1, 0, q;\n\t}"
+      : "=r"(r)
+      : "r"((uint32_t)v)
+      : "memory");
+  return r != 0;
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+template <int S, int NT>
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    zgemm_tc_persistent(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, TcArgs a,
+                        int tiles_m, int tiles_n) {
+  using Cfg = TcPCfg<S, NT>;
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + Cfg::STAGES * Cfg::STAGE);
+  uint64_t* empty = full + Cfg::STAGES;
+  uint64_t* tfull = empty + Cfg::STAGES;
+  uint64_t* tempty = tfull + 2;
+  uint64_t* fin = tempty + 2;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(fin + 1);
+  int* abort_flag = reinterpret_cast<int*>(tmem_slot + 1);
+  int* col_exp = abort_flag + 1;   // [2][NT/2] column exponents of the tiles in flight
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nk = (a.kp + BK - 1) / BK;
+  const long long tiles_item = (long long)tiles_m * tiles_n;
+  const long long ntiles = tiles_item * a.batch;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < Cfg::STAGES; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
+    for (int s = 0; s < 2; ++s) { mbar_init(&tfull[s], 1); mbar_init(&tempty[s], 128); }
+    mbar_init(fin, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(512u));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&mapA)) : "memory");
+      asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&mapB)) : "memory");
+      uint32_t kg = 0;   // stage-ring position, continuous across tiles
+      for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const int b = (int)(t / tiles_item);
+        const int r = (int)(t % tiles_item);
+        const int a_row0 = (r / tiles_n) * TILE_M, b_row0 = (r % tiles_n) * NT;
+        bool stop = false;
+        for (int kb = 0; kb < nk; ++kb, ++kg) {
+          const int st = (int)(kg % Cfg::STAGES);
+          if (!mbar_wait(&empty[st], ((kg / Cfg::STAGES) & 1) ^ 1)) {
+            atomicExch(abort_flag, 1);
+            if (a.err) atomicCAS(a.err, 0, 1);
+            stop = true;
+            break;
+          }
+          if (*((volatile int*)abort_flag)) { stop = true; break; }
+          uint8_t* sa = smem + st * Cfg::STAGE;
+          uint8_t* sb = sa + S * Cfg::A_TILE;
+          mbar_expect_tx(&full[st], (uint32_t)Cfg::STAGE);
+#pragma unroll
+          for (int p = 0; p < S; ++p) {
+            tma_load_2d(sa + p * Cfg::A_TILE, &mapA, kb * BK,
+                        (int)((long long)(b * a.planesA + p) * a.rowsA + a_row0), &full[st]);
+            tma_load_2d(sb + p * Cfg::B_TILE, &mapB, kb * BK,
+                        (int)((long long)(b * a.planesB + p) * a.rowsB + b_row0), &full[st]);
+          }
+        }
+        if (stop) break;
+      }
+      // drain: every issued stage must have landed before the CTA may exit
+      for (uint32_t k = (kg > (uint32_t)Cfg::STAGES ? kg - Cfg::STAGES : 0); k < kg; ++k)
+        mbar_wait(&full[k % Cfg::STAGES], (k / Cfg::STAGES) & 1);
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      constexpr uint32_t idesc = make_idesc(TILE_M, NT);
+      uint32_t kg = 0;
+      int it = 0;
+      bool stop = false;
+      for (long long t = blockIdx.x; t < ntiles && !stop; t += gridDim.x, ++it) {
+        const int buf = it & 1;
+        if (!mbar_wait(&tempty[buf], ((it >> 1) & 1) ^ 1)) {
+          atomicExch(abort_flag, 1);
+          if (a.err) atomicCAS(a.err, 0, 4);
+          break;
+        }
+        tc_fence_after();
+        const uint32_t acc0 = tmem + (uint32_t)(buf * Cfg::ACC);
+        for (int kb = 0; kb < nk; ++kb, ++kg) {
+          const int st = (int)(kg % Cfg::STAGES);
+          if (!mbar_wait(&full[st], (kg / Cfg::STAGES) & 1)) {
+            atomicExch(abort_flag, 1);
+            if (a.err) atomicCAS(a.err, 0, 2);
+            stop = true;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t sa = smem_u32(smem + st * Cfg::STAGE);
+          const uint32_t sb = sa + S * Cfg::A_TILE;
+          const uint64_t da0 = make_desc(sa), db0 = make_desc(sb);
+#pragma unroll
+          for (int d = 0; d < S; ++d) {
+#pragma unroll
+            for (int p = 0; p <= d; ++p) {
+              const int q = d - p;
+#pragma unroll
+              for (int kk = 0; kk < BK / 16; ++kk) {
+                const uint64_t da = da0 + (uint64_t)((p * Cfg::A_TILE + kk * 32) >> 4);
+                const uint64_t db = db0 + (uint64_t)((q * Cfg::B_TILE + kk * 32) >> 4);
+                const uint32_t acc = (kb > 0 || p > 0 || kk > 0) ? 1u : 0u;
+                tc_mma(acc0 + d * NT, da, db, idesc, acc);
+              }
+            }
+          }
+          tc_commit(&empty[st]);
+        }
+        if (!stop) tc_commit(&tfull[buf]);
+      }
+      // every issued MMA has completed before TMEM may be freed
+      tc_commit(fin);
+      mbar_wait(fin, 0);
+    }
+  } else {
+    const int quarter = warp & 3;
+    int it = 0;
+    for (long long t = blockIdx.x; t < ntiles; t += gridDim.x, ++it) {
+      const int buf = it & 1;
+      const int b = (int)(t / tiles_item);
+      const int r = (int)(t % tiles_item);
+      const int tm = r / tiles_n, tn = r % tiles_n;
+      int* cexp = col_exp + buf * (NT / 2);
+      for (int c = threadIdx.x - 64; c < NT / 2; c += 128) {
+        const int col = tn * (NT / 2) + c;
+        cexp[c] = col < a.n ? a.fb[(long long)b * a.n + col] : 0;
+      }
+      // the exponents are visible to all four warps, and all agree on stopping
+      if (epi_barrier_any(*((volatile int*)abort_flag) != 0)) break;
+      const bool ok = mbar_wait(&tfull[buf], (it >> 1) & 1);
+      if (epi_barrier_any(!ok)) {
+        atomicExch(abort_flag, 1);
+        if (a.err) atomicCAS(a.err, 0, 3);
+        break;
+      }
+      tc_fence_after();
+      const int row = tm * TILE_M + quarter * 32 + lane;
+      const int e_row = (row < a.m) ? a.ea[(long long)b * a.m + row] : 0;
+      double2* Cb = a.C + (long long)b * a.sC;
+      const uint32_t acc0 = tmem + (uint32_t)(buf * Cfg::ACC);
+      constexpr int CW = 8;   // fp32 columns per chunk
+#pragma unroll 1
+      for (int c0 = 0; c0 < NT; c0 += CW) {
+        constexpr int DH = S <= 6 ? S : 3;   // S <= 6 fits one int64; S >= 7 splits
+        long long hi[CW], lo[CW];
+#pragma unroll
+        for (int i = 0; i < CW; ++i) { hi[i] = 0; lo[i] = 0; }
+        uint32_t raw[S][CW];
+#pragma unroll
+        for (int d = 0; d < S; ++d) {
+          const uint32_t ta = acc0 + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(d * NT + c0);
+          tmem_ld8_nowait(ta, *reinterpret_cast<uint32_t(*)[8]>(&raw[d][0]));
+        }
+        tmem_wait_ld();
+#pragma unroll
+        for (int d = 0; d < S; ++d) {
+#pragma unroll
+          for (int i = 0; i < CW; ++i) {
+            const long long q = (long long)__float2ll_rn(__uint_as_float(raw[d][i]));
+            if (d < DH) hi[i] += q * (1LL << (7 * (DH - 1 - d)));
+            else lo[i] += q * (1LL << (7 * (S - 1 - d)));
+          }
+        }
+        if (row >= a.m) continue;
+        const int col0 = (tn * NT + c0) / 2;
+        double2 cin[CW / 2];
+        if (a.beta_kind != 0) {
+#pragma unroll
+          for (int jj = 0; jj < CW / 2; ++jj)
+            cin[jj] = (col0 + jj < a.n) ? Cb[(long long)(col0 + jj) * a.ldc + row] : make_double2(0.0, 0.0);
+        }
+#pragma unroll
+        for (int jj = 0; jj < CW / 2; ++jj) {
+          const int col = col0 + jj;
+          if (col >= a.n) continue;
+          const int sc = e_row + cexp[c0 / 2 + jj] - 12 - 7 * (S - 1);
+          double re = scaled_int_to_double(hi[2 * jj], sc + 7 * (S - DH));
+          double im = scaled_int_to_double(hi[2 * jj + 1], sc + 7 * (S - DH));
+          if (DH < S) {
+            re += scaled_int_to_double(lo[2 * jj], sc);
+            im += scaled_int_to_double(lo[2 * jj + 1], sc);
+          }
+          double2 out = make_double2(re, im);
+          if (!a.alpha_one) out = cmul(a.alpha, out);
+          if (a.beta_kind == 1) out = cadd(out, cin[jj]);
+          else if (a.beta_kind == 2) out = cadd(out, cmul(a.beta, cin[jj]));
+          Cb[(long long)col * a.ldc + row] = out;
+        }
+      }
+      tc_fence_before();
+      mbar_arrive(&tempty[buf]);
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512u));
+  }
+}
+
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
   if (!fn) {
@@ -608,6 +866,12 @@ int make_map(CUtensorMap* map, const void* base, int kp, long long rows, int box
 // Tile configuration <slices, N tile, CTAs per SM> of the slice counts below 6 (the others
 // use N = 64 and one CTA per SM: S x N TMEM columns must fit 512 / CTAs).  Compile-time
 // defaults; a build may override them to compare variants.
+#ifndef TC_PERSIST
+#define TC_PERSIST 0    // 1: every slice count through the persistent kernel
+#endif
+#ifndef TC_PERSIST5
+#define TC_PERSIST5 1   // 5 slices through the persistent kernel
+#endif
 #ifndef TC_NT3
 #define TC_NT3 80
 #define TC_MINB3 2
@@ -638,6 +902,38 @@ int launch_mma(const SlicedOperand& A, const SlicedOperand& B, const TcArgs& arg
   add_tc_complex_flops(cflops);
   timed_begin(st, TK_TC, cflops * (S * (S + 1) / 2), &ev);
   zgemm_tc_kernel<S, NT, MINB><<<grid, TC_THREADS, Cfg::SMEM, st>>>(ma, mb, args);
+  NEGF_CUDA_TRY(cudaGetLastError());
+  timed_end(st, TK_TC, ev);
+  count_launch();
+  return NEGF_OK;
+}
+
+int sm_count() {
+  static int n = 0;
+  if (n == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 148;
+  }
+  return n;
+}
+
+template <int S, int NT>
+int launch_persistent(const SlicedOperand& A, const SlicedOperand& B, const TcArgs& args, cudaStream_t st) {
+  using Cfg = TcPCfg<S, NT>;
+  CUtensorMap ma, mb;
+  NEGF_TRY(make_map(&ma, A.data, args.kp, (long long)args.batch * args.planesA * args.rowsA, TILE_M));
+  NEGF_TRY(make_map(&mb, B.data, args.kp, (long long)args.batch * args.planesB * args.rowsB, NT));
+  NEGF_CUDA_TRY(cudaFuncSetAttribute(zgemm_tc_persistent<S, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM));
+  const int tiles_m = (args.m + TILE_M - 1) / TILE_M;
+  const int tiles_n = (int)((2LL * args.n + NT - 1) / NT);
+  const long long ntiles = (long long)tiles_m * tiles_n * args.batch;
+  const int grid = (int)std::min<long long>(ntiles, sm_count());
+  cudaEvent_t ev;
+  const double cflops = 8.0 * args.m * (double)args.n * (args.kp / 2) * args.batch;
+  add_tc_complex_flops(cflops);
+  timed_begin(st, TK_TC, cflops * (S * (S + 1) / 2), &ev);
+  zgemm_tc_persistent<S, NT><<<grid, TC_THREADS, Cfg::SMEM, st>>>(ma, mb, args, tiles_m, tiles_n);
   NEGF_CUDA_TRY(cudaGetLastError());
   timed_end(st, TK_TC, ev);
   count_launch();
@@ -732,6 +1028,21 @@ int zgemm_tc(const SlicedOperand& A, const SlicedOperand& B, double2 alpha, doub
   args.alpha = alpha; args.beta = beta; args.err = err;
   args.alpha_one = (alpha.x == 1.0 && alpha.y == 0.0) ? 1 : 0;
   args.beta_kind = (beta.x == 0.0 && beta.y == 0.0) ? 0 : (beta.x == 1.0 && beta.y == 0.0) ? 1 : 2;
+#if TC_PERSIST
+  switch (S) {
+    case 3: return launch_persistent<3, 80>(A, B, args, st);
+    case 4: return launch_persistent<4, 64>(A, B, args, st);
+    case 5: return launch_persistent<5, 48>(A, B, args, st);
+    case 6: return launch_persistent<6, 32>(A, B, args, st);
+    case 7: return launch_persistent<7, 32>(A, B, args, st);
+    case 8: return launch_persistent<8, 32>(A, B, args, st);
+  }
+  return NEGF_EINVAL;
+#endif
+  // measured on GB300 (batch 128, M = 400): at 5 slices the persistent form issues 659 TFLOP/s
+  // against 561 for two per-tile CTAs per SM; at 3 slices (little MMA work per stage) and 7
+  // slices (two accumulator sets leave N = 32) the per-tile kernel is as fast or faster
+  if (S == 5 && TC_PERSIST5) return launch_persistent<5, 48>(A, B, args, st);
   switch (S) {
     case 3: return launch_mma<3, TC_NT3, TC_MINB3>(A, B, args, st);
     case 4: return launch_mma<4, TC_NT4, TC_MINB4>(A, B, args, st);
