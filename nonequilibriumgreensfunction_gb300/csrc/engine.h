@@ -111,7 +111,9 @@ class Engine {
   int s_sr_ = 8;       // Sancho-Rubio products: 2^-56, the decimation is ill-conditioned near band edges
   int s_res_ = 7;      // Newton-Schulz residual W X (2^-49, FP64-class)
   int s_res0_ = 5;     // the first residual (2^-35: the second step squares its error)
-  int s_upd_ = 3;      // Newton-Schulz update X R (R is small: 2^-21 of it is below the target)
+  int s_upd_ = 3;      // Newton-Schulz update X R: its error, ~sqrt(M) 2^-7S of |X||R|, must stay
+                       // well below |R| for quadratic convergence; 2 slices (~1e-3 at M = 400)
+                       // broke the mixed-form tolerance, 3 slices (~1e-5) keep it
   int ns_steps_ = 2;        // Newton-Schulz steps always taken
   int ns_max_steps_ = 4;    // more while the latest residual norm is above ns_tol_
   double ns_tol_ = 1e-5;     // residual norm before the last update; that update squares it

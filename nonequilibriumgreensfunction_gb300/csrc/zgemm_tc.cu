@@ -30,6 +30,8 @@
 // Replaces, in the mixed form, the ZGEMM calls of Source/Recursive_Greens.F90 and the
 // G Gamma products of Source/Calculate_Gnp.F90.
 #include <algorithm>
+#include <mutex>
+#include <map>
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
@@ -869,9 +871,6 @@ int make_map(CUtensorMap* map, const void* base, int kp, long long rows, int box
 #ifndef TC_PERSIST
 #define TC_PERSIST 0    // 1: every slice count through the persistent kernel
 #endif
-#ifndef TC_PERSIST5
-#define TC_PERSIST5 1   // 5 slices through the persistent kernel
-#endif
 #ifndef TC_NT3
 #define TC_NT3 80
 #define TC_MINB3 2
@@ -983,6 +982,7 @@ int slice_a(const double2* A, int lda, long long sA, int m, int k, int batch, in
     return NEGF_EINVAL;
   out.rows = m; out.k = padded_k(k); out.slices = slices; out.batch = batch;
   switch (slices) {
+    case 2: return slice_a_t<2>(A, lda, sA, m, k, batch, out, st);
     case 3: return slice_a_t<3>(A, lda, sA, m, k, batch, out, st);
     case 4: return slice_a_t<4>(A, lda, sA, m, k, batch, out, st);
     case 5: return slice_a_t<5>(A, lda, sA, m, k, batch, out, st);
@@ -999,6 +999,7 @@ int slice_b(const double2* B, int ldb, long long sB, int k, int n, int batch, in
     return NEGF_EINVAL;
   out.rows = 2 * n; out.k = padded_k(k); out.slices = slices; out.batch = batch;
   switch (slices) {
+    case 2: return slice_b_t<2>(B, ldb, sB, k, n, batch, out, st);
     case 3: return slice_b_t<3>(B, ldb, sB, k, n, batch, out, st);
     case 4: return slice_b_t<4>(B, ldb, sB, k, n, batch, out, st);
     case 5: return slice_b_t<5>(B, ldb, sB, k, n, batch, out, st);
@@ -1007,6 +1008,72 @@ int slice_b(const double2* B, int ldb, long long sB, int k, int n, int batch, in
     case 8: return slice_b_t<8>(B, ldb, sB, k, n, batch, out, st);
   }
   return NEGF_EINVAL;
+}
+
+int launch_persistent_s(int S, const SlicedOperand& A, const SlicedOperand& B, const TcArgs& args, cudaStream_t st);
+int launch_per_tile_s(int S, const SlicedOperand& A, const SlicedOperand& B, const TcArgs& args, cudaStream_t st);
+
+namespace {
+
+// Autotuner of the kernel variant per shape (slices, m, n, K', batch rounded up to a power
+// of two): the per-tile kernel (several CTAs per SM for S <= 5) or the persistent kernel.
+// Both issue each tile's MMAs in the same order into the same accumulators and run the same
+// epilogue, so their results are bitwise identical and the choice never changes a number.
+// The first call of a shape with beta = 0 runs both variants (each overwrites C with the
+// same values), times them with events on the caller's stream and keeps the faster; calls
+// with beta != 0 before that use the per-tile kernel.
+struct TuneKey {
+  int S, m, n, kp, batch;
+  bool operator<(const TuneKey& o) const {
+    if (S != o.S) return S < o.S;
+    if (m != o.m) return m < o.m;
+    if (n != o.n) return n < o.n;
+    if (kp != o.kp) return kp < o.kp;
+    return batch < o.batch;
+  }
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, int> g_tune;   // 0 per-tile, 1 persistent
+
+float time_variant(int v, int S, const SlicedOperand& A, const SlicedOperand& B, const TcArgs& args, cudaStream_t st) {
+  cudaEvent_t e0, e1;
+  if (cudaEventCreate(&e0) != cudaSuccess) return -1.0f;
+  if (cudaEventCreate(&e1) != cudaSuccess) { cudaEventDestroy(e0); return -1.0f; }
+  cudaEventRecord(e0, st);
+  const int rc = v ? launch_persistent_s(S, A, B, args, st) : launch_per_tile_s(S, A, B, args, st);
+  cudaEventRecord(e1, st);
+  float ms = -1.0f;
+  if (rc == NEGF_OK && cudaEventSynchronize(e1) == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return rc == NEGF_OK ? ms : -1.0f;
+}
+
+}  // namespace
+
+// returns the variant to launch, or -2 when tuning already ran the product (C is written)
+int choose_variant(int S, const SlicedOperand& A, const SlicedOperand& B, const TcArgs& args, cudaStream_t st) {
+  int bb = 1;
+  while (bb < args.batch) bb <<= 1;
+  const TuneKey key{S, args.m, args.n, args.kp, bb};
+  {
+    std::lock_guard<std::mutex> g(g_tune_mu);
+    auto it = g_tune.find(key);
+    if (it != g_tune.end()) return it->second;
+  }
+  if (args.beta_kind != 0) return 0;
+  // two timings each, after a first run of each that pays one-time costs
+  float best[2] = {1e30f, 1e30f};
+  for (int rep = 0; rep < 3; ++rep)
+    for (int v = 0; v < 2; ++v) {
+      const float ms = time_variant(v, S, A, B, args, st);
+      if (ms < 0.0f) return -3;
+      if (rep > 0 && ms < best[v]) best[v] = ms;
+    }
+  const int choice = best[1] < best[0] ? 1 : 0;
+  std::lock_guard<std::mutex> g(g_tune_mu);
+  g_tune[key] = choice;
+  return -2;
 }
 
 int zgemm_tc(const SlicedOperand& A, const SlicedOperand& B, double2 alpha, double2 beta, double2* C, int ldc,
@@ -1030,6 +1097,7 @@ int zgemm_tc(const SlicedOperand& A, const SlicedOperand& B, double2 alpha, doub
   args.beta_kind = (beta.x == 0.0 && beta.y == 0.0) ? 0 : (beta.x == 1.0 && beta.y == 0.0) ? 1 : 2;
 #if TC_PERSIST
   switch (S) {
+    case 2: return launch_persistent<2, 128>(A, B, args, st);
     case 3: return launch_persistent<3, 80>(A, B, args, st);
     case 4: return launch_persistent<4, 64>(A, B, args, st);
     case 5: return launch_persistent<5, 48>(A, B, args, st);
@@ -1039,11 +1107,29 @@ int zgemm_tc(const SlicedOperand& A, const SlicedOperand& B, double2 alpha, doub
   }
   return NEGF_EINVAL;
 #endif
-  // measured on GB300 (batch 128, M = 400): at 5 slices the persistent form issues 659 TFLOP/s
-  // against 561 for two per-tile CTAs per SM; at 3 slices (little MMA work per stage) and 7
-  // slices (two accumulator sets leave N = 32) the per-tile kernel is as fast or faster
-  if (S == 5 && TC_PERSIST5) return launch_persistent<5, 48>(A, B, args, st);
+  const int variant = choose_variant(S, A, B, args, st);
+  if (variant == -2) return NEGF_OK;        // the tuning runs computed C
+  if (variant == -3) return NEGF_ECUDA;
+  if (variant == 1) return launch_persistent_s(S, A, B, args, st);
+  return launch_per_tile_s(S, A, B, args, st);
+}
+
+int launch_persistent_s(int S, const SlicedOperand& A, const SlicedOperand& B, const TcArgs& args, cudaStream_t st) {
   switch (S) {
+    case 2: return launch_persistent<2, 128>(A, B, args, st);
+    case 3: return launch_persistent<3, 80>(A, B, args, st);
+    case 4: return launch_persistent<4, 64>(A, B, args, st);
+    case 5: return launch_persistent<5, 48>(A, B, args, st);
+    case 6: return launch_persistent<6, 32>(A, B, args, st);
+    case 7: return launch_persistent<7, 32>(A, B, args, st);
+    case 8: return launch_persistent<8, 32>(A, B, args, st);
+  }
+  return NEGF_EINVAL;
+}
+
+int launch_per_tile_s(int S, const SlicedOperand& A, const SlicedOperand& B, const TcArgs& args, cudaStream_t st) {
+  switch (S) {
+    case 2: return launch_mma<2, 128, 2>(A, B, args, st);   // internal: small corrections
     case 3: return launch_mma<3, TC_NT3, TC_MINB3>(A, B, args, st);
     case 4: return launch_mma<4, TC_NT4, TC_MINB4>(A, B, args, st);
     case 5: return launch_mma<5, TC_NT5, TC_MINB5>(A, B, args, st);
