@@ -90,7 +90,7 @@ Engine::~Engine() {
   inv_work_free(inv_);
   dfree(dWinv_); dfree(dW32_); dfree(dT_); dfree(sa_.data); dfree(sb_.data); dfree(sa_.exps); dfree(sb_.exps);
   dfree(sw_.data); dfree(sw_.exps); dfree(sgl_.data); dfree(sgl_.exps); dfree(sgr_.data); dfree(sgr_.exps);
-  dfree(dRnorm_); dfree(dNsActive_); dfree(dNsIdx_); dfree(dNsX_); dfree(dNsW_); dfree(dTcErr_);
+  dfree(dRnorm_); dfree(dNsIdx_); dfree(dNsX_); dfree(dNsW_); dfree(dTcErr_);
   if (hPin_) cudaFreeHost(hPin_);
   if (own_st_) cudaStreamDestroy(own_st_);
 }
@@ -206,7 +206,6 @@ int Engine::alloc() {
     sb_.data_bytes = sliced_bytes(2 * M_, kp, smax, cap);
     sa_.exps_count = sb_.exps_count = sw_.exps_count = (size_t)cap * M_;
     NEGF_TRY(dalloc(&dRnorm_, (size_t)cap, bytes_));
-    NEGF_TRY(dalloc(&dNsActive_, (size_t)cap, bytes_));
     NEGF_TRY(dalloc(&dNsIdx_, (size_t)cap, bytes_));
     NEGF_TRY(dalloc(&dNsX_, (size_t)cap * MM_, bytes_));
     NEGF_TRY(dalloc(&dNsW_, (size_t)cap * MM_, bytes_));

@@ -125,7 +125,6 @@ class Engine {
   SlicedOperand sa_, sb_, sw_;   // sw_: slices of the matrix under inversion (kept across NS steps)
   SlicedOperand sgl_, sgr_;      // Gamma_L, Gamma_R as B operands, sliced once per sweep
   unsigned long long* dRnorm_ = nullptr;
-  int* dNsActive_ = nullptr;  // per-matrix flags (zero_unmasked)
   int* dNsIdx_ = nullptr;     // matrices still taking Newton-Schulz steps beyond ns_steps_
   double2 *dNsX_ = nullptr, *dNsW_ = nullptr;   // their X and W, gathered into a compact batch
   long long ns_extra_ = 0;    // matrix-steps taken beyond ns_steps_ (statistics)

@@ -296,7 +296,5 @@ int gather_strided(int n, int count, const double2* src, long long sSrc, const i
                    cudaStream_t st);
 int scatter_strided(int n, int count, const double2* src, long long sSrc, const int* idx, double2* dst,
                     long long sDst, cudaStream_t st);
-// A[b] = 0 for every b with keep[b] == 0 (device flags)
-int zero_unmasked(int n, int batch, const int* keep, double2* A, long long sA, cudaStream_t st);
 
 }  // namespace negf

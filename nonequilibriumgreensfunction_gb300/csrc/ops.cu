@@ -796,17 +796,6 @@ int to_f64(int n, int batch, const float2* src, long long sS, double2* dst, long
 }
 
 namespace {
-__global__ void zero_unmasked_kernel(int n, const int* keep, double2* A, long long sA) {
-  const int b = blockIdx.y;
-  if (keep[b]) return;
-  const long long nn = (long long)n * n;
-  double2* Ab = A + (long long)b * sA;
-  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nn; e += (long long)gridDim.x * blockDim.x)
-    Ab[e] = make_double2(0.0, 0.0);
-}
-}  // namespace
-
-namespace {
 __global__ void gather_strided_kernel(int n, const double2* src, long long sSrc, const int* idx, double2* dst,
                                       long long sDst, int scatter) {
   const int i = blockIdx.y;
@@ -836,12 +825,6 @@ int scatter_strided(int n, int count, const double2* src, long long sSrc, const 
   return NEGF_OK;
 }
 
-int zero_unmasked(int n, int batch, const int* keep, double2* A, long long sA, cudaStream_t st) {
-  zero_unmasked_kernel<<<dim3(64, batch), 256, 0, st>>>(n, keep, A, sA);
-  NEGF_CUDA_TRY(cudaGetLastError());
-  count_launch();
-  return NEGF_OK;
-}
 
 int ns_residual(int n, int batch, double2* T, long long sT, unsigned long long* rnorm, cudaStream_t st) {
   dim3 grid((n + 31) / 32, batch);

@@ -77,3 +77,16 @@ def test_inverse_matches_lapack(need_gpu):
     S[:, 3] = 0
     _, info = capi.zinv(S)
     assert info == 4          # LAPACK INFO: 1-based index of the first zero pivot
+
+
+def test_tensor_core_variant_choice_does_not_change_results(need_gpu):
+    """The first product of a shape times the per-tile and the persistent tcgen05 kernels
+    and keeps the faster; both issue the same MMAs in the same order, so the tuning call
+    and the later (cached-choice) calls give bitwise equal results."""
+    rng = np.random.default_rng(11)
+    for s in (3, 5, 7):
+        a = rng.standard_normal((6, 96, 96)) + 1j * rng.standard_normal((6, 96, 96))
+        b = rng.standard_normal((6, 96, 96)) + 1j * rng.standard_normal((6, 96, 96))
+        first = capi.zgemm(a, b, slices=s)
+        again = capi.zgemm(a, b, slices=s)
+        assert np.array_equal(first, again)
