@@ -242,6 +242,53 @@ def serving_bench(seconds, device):
                     "wires sent as models and built on the device"}
 
 
+def run_scf_bench(args):
+    """Self-consistent bias point at the config-5 geometry: Npx = 60, Npy = Npz = 12 (M = 576),
+    W = 0.1 eV, mu_L - mu_R = 0.05 eV, eps_r = 100, a 0.1 eV gate on the wire surface, linear
+    mixing 0.3 for 10 iterations, mixed form.  The sample is 64 energies x 2 disorder seeds
+    per iteration (the configuration names 1024 x 8), stated in the output.  The mixed solve
+    is then compared with the FP64 solve on the converged potential: T(E) at 16 energies."""
+    from nonequilibriumgreensfunction_gb300 import Solver, scf
+    from nonequilibriumgreensfunction_gb300 import hamiltonian as HB
+    npx, npy, npz, n_seeds, n_e, n_iter = 60, 12, 12, 2, 64, 10
+    mu_l, mu_r = 0.025, -0.025
+    models = [HB.wire_model(W=0.1, seed=s, zeeman=ZEEMAN) for s in range(n_seeds)]
+    energies = np.linspace(-0.3, 0.3, n_e)
+    de = energies[1] - energies[0]
+    with Solver(npx, npy, npz, n_hamiltonians=n_seeds, max_batch=n_e * n_seeds, eta=ETA, sr_tol=SR_TOL,
+                precision="mixed") as s:
+        t0 = time.perf_counter()
+        out = scf.run_scf(s, models, energies, de, mu_l, mu_r, KT, eps_r=100.0, u_gate=0.1, beta=0.3,
+                          n_iter=n_iter)
+        wall = time.perf_counter() - t0
+    sub = np.linspace(0, n_e - 1, 16).astype(int)
+    e_sub = energies[sub]
+    f1 = np.array([scf.occupation(e, mu_l, KT) for e in e_sub])
+    f2 = np.array([scf.occupation(e, mu_r, KT) for e in e_sub])
+    t = {}
+    for prec in ("mixed", "fp64"):
+        with Solver(npx, npy, npz, max_batch=16, eta=ETA, sr_tol=SR_TOL, precision=prec) as s:
+            m = dict(models[0])
+            m["V"] = out["U"][..., 0]
+            s.build_hamiltonian(m)
+            t[prec] = s.solve_batch(e_sub, f1, f2, de)["T12"]
+    rel = np.abs(t["mixed"] - t["fp64"]) / np.maximum(np.abs(t["fp64"]), 1e-3)
+    solves = n_iter * n_e * n_seeds
+    line = {"metric": "self-consistent bias point: wall time per outer iteration", "workload": "scf_M576_Npx60",
+            "value": wall / n_iter, "unit": "s/iteration", "higher_is_better": False,
+            "solves_per_s": solves / wall, "iterations": n_iter,
+            "history_max_change_eV": [h["max_change"] for h in out["history"]],
+            "history_rel_change": [h["rel_change"] for h in out["history"]],
+            "poisson_iters": [h["poisson_iters"] for h in out["history"]],
+            "t_rel_err_max_on_converged_potential": float(rel.max()), "t_err_gate": 1e-6,
+            "config": {"npx": npx, "npy": npy, "npz": npz, "M": 4 * npy * npz, "seeds": n_seeds,
+                       "energies_per_iteration": n_e, "eps_r": 100.0, "gate_eV": 0.1, "mixing": 0.3,
+                       "mu_l": mu_l, "mu_r": mu_r, "kT": KT,
+                       "sample": "64 energies x 2 seeds per iteration (config: 1024 x 8)"},
+            "data": "synthetic"}
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -301,6 +348,8 @@ def main():
                     help="mixed form: requests of each compared step solved in FP64 (a prefix of the step)")
     ap.add_argument("--npx", type=int, default=NPX,
                     help="slices of the wire; the benchmark workload is 100, shorter wires only for profiling")
+    ap.add_argument("--workload", default="wire", choices=["wire", "scf"],
+                    help="wire: the solves/s benchmark; scf: the self-consistent bias point (config 5 geometry)")
     ap.add_argument("--kernel-case", default="none", choices=["none", "gemm_tc"],
                     help="profiling aid: run only one kernel case (gemm_tc: 16 complex 400^3 products at "
                          "--slices slices, twice) and exit")
@@ -318,6 +367,9 @@ def main():
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         run_reference(args, rank, world)
+        return
+    if args.workload == "scf":
+        run_scf_bench(args)
         return
     if args.kernel_case == "gemm_tc":
         from nonequilibriumgreensfunction_gb300 import capi
