@@ -206,6 +206,16 @@ NEGF_API int negf_calculate_observables(negf_handle* h, double dE, double f1, do
  * blocks of HopX (:150-156).  NEGF_ESTATE unless the handle was created with
  * calc_currents = 1 and negf_calculate_gnp ran for this energy.                         */
 NEGF_API int negf_calculate_currents(negf_handle* h, double* Jx, double* Jy, double* Jz);
+
+/* Energy- and orbital-resolved current densities of Calculate_Observables (erCD/orCD,
+ * Source/Calculate_Observables.F90:124-160, Source/Calculate_Gnp.F90:125-129) for the
+ * energy of the last negf_calculate_gnp call; any pointer may be NULL, values are added.
+ * ERJx/ERJy/ERJz/ERRhon: npx x npy x npz, the caller's column eCtr+1, unweighted
+ * (ERRhon = sum over orbitals of Re Gn(i,i) - Re Gp(i,i)).  ORJx/ORJy/ORJz: npx x npy x
+ * npz x norb^2 (pair ii*norb + jj), ORRhon: npx x npy x npz x norb, dE/(2 pi)-weighted.
+ * NEGF_ESTATE unless the handle has calc_currents = 1 and negf_calculate_gnp ran.       */
+NEGF_API int negf_calculate_resolved(negf_handle* h, double* ERJx, double* ERJy, double* ERJz, double* ERRhon,
+                                     double* ORJx, double* ORJy, double* ORJz, double* ORRhon);
 /* ---- batched interface -------------------------------------------------------------
  * Many energy points (and Hamiltonian slots, e.g. disorder seeds) in one device pass:
  * the GB300 replacement for the round-robin energy loop of Source/NEGF_Main.F90:21-27
@@ -244,6 +254,16 @@ typedef struct negf_batch_outputs {
     double* RhoN; double* RhoP;
     double* SigX; double* SigY; double* SigZ;
     double* Jx;   double* Jy;   double* Jz;
+    /* energy-resolved arrays (erCD, Source/Calculate_Observables.F90:124-157,
+     * Source/Calculate_Gnp.F90:125-127): npx x npy x npz x n, column n-1 for request n-1,
+     * UNweighted as the reference's ERJx(:,:,:,eCtr+1): the bond sums of dumVar and
+     * ERRhon = sum over orbitals of Re Gn(i,i) - Re Gp(i,i).  Need calc_currents.         */
+    double* ERJx; double* ERJy; double* ERJz; double* ERRhon;
+    /* orbital-resolved arrays (orCD, :127-160 and Calculate_Gnp.F90:128-129), summed over
+     * requests with the dE/(2 pi) weight: ORJx/y/z are npx x npy x npz x norb^2 x
+     * n_hamiltonians (pair index ii*norb + jj, ii on the bond's first site), ORRhon is
+     * npx x npy x npz x norb x n_hamiltonians.  Need calc_currents.                        */
+    double* ORJx; double* ORJy; double* ORJz; double* ORRhon;
     double* reserved[8];     /* must be NULL                                             */
 } negf_batch_outputs;
 NEGF_API int negf_solve_batch_ex(negf_handle* h, const negf_request* req, int32_t n, negf_result* res,

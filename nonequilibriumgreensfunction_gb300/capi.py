@@ -35,7 +35,7 @@ EXPORTED_SYMBOLS = (
     "negf_set_stream", "negf_profile", "negf_get_stats",
     "negf_set_hamiltonian", "negf_build_hamiltonian", "negf_contact_self_energy", "negf_get_retarded_greens",
     "negf_copy_g_columns", "negf_calculate_gnp", "negf_calculate_observables",
-    "negf_calculate_currents", "negf_solve_batch", "negf_solve_batch_ex",
+    "negf_calculate_currents", "negf_calculate_resolved", "negf_solve_batch", "negf_solve_batch_ex",
     "negf_zgemm", "negf_zinv", "negf_zgemm_noalloc", "negf_poisson_solve",
     "negf_server_create", "negf_server_submit", "negf_server_poll", "negf_server_wait",
     "negf_server_clock", "negf_server_destroy",
@@ -96,6 +96,8 @@ def wire_model_struct(model, shape):
 class NegfBatchOutputs(ctypes.Structure):
     _fields_ = [("RhoN", c_void_p), ("RhoP", c_void_p), ("SigX", c_void_p), ("SigY", c_void_p),
                 ("SigZ", c_void_p), ("Jx", c_void_p), ("Jy", c_void_p), ("Jz", c_void_p),
+                ("ERJx", c_void_p), ("ERJy", c_void_p), ("ERJz", c_void_p), ("ERRhon", c_void_p),
+                ("ORJx", c_void_p), ("ORJy", c_void_p), ("ORJz", c_void_p), ("ORRhon", c_void_p),
                 ("reserved", c_void_p * 8)]
 
 
@@ -157,6 +159,7 @@ def _declare(lib):
         "negf_calculate_observables": (c_int, [h, c_double, c_double, c_double, _dp, _dp, _dp, _dp,
                                                _dp, _dp, _dp, _dp]),
         "negf_calculate_currents": (c_int, [h, _dp, _dp, _dp]),
+        "negf_calculate_resolved": (c_int, [h, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp]),
         "negf_zgemm": (c_int, [c_int32, c_int32, c_int32, c_int32, _dp, _dp, c_int32, _dp, c_int32, _dp, _dp,
                                c_int32, c_int32]),
         "negf_zinv": (c_int, [c_int32, _dp, _dp, c_int32]),

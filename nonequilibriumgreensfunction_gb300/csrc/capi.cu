@@ -348,6 +348,39 @@ int negf_calculate_currents(negf_handle* h, double* Jx, double* Jy, double* Jz) 
   return NEGF_OK;
 }
 
+int negf_calculate_resolved(negf_handle* h, double* ERJx, double* ERJy, double* ERJz, double* ERRhon, double* ORJx,
+                            double* ORJy, double* ORJz, double* ORRhon) {
+  if (!h) return NEGF_EINVAL;
+  Engine& e = h->eng;
+  if (!e.currents_ || !e.dens_valid_) return NEGF_ESTATE;
+  NEGF_CUDA_TRY(cudaSetDevice(e.p_.device));
+  const bool er = ERJx || ERJy || ERJz || ERRhon, orb = ORJx || ORJy || ORJz || ORRhon;
+  if (!er && !orb) return NEGF_OK;
+  NEGF_TRY(e.ensure_resolved());
+  const long long total = e.nsite_total();
+  const int nq = e.n_or_fields(), no = e.p_.norb, no2 = no * no;
+  if (orb) NEGF_CUDA_TRY(cudaMemsetAsync(e.dOrAcc_, 0, sizeof(double) * nq * total, e.st_));
+  // the item of the last negf_calculate_gnp call is still in the handle's item list (slot 0)
+  NEGF_TRY(e.resolved(1, er, orb, 1));
+  std::vector<double> erh(er ? 4 * total : 0), orh(orb ? (size_t)nq * total : 0);
+  if (er) NEGF_CUDA_TRY(cudaMemcpyAsync(erh.data(), e.dEr_, sizeof(double) * erh.size(), cudaMemcpyDeviceToHost, e.st_));
+  if (orb)
+    NEGF_CUDA_TRY(cudaMemcpyAsync(orh.data(), e.dOrAcc_, sizeof(double) * orh.size(), cudaMemcpyDeviceToHost, e.st_));
+  NEGF_CUDA_TRY(cudaStreamSynchronize(e.st_));
+  double* ero[4] = {ERJx, ERJy, ERJz, ERRhon};
+  for (int f = 0; f < 4; ++f)
+    if (ero[f])
+      for (long long i = 0; i < total; ++i) ero[f][i] += erh[(size_t)f * total + i];
+  double* oro[3] = {ORJx, ORJy, ORJz};
+  for (int q = 0; q < nq; ++q) {
+    double* dst = q < 3 * no2 ? (oro[q / no2] ? oro[q / no2] + (size_t)(q % no2) * total : nullptr)
+                              : (ORRhon ? ORRhon + (size_t)(q - 3 * no2) * total : nullptr);
+    if (!dst) continue;
+    for (long long i = 0; i < total; ++i) dst[i] += orh[(size_t)q * total + i];
+  }
+  return NEGF_OK;
+}
+
 int negf_solve_batch(negf_handle* h, const negf_request* req, int32_t n, negf_result* res, double* RhoN, double* RhoP,
                      double* SigX, double* SigY, double* SigZ) {
   if (!h) return NEGF_EINVAL;
@@ -362,9 +395,13 @@ int negf_solve_batch_ex(negf_handle* h, const negf_request* req, int32_t n, negf
   if (out) {
     for (int i = 0; i < 8; ++i)
       if (out->reserved[i]) return NEGF_EINVAL;
-    if ((out->Jx || out->Jy || out->Jz) && !h->eng.currents_) return NEGF_ESTATE;
+    negf::ResolvedOut ro;
+    ro.er[0] = out->ERJx; ro.er[1] = out->ERJy; ro.er[2] = out->ERJz; ro.er[3] = out->ERRhon;
+    ro.orj[0] = out->ORJx; ro.orj[1] = out->ORJy; ro.orj[2] = out->ORJz; ro.orrho = out->ORRhon;
+    if ((out->Jx || out->Jy || out->Jz || ro.any_er() || ro.any_or()) && !h->eng.currents_) return NEGF_ESTATE;
     double* o[8] = {out->RhoN, out->RhoP, out->SigX, out->SigY, out->SigZ, out->Jx, out->Jy, out->Jz};
     for (int i = 0; i < 8; ++i) outs[i] = o[i];
+    return h->eng.batch_solve(req, n, res, outs, nullptr, &ro);
   }
   return h->eng.batch_solve(req, n, res, outs);
 }

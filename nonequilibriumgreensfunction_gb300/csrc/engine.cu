@@ -84,6 +84,7 @@ Engine::~Engine() {
   dfree(dP1_); dfree(dP2_); dfree(dCol1_); dfree(dColN_);
   dfree(dPx1_); dfree(dPy1_); dfree(dPz1_); dfree(dPx2_); dfree(dPy2_); dfree(dPz2_);
   if (currents_) { dfree(dYalt_); dfree(dCNalt_); }
+  dfree(dEr_); dfree(dOrAcc_);
   dfree(dSite_); dfree(dSums_); dfree(dTr_); dfree(dAcc_); dfree(dStatus_); dfree(dItems_);
   dfree(dSr_); dfree(dSrSigL_); dfree(dSrSigR_); dfree(dSrGamL_); dfree(dSrGamR_);
   dfree(dSrCmax_); dfree(dSrDos_); dfree(dSrActive_); dfree(dSrE_); dfree(dSrHend_); dfree(dSrStatus_);
@@ -733,6 +734,7 @@ int Engine::densities_impl(const std::vector<Item>& items, std::vector<double>& 
     c.sP = a.sP;
     c.q2_over_hbar = kQ * kQ / kHbar;
     c.site_out = dSite_;
+    c.P1 = dP1_; c.P2 = dP2_;
     NEGF_TRY(bond_currents(c, st_));
   }
   const size_t np = (size_t)B * sums_blocks_ * 2;
@@ -753,11 +755,41 @@ int Engine::densities_impl(const std::vector<Item>& items, std::vector<double>& 
   return NEGF_OK;
 }
 
+int Engine::ensure_resolved() {
+  if (!currents_) return NEGF_ESTATE;
+  const long long total = nsite_total();
+  if (!dEr_) NEGF_TRY(dalloc(&dEr_, (size_t)B_ * 4 * total, bytes_));
+  if (!dOrAcc_) NEGF_TRY(dalloc(&dOrAcc_, (size_t)p_.n_hamiltonians * n_or_fields() * total, bytes_));
+  return NEGF_OK;
+}
+
+int Engine::resolved(int batch, bool er, bool orb, int nslots) {
+  NEGF_TRY(ensure_resolved());
+  CurrentArgs c{};
+  c.n = M_; c.norb = p_.norb; c.npx = p_.npx; c.npy = p_.npy; c.npz = p_.npz; c.batch = batch; c.nf = nf_;
+  c.items = dItems_; c.Hall = dH_; c.Hop = dHop_;
+  c.Px1 = dPx1_; c.Py1 = dPy1_; c.Pz1 = dPz1_; c.Px2 = dPx2_; c.Py2 = dPy2_; c.Pz2 = dPz2_;
+  c.sP = (long long)p_.npx * M_ * p_.norb;
+  c.q2_over_hbar = kQ * kQ / kHbar;
+  c.site_out = dSite_;
+  c.P1 = dP1_; c.P2 = dP2_;
+  if (er) {
+    c.er_out = dEr_;
+    NEGF_TRY(bond_currents(c, st_));   // rewrites the J fields with the same values
+    c.er_out = nullptr;
+  }
+  if (orb) {
+    c.or_acc = dOrAcc_;
+    NEGF_TRY(orbital_resolved(c, nslots, st_));
+  }
+  return NEGF_OK;
+}
+
 // -------------------------------------------------------------------------------------
 // Batched solve
 // -------------------------------------------------------------------------------------
 int Engine::batch_solve(const negf_request* req, int n, negf_result* res, double* const* outs,
-                        double* site_items) {
+                        double* site_items, const ResolvedOut* ro) {
   if (n < 0 || (n > 0 && (!req || !res))) return NEGF_EINVAL;
   NEGF_CUDA_TRY(cudaSetDevice(p_.device));
   const long long total = nsite_total();
@@ -767,6 +799,13 @@ int Engine::batch_solve(const negf_request* req, int n, negf_result* res, double
     if (s < 0 || s >= nslots) return NEGF_EINVAL;
     if (!slot_set_[s]) return NEGF_ENOHAM;
   }
+  const bool want_er = ro && ro->any_er(), want_or = ro && ro->any_or();
+  if (want_er || want_or) {
+    NEGF_TRY(ensure_resolved());
+    if (want_or)
+      NEGF_CUDA_TRY(cudaMemsetAsync(dOrAcc_, 0, sizeof(double) * nslots * n_or_fields() * total, st_));
+  }
+  std::vector<double> er_host(want_er ? (size_t)B_ * 4 * total : 0);
   NEGF_CUDA_TRY(cudaMemsetAsync(dAcc_, 0, sizeof(double) * nslots * nf_ * total, st_));
   for (int c0 = 0; c0 < n; c0 += B_) {
     const int nb = std::min(B_, n - c0);
@@ -807,6 +846,10 @@ int Engine::batch_solve(const negf_request* req, int n, negf_result* res, double
     std::vector<double> ed, hd;
     NEGF_TRY(densities(items, ed, hd));
     NEGF_TRY(reduce_sites(nb, (int)total, nf_, nslots, dItems_, dSite_, dAcc_, st_));
+    if (want_er || want_or) NEGF_TRY(resolved(nb, want_er, want_or, nslots));
+    if (want_er)
+      NEGF_CUDA_TRY(cudaMemcpyAsync(er_host.data(), dEr_, sizeof(double) * 4 * total * nb, cudaMemcpyDeviceToHost,
+                                    st_));
     if (site_items)
       NEGF_CUDA_TRY(cudaMemcpyAsync(site_items + (size_t)c0 * nf_ * total, dSite_,
                                     sizeof(double) * nf_ * total * nb, cudaMemcpyDeviceToHost, st_));
@@ -830,6 +873,34 @@ int Engine::batch_solve(const negf_request* req, int n, negf_result* res, double
       o.status = stv;
       o.sr_iters = std::max(sr_iters[it.sr_l], sr_iters[S + it.sr_r]);
     }
+    if (want_er)   // request c0 + i -> column c0 + i of each energy-resolved array
+      for (int f = 0; f < 4; ++f) {
+        if (!ro->er[f]) continue;
+        for (int i = 0; i < nb; ++i) {
+          double* dst = ro->er[f] + (size_t)(c0 + i) * total;
+          const double* src = er_host.data() + ((size_t)i * 4 + f) * total;
+          for (long long k = 0; k < total; ++k) dst[k] += src[k];
+        }
+      }
+  }
+  if (want_or) {
+    const int nq = n_or_fields(), no2 = p_.norb * p_.norb;
+    std::vector<double> orh((size_t)nslots * nq * total);
+    NEGF_CUDA_TRY(cudaMemcpyAsync(orh.data(), dOrAcc_, sizeof(double) * orh.size(), cudaMemcpyDeviceToHost, st_));
+    NEGF_CUDA_TRY(cudaStreamSynchronize(st_));
+    for (int s = 0; s < nslots; ++s)
+      for (int q = 0; q < nq; ++q) {
+        double* dst;
+        if (q < 3 * no2) {
+          if (!ro->orj[q / no2]) continue;
+          dst = ro->orj[q / no2] + ((size_t)s * no2 + q % no2) * total;
+        } else {
+          if (!ro->orrho) continue;
+          dst = ro->orrho + ((size_t)s * p_.norb + (q - 3 * no2)) * total;
+        }
+        const double* src = orh.data() + ((size_t)s * nq + q) * total;
+        for (long long k = 0; k < total; ++k) dst[k] += src[k];
+      }
   }
   // add the slot-resolved site sums into the caller's arrays
   const size_t acc_n = (size_t)nslots * nf_ * total;

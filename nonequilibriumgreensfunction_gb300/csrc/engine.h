@@ -10,6 +10,16 @@
 
 namespace negf {
 
+// Energy- and orbital-resolved arrays of a batched solve (Source/Calculate_Observables.F90:
+// 124-160, Source/Calculate_Gnp.F90:125-129); every pointer may be null, values are added.
+struct ResolvedOut {
+  double* er[4] = {nullptr, nullptr, nullptr, nullptr};  // ERJx, ERJy, ERJz, ERRhon: nsite_total x n
+  double* orj[3] = {nullptr, nullptr, nullptr};          // ORJx/y/z: nsite_total x norb^2 x slots
+  double* orrho = nullptr;                               // ORRhon: nsite_total x norb x slots
+  bool any_er() const { return er[0] || er[1] || er[2] || er[3]; }
+  bool any_or() const { return orj[0] || orj[1] || orj[2] || orrho; }
+};
+
 struct SrJob {          // one Sancho-Rubio problem
   double energy;
   int slot;             // device end slice comes from this slot
@@ -34,9 +44,13 @@ class Engine {
 
   // outs[8] = RhoN, RhoP, SigX, SigY, SigZ, Jx, Jy, Jz (each may be null).  site_items
   // (optional): n x nf_ x nsite_total per-request dE-weighted site arrays, so a caller can
-  // sum energies in its own fixed order
+  // sum energies in its own fixed order.  ro (optional, needs calc_currents): the energy-
+  // and orbital-resolved arrays.
   int batch_solve(const negf_request* req, int n, negf_result* res, double* const* outs,
-                  double* site_items = nullptr);
+                  double* site_items = nullptr, const ResolvedOut* ro = nullptr);
+  // energy- and orbital-resolved outputs of the batch in dItems_ (after densities): er_out
+  // per item when `er`, or_acc += the batch's sums for slots 0..nslots-1 when `orb`
+  int resolved(int batch, bool er, bool orb, int nslots);
 
   // accessors used by the per-energy API
   int M() const { return M_; }
@@ -80,6 +94,12 @@ class Engine {
   double2 *dPx1_ = nullptr, *dPy1_ = nullptr, *dPz1_ = nullptr;
   double2 *dPx2_ = nullptr, *dPy2_ = nullptr, *dPz2_ = nullptr;
   double2 *dYalt_ = nullptr, *dCNalt_ = nullptr;
+  // energy/orbital-resolved outputs, allocated on first use: dEr_ [B_][4][nsite_total],
+  // dOrAcc_ [slots][3 norb^2 + norb][nsite_total]
+  double* dEr_ = nullptr;
+  double* dOrAcc_ = nullptr;
+  int ensure_resolved();
+  int n_or_fields() const { return 3 * p_.norb * p_.norb + p_.norb; }
   double* dSite_ = nullptr;
   double* dSums_ = nullptr;
   double* dTr_ = nullptr;

@@ -275,8 +275,17 @@ struct CurrentArgs {
   long long sP;
   double q2_over_hbar;
   double* site_out;
+  // energy- and orbital-resolved outputs (optional): er_out [item][4][npx*npy*npz] =
+  // unweighted (ERJx, ERJy, ERJz, ERRhon); or_acc [slot][3 norb^2 + norb][npx*npy*npz] =
+  // dE/(2 pi)-weighted (ORJx, ORJy, ORJz pairs ii*norb + jj, then ORRhon per orbital).
+  // Both read the diagonal site blocks P1, P2 ([item][x][n][norb]).
+  const double2 *P1 = nullptr, *P2 = nullptr;
+  double* er_out = nullptr;
+  double* or_acc = nullptr;
 };
 int bond_currents(const CurrentArgs& a, cudaStream_t st);
+// or_acc[slot] += this batch's orbital-resolved sums for slots 0..nslots-1
+int orbital_resolved(const CurrentArgs& a, int nslots, cudaStream_t st);
 
 // acc[slot][f][i] += sum over items b with items[b].slot == slot (in order) of
 // site_out[b][f][i], f < nf

@@ -488,6 +488,44 @@ __global__ void density_spin_kernel(DensityArgs a) {
 // and J += dumVar dE/(2 pi) in REAL(8), as the reference's dumVar (:7) is REAL(4).  The x
 // bond couples the same site of slices x and x+1 through HopX(a,a) and its conjugate
 // (:150-156).  Writes site_out fields 5, 6, 7 = Jx, Jy, Jz.
+// dumVar of one orbital pair: the two lead blocks of P at (a_i, b_j) and H(a_i, b_j),
+// H(b_j, a_i), rounded to REAL(4)
+__device__ __forceinline__ float bond_dum(double2 p1, double2 p2, double2 hab, double2 hba, double f1, double f2,
+                                          double pref) {
+  const double2 gn = make_double2(f1 * p1.x + f2 * p2.x, f1 * p1.y + f2 * p2.y);
+  const double2 gp = make_double2((1.0 - f1) * p1.x + (1.0 - f2) * p2.x, (1.0 - f1) * p1.y + (1.0 - f2) * p2.y);
+  double2 v = csub(cmul(hab, cconj(gn)), cmul(gn, hba));
+  v = csub(v, cmul(hab, cconj(gp)));
+  v = cadd(v, cmul(gp, hba));
+  return __double2float_rn(-pref * v.y);   // Re(i c v) = -c Im v
+}
+
+// bond d (0: +x, 1: +y, 2: +z) leaving site (x, y, z) stays inside the grid
+__device__ __forceinline__ bool bond_inside(const CurrentArgs& a, int d, int x, int y, int z) {
+  return d == 0 ? x < a.npx - 1 : (d == 1 ? y < a.npy - 1 : z < a.npz - 1);
+}
+
+// operands of orbital pair (ii, jj) of an inside bond d leaving site s = y + z npy of slice
+// x; H is the slice's Htotd block, prow the item's site-block row of (x, s)
+__device__ __forceinline__ void bond_pair(const CurrentArgs& a, const double2* H, long long prow, int d, int s, int ii,
+                                          int jj, double2& p1, double2& p2, double2& hab, double2& hba) {
+  const int no = a.norb;
+  const long long n = a.n;
+  const long long q = prow + ii * no + jj;
+  if (d == 0) {
+    const long long ri = (long long)s * no + ii, rj = (long long)s * no + jj;
+    const double2 hx = a.Hop[rj * n + ri];
+    p1 = a.Px1[q]; p2 = a.Px2[q]; hab = hx; hba = cconj(hx);
+    return;
+  }
+  const long long nb = d == 1 ? s + 1 : s + a.npy;
+  const long long ra = (long long)s * no + ii, rb = nb * no + jj;
+  p1 = (d == 1 ? a.Py1 : a.Pz1)[q];
+  p2 = (d == 1 ? a.Py2 : a.Pz2)[q];
+  hab = H[rb * n + ra];
+  hba = H[ra * n + rb];
+}
+
 __global__ void bond_currents_kernel(CurrentArgs a) {
   const int b = blockIdx.y;
   const int nsite = a.npy * a.npz;
@@ -497,42 +535,21 @@ __global__ void bond_currents_kernel(CurrentArgs a) {
   const int no = a.norb;
   const Item it = a.items[b];
   const double w = it.dE / (2.0 * 3.14159265358979323846);
-  const double pref = a.q2_over_hbar;
   const int x = idx / nsite, s = idx % nsite;
   const int y = s % a.npy, z = s / a.npy;
   const long long n = a.n;
   const double2* H = a.Hall + ((long long)it.slot * a.npx + x) * n * n;
   const long long prow = (long long)b * a.sP + ((long long)x * n + (long long)s * no) * no;
-  const double f1 = it.f1, f2 = it.f2;
-  // one bond term given the two lead blocks of P(a_i, b_j) and H(a_i, b_j), H(b_j, a_i)
-  auto term = [&](double2 p1, double2 p2, double2 hab, double2 hba) -> double {
-    const double2 gn = make_double2(f1 * p1.x + f2 * p2.x, f1 * p1.y + f2 * p2.y);
-    const double2 gp = make_double2((1.0 - f1) * p1.x + (1.0 - f2) * p2.x, (1.0 - f1) * p1.y + (1.0 - f2) * p2.y);
-    double2 v = csub(cmul(hab, cconj(gn)), cmul(gn, hba));
-    v = csub(v, cmul(hab, cconj(gp)));
-    v = cadd(v, cmul(gp, hba));
-    const float dum = __double2float_rn(-pref * v.y);   // Re(i c v) = -c Im v
-    return (double)dum * w;
-  };
-  double j[3] = {0.0, 0.0, 0.0};
-  if (x < a.npx - 1) {
-    const double2* hop = a.Hop;
+  double j[3] = {0.0, 0.0, 0.0}, ju[3] = {0.0, 0.0, 0.0};
+  for (int d = 0; d < 3; ++d) {
+    if (!bond_inside(a, d, x, y, z)) continue;
     for (int ii = 0; ii < no; ++ii)
       for (int jj = 0; jj < no; ++jj) {
-        const long long ri = (long long)s * no + ii, rj = (long long)s * no + jj;
-        const double2 hx = hop[rj * n + ri];
-        j[0] += term(a.Px1[prow + ii * no + jj], a.Px2[prow + ii * no + jj], hx, cconj(hx));
-      }
-  }
-  const double2* pb1[2] = {a.Py1, a.Pz1};
-  const double2* pb2[2] = {a.Py2, a.Pz2};
-  const int nb_site[2] = {y < a.npy - 1 ? s + 1 : -1, z < a.npz - 1 ? s + a.npy : -1};
-  for (int d = 0; d < 2; ++d) {
-    if (nb_site[d] < 0) continue;
-    for (int ii = 0; ii < no; ++ii)
-      for (int jj = 0; jj < no; ++jj) {
-        const long long ra = (long long)s * no + ii, rb = (long long)nb_site[d] * no + jj;
-        j[1 + d] += term(pb1[d][prow + ii * no + jj], pb2[d][prow + ii * no + jj], H[rb * n + ra], H[ra * n + rb]);
+        double2 p1, p2, hab, hba;
+        bond_pair(a, H, prow, d, s, ii, jj, p1, p2, hab, hba);
+        const double dum = (double)bond_dum(p1, p2, hab, hba, it.f1, it.f2, a.q2_over_hbar);
+        j[d] += dum * w;
+        ju[d] += dum;
       }
   }
   const long long o = (long long)x + (long long)a.npx * (y + (long long)a.npy * z);
@@ -540,6 +557,67 @@ __global__ void bond_currents_kernel(CurrentArgs a) {
   so[5LL * total + o] = j[0];
   so[6LL * total + o] = j[1];
   so[7LL * total + o] = j[2];
+  if (a.er_out) {
+    // energy-resolved fields (Calculate_Observables.F90:124-157, Calculate_Gnp.F90:125-127):
+    // the unweighted bond sums and sum over orbitals of Re Gn(i,i) - Re Gp(i,i)
+    double rho = 0.0;
+    for (int ii = 0; ii < no; ++ii) {
+      const double2 q1 = a.P1[prow + ii * no + ii], q2 = a.P2[prow + ii * no + ii];
+      rho += (it.f1 * q1.x + it.f2 * q2.x) - ((1.0 - it.f1) * q1.x + (1.0 - it.f2) * q2.x);
+    }
+    double* eo = a.er_out + (long long)b * 4 * total;
+    eo[o] = ju[0];
+    eo[total + o] = ju[1];
+    eo[2LL * total + o] = ju[2];
+    eo[3LL * total + o] = rho;
+  }
+}
+
+// Orbital-resolved bond currents and densities (ORJx/y/z of Calculate_Observables.F90:127-160,
+// ORRhon of Calculate_Gnp.F90:127-129), summed over the items of each slot in item order.
+// One thread per (slot, site, q): q < 3 norb^2 is orbital pair (ii, jj), ii*norb + jj =
+// q % norb^2, of bond direction q / norb^2 (x, y, z); q >= 3 norb^2 is orbital q - 3 norb^2
+// of the density.  or_acc[slot][q][site] += sum_b dE_b/(2 pi) value_b, q fastest across
+// threads so that a warp reads whole site blocks.
+__global__ void orbital_resolved_kernel(CurrentArgs a) {
+  const int no = a.norb, nq = 3 * no * no + no;
+  const int nsite = a.npy * a.npz;
+  const int total = a.npx * nsite;
+  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= (long long)total * nq) return;
+  const int slot = blockIdx.y;
+  const int q = (int)(idx % nq);
+  const int site = (int)(idx / nq);
+  const int x = site / nsite, s = site % nsite;
+  const int y = s % a.npy, z = s / a.npy;
+  const long long n = a.n;
+  double acc = 0.0;
+  if (q < 3 * no * no) {
+    const int d = q / (no * no), ii = (q % (no * no)) / no, jj = q % no;
+    if (bond_inside(a, d, x, y, z)) {
+      for (int b = 0; b < a.batch; ++b) {
+        const Item it = a.items[b];
+        if (it.slot != slot) continue;
+        const double w = it.dE / (2.0 * 3.14159265358979323846);
+        const double2* H = a.Hall + ((long long)it.slot * a.npx + x) * n * n;
+        const long long prow = (long long)b * a.sP + ((long long)x * n + (long long)s * no) * no;
+        double2 p1, p2, hab, hba;
+        bond_pair(a, H, prow, d, s, ii, jj, p1, p2, hab, hba);
+        acc += (double)bond_dum(p1, p2, hab, hba, it.f1, it.f2, a.q2_over_hbar) * w;
+      }
+    }
+  } else {
+    const int ii = q - 3 * no * no;
+    for (int b = 0; b < a.batch; ++b) {
+      const Item it = a.items[b];
+      if (it.slot != slot) continue;
+      const double w = it.dE / (2.0 * 3.14159265358979323846);
+      const long long pd = (long long)b * a.sP + ((long long)x * n + (long long)s * no) * no + ii * no + ii;
+      acc += (it.f1 * a.P1[pd].x + it.f2 * a.P2[pd].x) * w;
+    }
+  }
+  const long long o = (long long)x + (long long)a.npx * (y + (long long)a.npy * z);
+  a.or_acc[((long long)slot * nq + q) * total + o] += acc;
 }
 
 __global__ void reduce_sites_kernel(int batch, int total, int nf, int nslots, const Item* items,
@@ -605,6 +683,16 @@ int bond_currents(const CurrentArgs& a, cudaStream_t st) {
   const int total = a.npx * a.npy * a.npz;
   dim3 grid((total + 127) / 128, a.batch);
   bond_currents_kernel<<<grid, 128, 0, st>>>(a);
+  NEGF_CUDA_TRY(cudaGetLastError());
+  count_launch();
+  return NEGF_OK;
+}
+
+int orbital_resolved(const CurrentArgs& a, int nslots, cudaStream_t st) {
+  if (a.norb > 4 || !a.or_acc || nslots < 1) return NEGF_EINVAL;
+  const long long work = (long long)a.npx * a.npy * a.npz * (3 * a.norb * a.norb + a.norb);
+  dim3 grid((unsigned)((work + 255) / 256), nslots);
+  orbital_resolved_kernel<<<grid, 256, 0, st>>>(a);
   NEGF_CUDA_TRY(cudaGetLastError());
   count_launch();
   return NEGF_OK;

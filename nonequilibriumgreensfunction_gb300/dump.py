@@ -58,8 +58,9 @@ def _site_loop(npx, npy, npz):
 
 def write_reference_files(outdir: str, rec: dict) -> list:
     """Write scalars.txt, Greens.txt, Transmissions.txt and, when present in the record,
-    Poissons.txt (Phi, ro) and SigExp.txt (SigX/Y/Z), in Dump_Data's order.  Returns the
-    paths written."""
+    Poissons.txt (Phi, ro), ERCD.txt (ERJx/y/z, ERRhon: (npx, npy, npz, n_e)), ORCD.txt
+    (ORJx/y/z: (npx, npy, npz, norb**2), ORRhon: (npx, npy, npz, norb)) and SigExp.txt
+    (SigX/Y/Z), in Dump_Data's order.  Returns the paths written."""
     os.makedirs(outdir, exist_ok=True)
     npx, npy, npz = int(rec["npx"]), int(rec["npy"]), int(rec["npz"])
     out = []
@@ -116,6 +117,22 @@ def write_reference_files(outdir: str, rec: dict) -> list:
         for x, y, z in _site_loop(npx, npy, npz):
             p += [es11_4(rec["Phi"][x, y, z]), es11_4(rec["ro"][x, y, z])]
         put("Poissons.txt", p)
+    if rec.get("ERJx") is not None:          # ERCD.txt (:100-114): per site, per energy
+        er = [rec[k] for k in ("ERJx", "ERJy", "ERJz", "ERRhon")]
+        lines = []
+        for x, y, z in _site_loop(npx, npy, npz):
+            for i in range(n_e):
+                lines += [es11_4(a[x, y, z, i]) for a in er]
+        put("ERCD.txt", lines)
+    if rec.get("ORJx") is not None:          # ORCD.txt (:116-132): pairs, then orbitals
+        norb = int(rec["norb"])
+        oj = [rec[k] for k in ("ORJx", "ORJy", "ORJz")]
+        lines = []
+        for x, y, z in _site_loop(npx, npy, npz):
+            for q in range(norb * norb):
+                lines += [es11_4(a[x, y, z, q]) for a in oj]
+            lines += [es11_4(rec["ORRhon"][x, y, z, o]) for o in range(norb)]
+        put("ORCD.txt", lines)
     if rec.get("SigX") is not None:          # SigExp.txt (:134-146)
         sp = []
         for x, y, z in _site_loop(npx, npy, npz):
@@ -187,6 +204,19 @@ def read_reference_files(outdir: str) -> dict:
     pp = os.path.join(outdir, "Poissons.txt")
     if os.path.exists(pp):
         rec["Phi"], rec["ro"] = sites(_load(pp), 2)
+    ep = os.path.join(outdir, "ERCD.txt")
+    if os.path.exists(ep):
+        a = _load(ep).reshape(npx, npy, npz, n_e, 4)
+        for f, k in enumerate(("ERJx", "ERJy", "ERJz", "ERRhon")):
+            rec[k] = a[..., f].copy()
+    op = os.path.join(outdir, "ORCD.txt")
+    if os.path.exists(op):
+        no = rec["norb"]
+        a = _load(op).reshape(npx, npy, npz, 3 * no * no + no)
+        pairs = a[..., :3 * no * no].reshape(npx, npy, npz, no * no, 3)
+        for f, k in enumerate(("ORJx", "ORJy", "ORJz")):
+            rec[k] = pairs[..., f].copy()
+        rec["ORRhon"] = a[..., 3 * no * no:].copy()
     sp = os.path.join(outdir, "SigExp.txt")
     if os.path.exists(sp):
         rec["SigX"], rec["SigY"], rec["SigZ"] = sites(_load(sp), 3)
@@ -204,11 +234,14 @@ def read_npz(path: str) -> dict:
 
 
 def record_from_sweep(npx, npy, npz, energies, dE, mu, mu_t, out, rho_n, rho_p, f1=None, f2=None,
-                      spin=None, currents=None, flux=0.0, disorder=0.0, norb=4, phi=None, ro=None):
+                      spin=None, currents=None, flux=0.0, disorder=0.0, norb=4, phi=None, ro=None,
+                      er=None, orb=None):
     """Assemble a record from a batched solve of one Hamiltonian slot: ``out`` is the dict
     Solver.solve_batch returns for ``energies`` (in order), rho_n/rho_p/spin/currents the
-    slot's (npx, npy, npz) sums.  With the per-energy occupations f1, f2, ContactCurrent is
-    the sum over energies of Calculate_Observables.F90:102-103 (zero without them)."""
+    slot's (npx, npy, npz) sums, er = (ERJx, ERJy, ERJz, ERRhon) the (npx, npy, npz, n_e)
+    energy-resolved arrays and orb = (ORJx, ORJy, ORJz, ORRhon) the slot's orbital-resolved
+    ones.  With the per-energy occupations f1, f2, ContactCurrent is the sum over energies
+    of Calculate_Observables.F90:102-103 (zero without them)."""
     energies = np.asarray(energies, dtype=np.float64)
     de = np.broadcast_to(np.asarray(dE, dtype=np.float64), energies.shape)
     contact_current = np.zeros(2)
@@ -231,4 +264,8 @@ def record_from_sweep(npx, npy, npz, energies, dE, mu, mu_t, out, rho_n, rho_p, 
         rec["SigX"], rec["SigY"], rec["SigZ"] = spin
     if phi is not None:
         rec["Phi"], rec["ro"] = phi, ro
+    if er is not None:
+        rec["ERJx"], rec["ERJy"], rec["ERJz"], rec["ERRhon"] = er
+    if orb is not None:
+        rec["ORJx"], rec["ORJy"], rec["ORJz"], rec["ORRhon"] = orb
     return rec

@@ -65,18 +65,26 @@ MODULE negf_gpu_shim
             REAL(C_DOUBLE), VALUE :: f1, f2, de
             REAL(C_DOUBLE)        :: rhon(*), rhop(*)
         END FUNCTION
+        ! an absent OPTIONAL dummy of a BIND(C) interface is passed as a null pointer
+        ! (Fortran 2018, 18.3.6), which is what the C entry points take for "not wanted"
         INTEGER(C_INT) FUNCTION negf_calculate_observables(h, de, f1, f2, t12, eden, hden, modes, cc, sx, sy, sz) &
                 BIND(C, NAME="negf_calculate_observables")
             IMPORT :: C_INT, C_PTR, C_DOUBLE
             TYPE(C_PTR), VALUE    :: h
             REAL(C_DOUBLE), VALUE :: de, f1, f2
             REAL(C_DOUBLE)        :: t12, eden, hden, modes(2), cc(2)
-            TYPE(C_PTR), VALUE    :: sx, sy, sz
+            REAL(C_DOUBLE), OPTIONAL :: sx(*), sy(*), sz(*)
         END FUNCTION
         INTEGER(C_INT) FUNCTION negf_calculate_currents(h, jx, jy, jz) BIND(C, NAME="negf_calculate_currents")
             IMPORT :: C_INT, C_PTR, C_DOUBLE
             TYPE(C_PTR), VALUE    :: h
             REAL(C_DOUBLE)        :: jx(*), jy(*), jz(*)
+        END FUNCTION
+        INTEGER(C_INT) FUNCTION negf_calculate_resolved(h, erjx, erjy, erjz, errhon, orjx, orjy, orjz, orrhon) &
+                BIND(C, NAME="negf_calculate_resolved")
+            IMPORT :: C_INT, C_PTR, C_DOUBLE
+            TYPE(C_PTR), VALUE    :: h
+            REAL(C_DOUBLE), OPTIONAL :: erjx(*), erjy(*), erjz(*), errhon(*), orjx(*), orjy(*), orjz(*), orrhon(*)
         END FUNCTION
     END INTERFACE
 
@@ -147,6 +155,15 @@ SUBROUTINE Calculate_Gnp
     INTEGER(C_INT) :: st
     st = negf_calculate_gnp(negf_h, f1, f2, deltaE, RhoN, RhoP)
     CALL negf_shim_check(st, "Calculate_Gnp")
+    ! energy- and orbital-resolved densities (Source/Calculate_Gnp.F90:125-129)
+    IF (erCD == 1) THEN
+        st = negf_calculate_resolved(negf_h, errhon=ERRhon(:, :, :, eCtr+1))
+        CALL negf_shim_check(st, "Calculate_Gnp (ERRhon)")
+    ENDIF
+    IF (orCD == 1) THEN
+        st = negf_calculate_resolved(negf_h, orrhon=ORRhon)
+        CALL negf_shim_check(st, "Calculate_Gnp (ORRhon)")
+    ENDIF
 END SUBROUTINE Calculate_Gnp
 
 
@@ -156,12 +173,12 @@ SUBROUTINE Calculate_Observables
     IMPLICIT NONE
     INTEGER(C_INT) :: st
     REAL(C_DOUBLE) :: t, ed, hd, modes(2)
-    TYPE(C_PTR)    :: sx, sy, sz
-    sx = C_NULL_PTR; sy = C_NULL_PTR; sz = C_NULL_PTR
     IF (calcSigExp == 1) THEN
-        sx = C_LOC(SigXExp); sy = C_LOC(SigYExp); sz = C_LOC(SigZExp)
+        st = negf_calculate_observables(negf_h, deltaE, f1, f2, t, ed, hd, modes, ContactCurrent, &
+                                        SigXExp, SigYExp, SigZExp)
+    ELSE
+        st = negf_calculate_observables(negf_h, deltaE, f1, f2, t, ed, hd, modes, ContactCurrent)
     ENDIF
-    st = negf_calculate_observables(negf_h, deltaE, f1, f2, t, ed, hd, modes, ContactCurrent, sx, sy, sz)
     CALL negf_shim_check(st, "Calculate_Observables")
     T12(eCtr+1) = T12(eCtr+1) + t
     EDensity(eCtr+1) = EDensity(eCtr+1) + ed
@@ -171,4 +188,15 @@ SUBROUTINE Calculate_Observables
     ! bond currents (Source/Calculate_Observables.F90:110-169)
     st = negf_calculate_currents(negf_h, Jx, Jy, Jz)
     CALL negf_shim_check(st, "Calculate_Observables (currents)")
+    ! energy- and orbital-resolved current densities (:124-160); ERJx(:,:,:,eCtr+1) is
+    ! contiguous, so the library adds into the caller's column in place
+    IF (erCD == 1) THEN
+        st = negf_calculate_resolved(negf_h, erjx=ERJx(:, :, :, eCtr+1), erjy=ERJy(:, :, :, eCtr+1), &
+                                     erjz=ERJz(:, :, :, eCtr+1))
+        CALL negf_shim_check(st, "Calculate_Observables (ERCD)")
+    ENDIF
+    IF (orCD == 1) THEN
+        st = negf_calculate_resolved(negf_h, orjx=ORJx, orjy=ORJy, orjz=ORJz)
+        CALL negf_shim_check(st, "Calculate_Observables (ORCD)")
+    ENDIF
 END SUBROUTINE Calculate_Observables

@@ -202,6 +202,19 @@ class Solver:
                 raise ValueError("site arrays must be Fortran-ordered float64")
         check(self.lib.negf_calculate_currents(self._h, _ptr(jx), _ptr(jy), _ptr(jz)), "negf_calculate_currents")
 
+    def calculate_resolved(self, er=None, orb=None):
+        """Energy- and orbital-resolved current densities (erCD/orCD,
+        Calculate_Observables.F90:124-160, Calculate_Gnp.F90:125-129) of the energy of the
+        last calculate_gnp call.  ``er`` = (ERJx, ERJy, ERJz, ERRhon), (npx, npy, npz) arrays
+        the unweighted values are added to; ``orb`` = (ORJx, ORJy, ORJz) of shape (npx, npy,
+        npz, norb**2) and ORRhon of shape (npx, npy, npz, norb), dE/(2 pi)-weighted.  All
+        Fortran-ordered float64; None entries are skipped."""
+        arrs = tuple(er if er is not None else (None,) * 4) + tuple(orb if orb is not None else (None,) * 4)
+        for a in arrs:
+            if a is not None and not (a.flags.f_contiguous and a.dtype == np.float64):
+                raise ValueError("site arrays must be Fortran-ordered float64")
+        check(self.lib.negf_calculate_resolved(self._h, *(_ptr(a) for a in arrs)), "negf_calculate_resolved")
+
     def energy_sweep(self, energy, f1, f2, dE, rho_n=None, rho_p=None, contact_current=None, spin=None,
                      currents=None):
         """Energy_Sweep.F90:28-46 for one energy; returns the per-energy observables."""
@@ -215,13 +228,18 @@ class Solver:
         return obs
 
     # -- batched ---------------------------------------------------------------------
-    def solve_batch(self, energies, f1, f2, dE, slots=None, rho_n=None, rho_p=None, spin=None, currents=None):
+    def solve_batch(self, energies, f1, f2, dE, slots=None, rho_n=None, rho_p=None, spin=None, currents=None,
+                    er=None, orb=None):
         """Solve len(energies) energy points (chunked by max_batch on the device).
 
         ``rho_n``/``rho_p``/``spin``/``currents`` (if given) are (npx, npy, npz,
         n_hamiltonians) Fortran-ordered arrays the dE-weighted densities, spin densities
-        (SigX, SigY, SigZ) and bond currents (Jx, Jy, Jz) are added to.
-        Returns a dict of per-request arrays."""
+        (SigX, SigY, SigZ) and bond currents (Jx, Jy, Jz) are added to.  ``er`` =
+        (ERJx, ERJy, ERJz, ERRhon), each (npx, npy, npz, n): the unweighted energy-resolved
+        values of request i are added to [..., i].  ``orb`` = (ORJx, ORJy, ORJz) of shape
+        (npx, npy, npz, norb**2, n_hamiltonians) and ORRhon (npx, npy, npz, norb,
+        n_hamiltonians): the dE-weighted orbital-resolved sums.  Returns a dict of
+        per-request arrays."""
         energies = np.asarray(energies, dtype=np.float64)
         n = energies.size
         f1 = np.broadcast_to(np.asarray(f1, dtype=np.float64), (n,))
@@ -237,14 +255,16 @@ class Solver:
         sx = sy = sz = None
         if spin is not None:
             sx, sy, sz = spin
-        if currents is None:
+        if currents is None and er is None and orb is None:
             rc = self.lib.negf_solve_batch(self._h, req, n, res, _ptr(rho_n), _ptr(rho_p), _ptr(sx), _ptr(sy),
                                            _ptr(sz))
             check(rc, "negf_solve_batch")
         else:
             outs = capi.NegfBatchOutputs()
-            for name, a in zip(("RhoN", "RhoP", "SigX", "SigY", "SigZ", "Jx", "Jy", "Jz"),
-                               (rho_n, rho_p, sx, sy, sz) + tuple(currents)):
+            arrs = ((rho_n, rho_p, sx, sy, sz) + tuple(currents if currents is not None else (None,) * 3)
+                    + tuple(er if er is not None else (None,) * 4) + tuple(orb if orb is not None else (None,) * 4))
+            for name, a in zip(("RhoN", "RhoP", "SigX", "SigY", "SigZ", "Jx", "Jy", "Jz",
+                                "ERJx", "ERJy", "ERJz", "ERRhon", "ORJx", "ORJy", "ORJz", "ORRhon"), arrs):
                 if a is not None and not (a.flags.f_contiguous and a.dtype == np.float64):
                     raise ValueError("site arrays must be Fortran-ordered float64")
                 setattr(outs, name, None if a is None else a.ctypes.data)

@@ -334,7 +334,7 @@ def site_density(gd, npy, npz, norb=4):
 # Calculate_Observables, Source/Calculate_Observables.F90:2-169 (non-BdG branch)
 # ---------------------------------------------------------------------------
 def calculate_observables(gnp, grrgt, gam_l, gam_r, htotd, hopx, f1, f2, de, npy, npz,
-                          calc_spin=False, calc_currents=True, norb=4):
+                          calc_spin=False, calc_currents=True, norb=4, calc_resolved=False):
     npx = htotd.shape[0]
     nn = npy * norb
     res = {}
@@ -365,9 +365,9 @@ def calculate_observables(gnp, grrgt, gam_l, gam_r, htotd, hopx, f1, f2, de, npy
     res["ContactCurrent"] = np.array([Q_E * de / H_PLANCK * (t12 * (f2 - f1)),
                                       Q_E * de / H_PLANCK * (t12 * (f1 - f2))])  # :102-103
     if calc_currents and "Gnu" in gnp:                      # :110-169, dumVar is REAL(4)
-        jx = np.zeros((npx, npy, npz))
-        jy = np.zeros((npx, npy, npz))
-        jz = np.zeros((npx, npy, npz))
+        j = np.zeros((3, npx, npy, npz))                    # Jx, Jy, Jz
+        er = np.zeros((3, npx, npy, npz))                   # ERJx/y/z at this energy (:124-157)
+        orj = np.zeros((3, npx, npy, npz, norb * norb))     # ORJx/y/z, pair (ii-1)*Norb+jj (:127-160)
         gnu, gnl, gpu_, gpl = gnp["Gnu"], gnp["Gnl"], gnp["Gpu"], gnp["Gpl"]
         pref = 1j * Q_E * Q_E / HBAR
         w = de / (2.0 * PI)
@@ -377,30 +377,46 @@ def calculate_observables(gnp, grrgt, gam_l, gam_r, htotd, hopx, f1, f2, de, npy
                 for zz in range(npz):
                     idx = yy * norb + zz * nn
                     a = slice(idx, idx + norb)
+                    terms = [None, None, None]
                     if yy < npy - 1:
                         b = slice(idx + norb, idx + 2 * norb)
-                        v = (h[a, b] * gnd[xx][b, a].T - gnd[xx][a, b] * h[b, a].T
-                             - h[a, b] * gpd[xx][b, a].T + gpd[xx][a, b] * h[b, a].T)
-                        jy[xx, yy, zz] = np.sum(np.float32(np.real(pref * v)).astype(np.float64) * w)
+                        terms[1] = (h[a, b] * gnd[xx][b, a].T - gnd[xx][a, b] * h[b, a].T
+                                    - h[a, b] * gpd[xx][b, a].T + gpd[xx][a, b] * h[b, a].T)
                     if zz < npz - 1:
                         b = slice(idx + nn, idx + nn + norb)
-                        v = (h[a, b] * gnd[xx][b, a].T - gnd[xx][a, b] * h[b, a].T
-                             - h[a, b] * gpd[xx][b, a].T + gpd[xx][a, b] * h[b, a].T)
-                        jz[xx, yy, zz] = np.sum(np.float32(np.real(pref * v)).astype(np.float64) * w)
+                        terms[2] = (h[a, b] * gnd[xx][b, a].T - gnd[xx][a, b] * h[b, a].T
+                                    - h[a, b] * gpd[xx][b, a].T + gpd[xx][a, b] * h[b, a].T)
                     if xx < npx - 1:
                         hx = hopx[a, a]
-                        v = (hx * gnl[xx][a, a].T - gnu[xx][a, a] * np.conj(hx)
-                             - hx * gpl[xx][a, a].T + gpu_[xx][a, a] * np.conj(hx))
-                        jx[xx, yy, zz] = np.sum(np.float32(np.real(pref * v)).astype(np.float64) * w)
-        res["Jx"], res["Jy"], res["Jz"] = jx, jy, jz
+                        terms[0] = (hx * gnl[xx][a, a].T - gnu[xx][a, a] * np.conj(hx)
+                                    - hx * gpl[xx][a, a].T + gpu_[xx][a, a] * np.conj(hx))
+                    for d, v in enumerate(terms):
+                        if v is None:
+                            continue
+                        dum = np.float32(np.real(pref * v)).astype(np.float64)   # [ii, jj]
+                        j[d, xx, yy, zz] = np.sum(dum * w)
+                        er[d, xx, yy, zz] = np.sum(dum)
+                        orj[d, xx, yy, zz] = (dum * w).ravel()
+        res["Jx"], res["Jy"], res["Jz"] = j
+        if calc_resolved:
+            res["ERJx"], res["ERJy"], res["ERJz"] = er
+            res["ORJx"], res["ORJy"], res["ORJz"] = orj
     return res
+
+
+def orbital_density(gd, npy, npz, norb=4):
+    """Re diag(G?d) per orbital of each site -> (npx, npy, npz, norb) (ORRhon before its
+    dE/(2 pi) weight, Calculate_Gnp.F90:128-129)."""
+    npx = gd.shape[0]
+    diag = np.real(np.diagonal(gd, axis1=1, axis2=2))       # (npx, M)
+    return diag.reshape(npx, npz, npy, norb).transpose(0, 2, 1, 3)
 
 
 # ---------------------------------------------------------------------------
 # Energy_Sweep, Source/Energy_Sweep.F90:1-46
 # ---------------------------------------------------------------------------
 def energy_sweep(htotd, hopx, energy, mu_lead, de, npy, npz, opt: SolveOptions,
-                 calc_currents=False, keep_blocks=False):
+                 calc_currents=False, keep_blocks=False, calc_resolved=False):
     """One energy point.  ``mu_lead`` = (muT - mu(1), muT - mu(2)), the lead
     electrochemical potentials.  Returns a dict of per-energy results, with RhoN/RhoP
     and spin already weighted by dE/(2 pi) as the reference accumulates them."""
@@ -421,8 +437,13 @@ def energy_sweep(htotd, hopx, energy, mu_lead, de, npy, npz, opt: SolveOptions,
     out["RhoP"] = site_density(gnp["Gpd"], npy, npz, opt.norb) * (de / (2.0 * PI))
     obs = calculate_observables(gnp, rg["GRRgt"], cse["GammaL"], cse["GammaR"], htotd, hopx,
                                 f1, f2, de, npy, npz, calc_spin=opt.calc_spin,
-                                calc_currents=calc_currents, norb=opt.norb)
+                                calc_currents=calc_currents, norb=opt.norb, calc_resolved=calc_resolved)
     out.update(obs)
+    if calc_resolved:                                           # Calculate_Gnp.F90:125-129
+        on = orbital_density(gnp["Gnd"], npy, npz, opt.norb)
+        op = orbital_density(gnp["Gpd"], npy, npz, opt.norb)
+        out["ERRhon"] = (on - op).sum(axis=3)
+        out["ORRhon"] = on * (de / (2.0 * PI))
     if keep_blocks:
         out.update(cse)
         out.update(rg)

@@ -72,3 +72,33 @@ def test_npz_is_lossless(tmp_path):
     back = dump.read_npz(str(tmp_path / "run.npz"))
     for k, v in rec.items():
         assert np.array_equal(np.asarray(back[k]), np.asarray(v)), k
+
+
+def test_resolved_files_follow_dump_data(tmp_path):
+    """ERCD.txt: per site (z fastest), per energy the four values ERJx, ERJy, ERJz, ERRhon;
+    ORCD.txt: per site the norb^2 pair triples (ORJx, ORJy, ORJz), then the norb ORRhon
+    values (Source/Dump_Data.F90:100-132)."""
+    npx, npy, npz, n_e = 2, 2, 1, 3
+    rng = np.random.default_rng(3)
+    rec = _record(npx=npx, npy=npy, npz=npz, n_e=n_e, poisson=False, spin=False)
+    for k in ("ERJx", "ERJy", "ERJz", "ERRhon"):
+        rec[k] = rng.normal(size=(npx, npy, npz, n_e))
+    for k in ("ORJx", "ORJy", "ORJz"):
+        rec[k] = rng.normal(size=(npx, npy, npz, 16))
+    rec["ORRhon"] = rng.normal(size=(npx, npy, npz, 4))
+    names = sorted(os.path.basename(p) for p in dump.write_reference_files(str(tmp_path), rec))
+    assert "ERCD.txt" in names and "ORCD.txt" in names
+    e = [x for x in open(tmp_path / "ERCD.txt").read().split("\n") if x]
+    assert len(e) == 4 * n_e * npx * npy * npz
+    assert e[0] == dump.es11_4(rec["ERJx"][0, 0, 0, 0]) and e[3] == dump.es11_4(rec["ERRhon"][0, 0, 0, 0])
+    assert e[4] == dump.es11_4(rec["ERJx"][0, 0, 0, 1])                 # next energy
+    assert e[4 * n_e] == dump.es11_4(rec["ERJx"][0, 1, 0, 0])           # next site: y
+    o = [x for x in open(tmp_path / "ORCD.txt").read().split("\n") if x]
+    per_site = 3 * 16 + 4
+    assert len(o) == per_site * npx * npy * npz
+    assert o[1] == dump.es11_4(rec["ORJy"][0, 0, 0, 0]) and o[3] == dump.es11_4(rec["ORJx"][0, 0, 0, 1])
+    assert o[48] == dump.es11_4(rec["ORRhon"][0, 0, 0, 0])
+    back = dump.read_reference_files(str(tmp_path))
+    for k in ("ERJx", "ERJy", "ERJz", "ERRhon", "ORJx", "ORJy", "ORJz", "ORRhon"):
+        assert back[k].shape == rec[k].shape
+        assert np.allclose(back[k], rec[k], rtol=5.1e-5, atol=0), k

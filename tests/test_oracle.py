@@ -191,3 +191,27 @@ def test_bond_currents_obey_kirchhoff_and_landauer():
         through = jx[:-1].sum(axis=(1, 2))
         assert np.ptp(through) <= 1e-6 * np.abs(through).max()
         assert abs(through.mean() - 2.0 * r["T12"] * (r["f1"] - r["f2"])) <= 1e-3 * abs(through.mean())
+
+
+def test_resolved_currents_decompose_the_totals():
+    """The energy- and orbital-resolved arrays of the restatement (erCD/orCD,
+    Calculate_Observables.F90:124-160, Calculate_Gnp.F90:125-129) are decompositions of the
+    totals: ERJ dE/(2 pi) = J, the ORJ pairs sum to J, the ORRhon orbitals sum to RhoN and
+    ERRhon dE/(2 pi) = RhoN - RhoP."""
+    npx, npy, npz = 4, 2, 3
+    htotd, hopx = HB.ti_wire(npx, npy, npz, W=0.2, seed=4, flux=0.4, zeeman=0.01)
+    opt = O.SolveOptions(eta=1e-5, sr_tol=1e-10, kT=0.025)
+    de = 0.013
+    w = de / (2.0 * O.PI)
+    r = O.energy_sweep(htotd, hopx, 0.07, (0.005, -0.005), de, npy, npz, opt, calc_currents=True,
+                       calc_resolved=True)
+    for d in "xyz":
+        j = r["J" + d]
+        scale = np.abs(j).max()
+        assert r["ORJ" + d].shape == (npx, npy, npz, 16)
+        assert np.abs(r["ERJ" + d] * w - j).max() <= 1e-13 * scale
+        assert np.abs(r["ORJ" + d].sum(axis=3) - j).max() <= 1e-13 * scale
+    assert r["ORRhon"].shape == (npx, npy, npz, 4)
+    assert np.abs(r["ORRhon"].sum(axis=3) - r["RhoN"]).max() <= 1e-13 * np.abs(r["RhoN"]).max()
+    diff = r["RhoN"] - r["RhoP"]
+    assert np.abs(r["ERRhon"] * w - diff).max() <= 1e-12 * np.abs(diff).max()
