@@ -45,8 +45,8 @@ extern "C" {
 #define NEGF_EINVAL       (-1)   /* bad argument or size                                 */
 #define NEGF_ENOMEM       (-2)   /* device allocation failed                             */
 #define NEGF_ECUDA        (-3)   /* a CUDA runtime call failed                           */
-#define NEGF_ESR_NOCONV   (-4)   /* Sancho-Rubio hit sr_max_iter (Contact_Self_Energy.F90:248-251) */
-#define NEGF_ENAN         (-5)   /* NaN in the Sancho-Rubio update (Contact_Self_Energy.F90:228-237) */
+#define NEGF_ESR_NOCONV   (-4)   /* Sancho-Rubio hit sr_max_iter (Contact_Self_Energy.F90:202-205) */
+#define NEGF_ENAN         (-5)   /* NaN in the Sancho-Rubio update (Contact_Self_Energy.F90:182-191) */
 #define NEGF_ESTATE       (-6)   /* call order violated (e.g. Greens before self-energy) */
 #define NEGF_EADMIT       (-7)   /* request larger than the handle's admission budget    */
 #define NEGF_ETIMEDOUT    (-8)   /* bounded device wait ran out                          */
@@ -60,7 +60,7 @@ extern "C" {
 #define NEGF_PREC_MIXED    1     /* tcgen05 BF16 sliced products, FP64 refinement        */
 
 typedef struct negf_params {
-    int32_t npx, npy, npz;   /* lattice (Source/NEGF_Module.F90:26)                      */
+    int32_t npx, npy, npz;   /* lattice (Source/NEGF_Module.F90:27)                      */
     int32_t norb;            /* orbitals per site; 4 for the TI models                   */
     int32_t n_hamiltonians;  /* Htotd slots held on the device (e.g. disorder seeds)     */
     int32_t max_batch;       /* energy points solved together by negf_solve_batch        */
@@ -165,10 +165,10 @@ NEGF_API int negf_build_hamiltonian(negf_handle* h, int32_t slot, const negf_wir
  * The four calls below are the drop-in for the reference's subroutines, in the order
  * Energy_Sweep makes them.  All device results stay in the handle between calls.       */
 
-/* Contact_Self_Energy (Source/Contact_Self_Energy.F90:1-152, contactType 0):
+/* Contact_Self_Energy (Source/Contact_Self_Energy.F90:1-106, contactType 0):
  * Sancho-Rubio decimation of both semi-infinite leads at `energy`.  Writes SigmaL,
  * SigmaR, GammaL, GammaR (M x M complex, any may be NULL) and dosc[2] = (DOSc1, DOSc2)
- * increments (:140-143).  Returns NEGF_ESR_NOCONV / NEGF_ENAN as errorFlag would be set. */
+ * increments (:94-97).  Returns NEGF_ESR_NOCONV / NEGF_ENAN as errorFlag would be set. */
 NEGF_API int negf_contact_self_energy(negf_handle* h, double energy,
                              double* SigmaL, double* SigmaR, double* GammaL, double* GammaR,
                              double* dosc);
@@ -330,8 +330,8 @@ NEGF_API double negf_server_clock(const negf_server* s);
 NEGF_API int negf_server_destroy(negf_server* s);
 
 /* ---- self-consistent bias point: Poisson ---------------------------------------------
- * The electrostatic step of the Poisson <-> NEGF loop (SIP_Main / SIP_V1,
- * Source/SIP_Solver.F90:35-231, called from Source/NEGF_Main.F90:10-12), on the current
+ * The electrostatic step of the Poisson <-> NEGF loop (Solve_Equilibrium / SIP_V1,
+ * Source/SIP_Solver.F90:1-201, called from Source/NEGF_Main.F90:10-12), on the current
  * CUDA device.  For each of n_grids site grids (npx x npy x npz, column-major, grids
  * consecutive) it solves for the electron potential energy U (eV)
  *     6 U_i - sum_{in-grid neighbours j} U_j = kappa rho_i + sum of the boundary values

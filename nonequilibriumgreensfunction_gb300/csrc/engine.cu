@@ -1,7 +1,7 @@
 // Host orchestration of the per-energy NEGF solve (FP64 form).
 //
 // Mapping to the reference (all paths relative to the reference project):
-//   solve_sr   - Contact_Self_Energy / Sancho_Rubio, Source/Contact_Self_Energy.F90:114-147,156-269
+//   solve_sr   - Contact_Self_Energy / Sancho_Rubio, Source/Contact_Self_Energy.F90:68-101,110-223
 //   solve_rgf  - Energy_Sweep InvGRd assembly (Source/Energy_Sweep.F90:31-38) and
 //                Get_Retarded_Greens (Source/Recursive_Greens.F90:2-107), fused with the
 //                G Gamma G^H products of Calculate_Gnp (Source/Calculate_Gnp.F90:10-114)
@@ -21,7 +21,7 @@
 //    reductions read (diagonal norb x norb site blocks), Gn = f1 P_1 + f2 P_2 and
 //    Gp = (1-f1) P_1 + (1-f2) P_2 (Calculate_Gnp.F90:10-114 with the scalars pulled out).
 //  * When H_1 == H_N the two leads share one decimation: the right-lead recursion is the
-//    left one with t and t~ exchanged (Contact_Self_Energy.F90:121,133), so the products
+//    left one with t and t~ exchanged (Contact_Self_Energy.F90:75,87), so the products
 //    that involve only t, t~ are shared and each lead keeps its own T and stop test.
 //  * HopX that is block diagonal in norb x norb site blocks (every channel built by
 //    Source/Build_Hamiltonian.F90:59-64) is applied as a site-local operator.
@@ -451,7 +451,7 @@ int Engine::invert_impl(double2* A, long long sA, int batch, int* status_dev) {
 }
 
 // -------------------------------------------------------------------------------------
-// Sancho-Rubio (Source/Contact_Self_Energy.F90:156-269), batched over problems
+// Sancho-Rubio (Source/Contact_Self_Energy.F90:110-223), batched over problems
 // -------------------------------------------------------------------------------------
 int Engine::solve_sr(const std::vector<SrJob>& jobs, std::vector<int>& status, std::vector<int>& iters) {
   cudaEvent_t ph;

@@ -293,7 +293,7 @@ __global__ void identity_kernel(int n, double2* A, long long sA) {
     d[e] = make_double2((e % n) == (e / n) ? 1.0 : 0.0, 0.0);
 }
 
-// ---- Sancho-Rubio pieces (Contact_Self_Energy.F90:156-269) ---------------------------
+// ---- Sancho-Rubio pieces (Contact_Self_Energy.F90:110-223) ---------------------------
 __global__ void form_alpha_kernel(int n, const double* energies, const double2* const* hend, double eta, double extra,
                                   double2* A, long long sA) {
   const int b = blockIdx.y;

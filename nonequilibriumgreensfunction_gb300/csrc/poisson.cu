@@ -1,5 +1,5 @@
 // Electrostatics of the self-consistent bias point on the device: the role of SIP_V1
-// (Source/SIP_Solver.F90:35-231) in the Poisson <-> NEGF loop of Source/NEGF_Main.F90:7-38.
+// (Source/SIP_Solver.F90:36-201) in the Poisson <-> NEGF loop of Source/NEGF_Main.F90:7-38.
 //
 // The system is the 7-point Laplacian on the npx x npy x npz site grid with Dirichlet
 // values outside it (contacts at x = -1 and x = npx, a gate on every y and z face):

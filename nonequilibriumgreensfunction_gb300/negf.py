@@ -4,7 +4,7 @@ The reference's hot path is Energy_Sweep (Source/Energy_Sweep.F90:1-46) calling 
 subroutines that share NEGF_Module globals.  ``Solver`` keeps their names and argument
 meaning, with the globals made explicit:
 
-    Solver.contact_self_energy(energy)        Contact_Self_Energy   (Contact_Self_Energy.F90:1-152)
+    Solver.contact_self_energy(energy)        Contact_Self_Energy   (Contact_Self_Energy.F90:1-106)
     Solver.get_retarded_greens()              Get_Retarded_Greens   (Recursive_Greens.F90:2-107)
     Solver.calculate_gnp(f1, f2, dE, ...)     Calculate_Gnp         (Calculate_Gnp.F90:1-136)
     Solver.calculate_observables(dE, f1, f2)  Calculate_Observables (Calculate_Observables.F90:2-169)

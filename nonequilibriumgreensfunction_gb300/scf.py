@@ -7,7 +7,7 @@ samples as one batched device solve, and solves the 7-point Poisson problem for 
 potential on the device (negf_poisson_solve, the role of SIP_V1 in
 Source/SIP_Solver.F90).  The potential is mixed linearly, U <- U + beta (U_poisson - U),
 for a fixed number of iterations; the history records max |U_poisson - U| and the
-reference's relative-change test max |dU| / (1e-10 + |U|) (Source/SIP_Solver.F90:214-219).
+reference's relative-change test max |dU| / (1e-10 + |U|) (Source/SIP_Solver.F90:185-189).
 
 Electrostatics (the configuration's choices; the reference's own Poisson setup differs and
 is documented with the oracle):

@@ -8,8 +8,8 @@ It restates, in NumPy complex128 with LAPACK ``zgetrf``/``zgetri`` (the routines
 reference calls through MKL), the reference's per-energy path:
 
     Source/Energy_Sweep.F90:1-46            energy_sweep()
-    Source/Contact_Self_Energy.F90:1-152    contact_self_energy()
-    Source/Contact_Self_Energy.F90:156-269  sancho_rubio()
+    Source/Contact_Self_Energy.F90:1-106    contact_self_energy()
+    Source/Contact_Self_Energy.F90:110-223  sancho_rubio()
     Source/MKL_Routines_Cluster.F90:2-33    invert_matrix()
     Source/Recursive_Greens.F90:2-107       get_retarded_greens()
     Source/Calculate_Gnp.F90:1-136          calculate_gnp()
@@ -154,8 +154,8 @@ def build_hamiltonian_reference(npx, npy, npz, a0=1.0, mu_t=0.0, ab_phi=0.0, bcy
 class SolveOptions:
     """Per-run switches.  Defaults are the reference's own values."""
     eta: float = ETA_SIGMA_REFERENCE        # Source/Constants.F90:7
-    sr_tol: float = 1e-8                     # Source/Contact_Self_Energy.F90:200
-    sr_max_iter: int = 20000                 # Source/Contact_Self_Energy.F90:200,248
+    sr_tol: float = 1e-8                     # Source/Contact_Self_Energy.F90:154
+    sr_max_iter: int = 20000                 # Source/Contact_Self_Energy.F90:154,202
     kT: float = 0.0                          # 0 -> T=0 step, Source/Energy_Sweep.F90:11-21
     calc_spin: bool = False                  # calcSigExp, Source/Read_In_Allocate.F90:93
     norb: int = 4
@@ -185,66 +185,66 @@ def invert_matrix(g: np.ndarray):
 
 
 # ---------------------------------------------------------------------------
-# Sancho-Rubio, Source/Contact_Self_Energy.F90:156-269
+# Sancho-Rubio, Source/Contact_Self_Energy.F90:110-223
 # ---------------------------------------------------------------------------
 def sancho_rubio(alpha: np.ndarray, beta: np.ndarray, eta: float, tol: float, max_iter: int):
     """Lopez-Sancho/Rubio decimation.  Returns (Sigma, error_flag, iterations).
 
     The iteration counter is local to the call; in the reference it is an implicitly
-    SAVEd ``INTEGER :: counter=1`` (Contact_Self_Energy.F90:165) shared by all calls, a
+    SAVEd ``INTEGER :: counter=1`` (Contact_Self_Energy.F90:119) shared by all calls, a
     difference that only matters when the 20000-iteration cap is hit.
     """
     nn = alpha.shape[0]
     ident = np.eye(nn, dtype=complex)
     betad = beta.conj().T
-    # :187 tmp = inv(alpha + i*eta) (an extra i*eta on top of the one in alpha)
+    # :141 tmp = inv(alpha + i*eta) (an extra i*eta on top of the one in alpha)
     tmp, err = invert_matrix(alpha + ident * complex(0.0, eta))
-    t = -tmp @ betad                    # :193
-    tt = -tmp @ beta                    # :195
-    cap_t = t.copy()                    # :197
-    toldt = ident.copy()                # :198
-    change_max = 1.0                    # change initialised to c1, :181
+    t = -tmp @ betad                    # :147
+    tt = -tmp @ beta                    # :149
+    cap_t = t.copy()                    # :151
+    toldt = ident.copy()                # :152
+    change_max = 1.0                    # change initialised to c1, :135
     counter = 1
-    while counter <= max_iter and change_max > tol:       # :200
+    while counter <= max_iter and change_max > tol:       # :154
         counter += 1
-        toldt = toldt @ tt                                  # :203-204
-        cmat1 = ident - t @ tt - tt @ t                     # :206-208
-        tmp, err = invert_matrix(cmat1)                     # :209
+        toldt = toldt @ tt                                  # :157-158
+        cmat1 = ident - t @ tt - tt @ t                     # :160-162
+        tmp, err = invert_matrix(cmat1)                     # :163
         if err:
-            raise RuntimeError("Sancho_Rubio: singular inv(Id - t*tt - tt*t)")  # :210-213 STOP
-        t = (tmp @ t) @ t                                   # :216-218
-        tt = (tmp @ tt) @ tt                                # :220-222
-        change = toldt @ t                                  # :224
-        cap_t = cap_t + change                              # :226
+            raise RuntimeError("Sancho_Rubio: singular inv(Id - t*tt - tt*t)")  # :164-167 STOP
+        t = (tmp @ t) @ t                                   # :170-172
+        tt = (tmp @ tt) @ tt                                # :174-176
+        change = toldt @ t                                  # :178
+        cap_t = cap_t + change                              # :180
         abs_change = np.abs(change)
-        if np.isnan(abs_change).any():                      # :228-237
+        if np.isnan(abs_change).any():                      # :182-191
             return None, 1, counter - 1
         change_max = float(abs_change.max())
-    cmat1 = beta @ cap_t + alpha                            # :241-242
-    gfinal, err = invert_matrix(cmat1)                      # :243
-    if counter == max_iter:                                 # :248-251
+    cmat1 = beta @ cap_t + alpha                            # :195-196
+    gfinal, err = invert_matrix(cmat1)                      # :197
+    if counter == max_iter:                                 # :202-205
         err = 1
-    sigma = (beta @ gfinal) @ beta.conj().T                 # :254-255
+    sigma = (beta @ gfinal) @ beta.conj().T                 # :208-209
     return sigma, err, counter - 1
 
 
 # ---------------------------------------------------------------------------
-# Contact_Self_Energy (contactType 0), Source/Contact_Self_Energy.F90:1-152
+# Contact_Self_Energy (contactType 0), Source/Contact_Self_Energy.F90:1-106
 # ---------------------------------------------------------------------------
 def contact_self_energy(htotd, hopx, energy, opt: SolveOptions):
     """Returns dict with SigmaL, SigmaR, GammaL, GammaR, dosc (2,), sr_err (2,), sr_iters (2,)."""
     npx, m, _ = htotd.shape
     ident = np.eye(m, dtype=complex)
-    ce = complex(energy, opt.eta)                           # :62
-    alpha = -htotd[0] + ident * ce                          # :117-120
+    ce = complex(energy, opt.eta)                           # :16
+    alpha = -htotd[0] + ident * ce                          # :71-74
     sig_l, err_l, it_l = sancho_rubio(alpha, -hopx.conj().T, opt.eta, opt.sr_tol, opt.sr_max_iter)
-    alpha = -htotd[npx - 1] + ident * ce                    # :129-132
+    alpha = -htotd[npx - 1] + ident * ce                    # :83-86
     sig_r, err_r, it_r = sancho_rubio(alpha, -hopx, opt.eta, opt.sr_tol, opt.sr_max_iter)
     if sig_l is None or sig_r is None:
         raise FloatingPointError("Sancho_Rubio produced NaN")
-    dosc = np.array([-np.imag(np.trace(sig_l)) / PI, -np.imag(np.trace(sig_r)) / PI])  # :140-143
-    gam_l = 1j * (sig_l - sig_l.conj().T)                   # :146
-    gam_r = 1j * (sig_r - sig_r.conj().T)                   # :147
+    dosc = np.array([-np.imag(np.trace(sig_l)) / PI, -np.imag(np.trace(sig_r)) / PI])  # :94-97
+    gam_l = 1j * (sig_l - sig_l.conj().T)                   # :100
+    gam_r = 1j * (sig_r - sig_r.conj().T)                   # :101
     return dict(SigmaL=sig_l, SigmaR=sig_r, GammaL=gam_l, GammaR=gam_r, dosc=dosc,
                 sr_err=np.array([err_l, err_r]), sr_iters=np.array([it_l, it_r]))
 

@@ -5,10 +5,10 @@ checker the device Poisson solver and the self-consistent loop are compared agai
 
 What it restates:
 
-    Source/SIP_Solver.F90:35-231    sip_iteration()  Stone's strongly implicit procedure, both
+    Source/SIP_Solver.F90:36-201    sip_iteration()  Stone's strongly implicit procedure, both
                                                       sweep orders (odd/even outer iteration)
-    Source/SIP_Module.F90:66-68     SIP_ALPHAS       the relaxation parameters cycled by iteration
-    Source/SIP_Solver.F90:214-221   the update Phi += PhiDelta and the relative-change test
+    Source/SIP_Module.F90:47-49     SIP_ALPHAS       the relaxation parameters cycled by iteration
+    Source/SIP_Solver.F90:185-190   the update Phi += PhiDelta and the relative-change test
     Source/NEGF_Main.F90:7-38       scf_loop()       Poisson -> Build_Hamiltonian -> energy loop
 
 The electrostatic problem is the one of the self-consistent configuration (7-point
@@ -22,7 +22,7 @@ potential energy U (eV) on each site:
 so that electrons raise their own potential energy.  The reference's Poisson differs and
 this restatement says where: it normalises eps by the Bi2Se3 value and has no kappa
 (Source/SIP_Coefficients.F90), shifts the SIP diagonal by -ro as a linearisation of its
-nonlinear problem (Source/SIP_Solver.F90:59-63), takes one SIP sweep per outer iteration
+nonlinear problem (Source/SIP_Solver.F90:62-67), takes one SIP sweep per outer iteration
 with Phi += PhiDelta, and adds Phi to the on-site energy with the opposite sign convention
 (Source/Build_Hamiltonian.F90:104-112).  Here each outer iteration solves the linear
 problem to convergence with the same SIP recurrences and mixes linearly:
@@ -40,7 +40,7 @@ from oracle import negf_oracle as O
 
 EPS0 = 8.85418782e-12          # Source/Constants.F90:5
 LATTICE_M = 1e-9               # lattice constant a = 1 nm
-SIP_ALPHAS = (0.25, 0.35, 0.45, 0.35, 0.25, 0.15)   # Source/SIP_Module.F90:66-68
+SIP_ALPHAS = (0.25, 0.35, 0.45, 0.35, 0.25, 0.15)   # Source/SIP_Module.F90:47-49
 
 
 def kappa(eps_r: float) -> float:
@@ -103,7 +103,7 @@ def _hyperplanes(shape):
 
 
 def _sip_sweep(coef, rhs_res, alpha, planes):
-    """One SIP correction in the first sweep order of Source/SIP_Solver.F90:35-116 on a
+    """One SIP correction in the first sweep order of Source/SIP_Solver.F90:59-117 on a
     grid whose unknowns are ordered i fastest, then j, then k.  coef = (B, C, D, E, F, G, H)
     are the couplings to (k-1, j-1, i-1, self, i+1, j+1, k+1); rhs_res is the residual R.
     Points of one hyperplane i+j+k = s depend only on the plane before (forward) or after
@@ -125,11 +125,11 @@ def _sip_sweep(coef, rhs_res, alpha, planes):
         e[I, J, K] = (F[i, j, k] - alpha * (a[I, J, K] * e[I, J, K - 1] + b[I, J, K] * e[I, J - 1, K])) / d[I, J, K]
         f[I, J, K] = (G[i, j, k] - alpha * (c[I, J, K] * f[I - 1, J, K] + a[I, J, K] * f[I, J, K - 1])) / d[I, J, K]
         g[I, J, K] = (H[i, j, k] - alpha * (c[I, J, K] * g[I - 1, J, K] + b[I, J, K] * g[I, J - 1, K])) / d[I, J, K]
-    for (i, j, k) in planes:                                   # :99-107
+    for (i, j, k) in planes:                                   # :95-106
         I, J, K = i + 1, j + 1, k + 1
         v[I, J, K] = (rhs_res[i, j, k] - a[I, J, K] * v[I, J, K - 1] - b[I, J, K] * v[I, J - 1, K]
                       - c[I, J, K] * v[I - 1, J, K]) / d[I, J, K]
-    for (i, j, k) in reversed(planes):                         # :109-115
+    for (i, j, k) in reversed(planes):                         # :108-116
         I, J, K = i + 1, j + 1, k + 1
         dl[I, J, K] = v[I, J, K] - e[I, J, K] * dl[I + 1, J, K] - f[I, J, K] * dl[I, J + 1, K] \
             - g[I, J, K] * dl[I, J, K + 1]
@@ -137,12 +137,12 @@ def _sip_sweep(coef, rhs_res, alpha, planes):
 
 
 def sip_iteration(u, b, it, planes):
-    """One outer SIP iteration (Source/SIP_Solver.F90:35-221) on A u = b written as the
+    """One outer SIP iteration (Source/SIP_Solver.F90:36-190) on A u = b written as the
     reference's 7-point form  B u(k-1) + C u(j-1) + D u(i-1) + E u + F u(i+1) + G u(j+1)
     + H u(k+1) = ro  with B..H = 1, E = -6 and ro = -b.  Even iterations use the first sweep
-    order; odd ones reverse j and k (the second sweep, :118-212), which is the first sweep
+    order; odd ones reverse j and k (the second sweep, :120-181), which is the first sweep
     on the grid flipped in j and k with (B, C, G, H) -> (H, G, C, B).  alpha cycles through
-    SIP_ALPHAS (:20).  Returns u + PhiDelta and max |PhiDelta|."""
+    SIP_ALPHAS (:16).  Returns u + PhiDelta and max |PhiDelta|."""
     one = np.ones_like(u)
     coef = (one, one, one, -6.0 * one, one, one, one)
     # R = ro - (stencil) u with ro = -b: the reference's residual, zero neighbours outside

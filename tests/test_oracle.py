@@ -72,7 +72,7 @@ def test_clean_wire_has_integer_transmission():
 def test_self_energy_satisfies_surface_dyson_equation():
     # Sigma_L = H^H (alpha - Sigma_L)^-1 H, Sigma_R = H (alpha - Sigma_R)^-1 H^H, alpha = (E + i eta) - H_1.
     # The reference seeds the decimation with inv(alpha + i eta) (an extra i eta,
-    # Contact_Self_Energy.F90:187) while the final g uses alpha, so the equation holds up to
+    # Contact_Self_Energy.F90:141) while the final g uses alpha, so the equation holds up to
     # O(eta): the residual must shrink in proportion to eta.
     htotd, hopx = _wire(npx=3, W=0.0)
     m = htotd.shape[1]

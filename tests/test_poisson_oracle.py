@@ -1,5 +1,5 @@
 """The Poisson oracle: the restatement of Stone's strongly implicit procedure
-(Source/SIP_Solver.F90:35-231) is pinned against a sparse direct solve of the same
+(Source/SIP_Solver.F90:36-201) is pinned against a sparse direct solve of the same
 7-point system.  CPU only."""
 import numpy as np
 import pytest
