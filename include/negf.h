@@ -61,7 +61,8 @@ extern "C" {
 
 typedef struct negf_params {
     int32_t npx, npy, npz;   /* lattice (Source/NEGF_Module.F90:27)                      */
-    int32_t norb;            /* orbitals per site; 4 for the TI models                   */
+    int32_t norb;            /* orbitals per site (<= 8); 4 for the TI models, 8 for their
+                                BdG form with superconducting contacts                  */
     int32_t n_hamiltonians;  /* Htotd slots held on the device (e.g. disorder seeds)     */
     int32_t max_batch;       /* energy points solved together by negf_solve_batch        */
     double  eta;             /* eta_sigma, Source/Constants.F90:7 (reference 1e-4)       */
@@ -84,7 +85,34 @@ typedef struct negf_params {
     double  spin_ops[3][4][4][2]; /* gMx, gMy, gMz (row-major [row][col][re,im]) used by
                                      the spin reduction, Source/Read_In_Allocate.F90:183-196;
                                      all zero = the reference's tau0 (x) sigma_j          */
+    /* Contacts (contactType, Source/Read_In_Allocate.F90:19, Contact_Self_Energy.F90:19-92):
+     *   NEGF_CONTACT_LEADS   semi-infinite leads, Sancho-Rubio decimation (default);
+     *   NEGF_CONTACT_PBIG    phenomenological: Sigma = -i rate on every orbital of the end
+     *                        slice (:19-23);
+     *   NEGF_CONTACT_PSMALL  the same on the first npy*norb orbitals only (:24-28);
+     *   NEGF_CONTACT_SC      superconducting contacts (:29-67) on a BdG Hamiltonian: norb =
+     *                        2 nh, each site block holds the nh electron orbitals first and
+     *                        their holes after them (Read_In_Allocate.F90:69-71,
+     *                        Build_Hamiltonian.F90:52-56).  T12 is then the supercurrent
+     *                        transmission of Calculate_Observables.F90:60-81, and EDensity,
+     *                        HDensity, spin and bond currents run over the electron orbitals
+     *                        (:14-15, :37-39, :114-115).                                  */
+    int32_t contact_type;
+    int32_t reserved1;       /* must be zero                                             */
+    double  tunneling_rate;  /* phenomenological and SC contacts (Contact_Self_Energy.F90:10);
+                                0 = the reference's 1                                    */
+    double  delta_sc[2];     /* DeltaSCL, DeltaSCR in eV (Read_In_Allocate.F90:74-75)    */
+    double  chi_lr;          /* Josephson phase of the left contact (Read_In_Allocate.F90:72) */
+    double  gds[4][4][2];    /* gDS, the nh x nh pairing structure of the SC contacts
+                                (Read_In_Allocate.F90:199-202, 214-215), row-major; all zero
+                                = the four-orbital models' gDS                           */
+    int32_t reserved2[8];    /* must be zero                                             */
 } negf_params;
+
+#define NEGF_CONTACT_LEADS   0
+#define NEGF_CONTACT_PBIG    1
+#define NEGF_CONTACT_PSMALL  2
+#define NEGF_CONTACT_SC      3
 
 typedef struct negf_handle negf_handle;
 

@@ -28,6 +28,7 @@ NEGF_ESCRATCH = -12
 
 NEGF_PREC_FP64 = 0
 NEGF_PREC_MIXED = 1
+NEGF_CONTACT_LEADS, NEGF_CONTACT_PBIG, NEGF_CONTACT_PSMALL, NEGF_CONTACT_SC = 0, 1, 2, 3
 
 # every symbol include/negf.h declares
 EXPORTED_SYMBOLS = (
@@ -52,6 +53,10 @@ class NegfParams(ctypes.Structure):
         ("residual_slices", c_int32), ("sr_slices", c_int32), ("calc_currents", c_int32),
         ("reserved", c_int32 * 3),
         ("spin_ops", c_double * (3 * 4 * 4 * 2)),
+        ("contact_type", c_int32), ("reserved1", c_int32),
+        ("tunneling_rate", c_double), ("delta_sc", c_double * 2), ("chi_lr", c_double),
+        ("gds", c_double * (4 * 4 * 2)),
+        ("reserved2", c_int32 * 8),
     ]
 
 

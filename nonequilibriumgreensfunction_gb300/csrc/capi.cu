@@ -214,7 +214,7 @@ int negf_contact_self_energy(negf_handle* h, double energy, double* SigmaL, doub
   NEGF_CUDA_TRY(cudaSetDevice(e.p_.device));
   std::vector<negf::SrJob> jobs;
   const int rep = e.slot_rep_[0];
-  if (e.slot_joint_[rep]) {
+  if (e.slot_joint_[rep] || e.p_.contact_type != NEGF_CONTACT_LEADS) {
     jobs.push_back(negf::SrJob{energy, rep, 0, 1, 1});
     h->sr_l = h->sr_r = 0;
   } else {
@@ -314,15 +314,19 @@ int negf_calculate_observables(negf_handle* h, double dE, double f1, double f2, 
   Engine& e = h->eng;
   if (!e.dens_valid_) return NEGF_ESTATE;
   NEGF_CUDA_TRY(cudaSetDevice(e.p_.device));
-  double tr[4];
+  double tr[4], trj = 0.0;
   NEGF_CUDA_TRY(cudaMemcpyAsync(tr, e.dTr_, sizeof(tr), cudaMemcpyDeviceToHost, e.st_));
+  if (e.sc_()) NEGF_CUDA_TRY(cudaMemcpyAsync(&trj, e.dTrJ_, sizeof(double), cudaMemcpyDeviceToHost, e.st_));
   NEGF_CUDA_TRY(cudaStreamSynchronize(e.st_));
-  const double t12 = tr[1];
+  const double t12 = e.sc_() ? trj : tr[1];
   if (T12) *T12 = t12;
   if (EDensity) *EDensity = e.last_edens_;
   if (HDensity) *HDensity = e.last_hdens_;
   if (modes) { modes[0] = tr[0] + tr[1]; modes[1] = tr[2] + tr[3]; }
-  if (contact_current) {   // Source/Calculate_Observables.F90:102-103
+  if (contact_current && e.sc_()) {   // supercurrent, Source/Calculate_Observables.F90:79-80
+    contact_current[0] += negf::kQ * dE / negf::kH * t12;
+    contact_current[1] += negf::kQ * dE / negf::kH * (-t12);
+  } else if (contact_current) {   // Source/Calculate_Observables.F90:102-103
     contact_current[0] += negf::kQ * dE / negf::kH * (t12 * (f2 - f1));
     contact_current[1] += negf::kQ * dE / negf::kH * (t12 * (f1 - f2));
   }

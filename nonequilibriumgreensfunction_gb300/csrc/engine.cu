@@ -29,6 +29,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <complex>
 #include <cstddef>
 #include <cstring>
 #include <map>
@@ -84,7 +85,7 @@ Engine::~Engine() {
   dfree(dP1_); dfree(dP2_); dfree(dCol1_); dfree(dColN_);
   dfree(dPx1_); dfree(dPy1_); dfree(dPz1_); dfree(dPx2_); dfree(dPy2_); dfree(dPz2_);
   if (currents_) { dfree(dYalt_); dfree(dCNalt_); }
-  dfree(dEr_); dfree(dOrAcc_);
+  dfree(dEr_); dfree(dOrAcc_); dfree(dContactCoef_); dfree(dG11_); dfree(dTrJ_);
   dfree(dSite_); dfree(dSums_); dfree(dTr_); dfree(dAcc_); dfree(dStatus_); dfree(dItems_);
   dfree(dSr_); dfree(dSrSigL_); dfree(dSrSigR_); dfree(dSrGamL_); dfree(dSrGamR_);
   dfree(dSrCmax_); dfree(dSrDos_); dfree(dSrActive_); dfree(dSrE_); dfree(dSrHend_); dfree(dSrStatus_);
@@ -97,7 +98,17 @@ Engine::~Engine() {
 }
 
 int Engine::init(const negf_params& p) {
-  if (p.npx < 2 || p.npy < 1 || p.npz < 1 || p.norb < 1 || p.norb > 4) return NEGF_EINVAL;
+  if (p.npx < 2 || p.npy < 1 || p.npz < 1 || p.norb < 1 || p.norb > 8) return NEGF_EINVAL;
+  if (p.contact_type < NEGF_CONTACT_LEADS || p.contact_type > NEGF_CONTACT_SC || p.reserved1 != 0) return NEGF_EINVAL;
+  for (int i = 0; i < 8; ++i)
+    if (p.reserved2[i] != 0) return NEGF_EINVAL;
+  // SC contacts act on a BdG Hamiltonian: nh electron orbitals, then their holes
+  const int nh = p.contact_type == NEGF_CONTACT_SC ? p.norb / 2 : p.norb;
+  if (p.contact_type == NEGF_CONTACT_SC && (p.norb % 2 != 0 || nh > 4)) return NEGF_EINVAL;
+  if (p.calc_spin && nh > 4) return NEGF_EINVAL;
+  if (!(p.tunneling_rate >= 0.0) || !std::isfinite(p.delta_sc[0]) || !std::isfinite(p.delta_sc[1]) ||
+      !std::isfinite(p.chi_lr))
+    return NEGF_EINVAL;
   if (p.n_hamiltonians < 1 || p.max_batch < 1 || p.max_batch > 4096) return NEGF_EINVAL;
   if (!(p.eta >= 0.0) || !(p.sr_tol > 0.0) || p.sr_max_iter < 1) return NEGF_EINVAL;
   if (p.precision != NEGF_PREC_FP64 && p.precision != NEGF_PREC_MIXED) return NEGF_EINVAL;
@@ -115,6 +126,7 @@ int Engine::init(const negf_params& p) {
   S_ = 2 * p.max_batch;
   keep_columns_ = p.keep_g_columns != 0;
   currents_ = p.calc_currents != 0;
+  nh_ = nh;
   nf_ = currents_ ? 8 : 5;
   mixed_ = p.precision == NEGF_PREC_MIXED;
   if (mixed_ && p.mixed_slices != 0) s_rgf_ = p.mixed_slices;
@@ -168,6 +180,11 @@ int Engine::alloc() {
     dCNalt_ = dCN_;
   }
   sums_blocks_ = (int)((total + 255) / 256);
+  if (p_.contact_type != NEGF_CONTACT_LEADS) NEGF_TRY(dalloc(&dContactCoef_, (size_t)S_ * 6, bytes_));
+  if (sc_()) {
+    NEGF_TRY(dalloc(&dG11_, (size_t)B_ * M_ * p_.norb, bytes_));
+    NEGF_TRY(dalloc(&dTrJ_, (size_t)B_, bytes_));
+  }
   NEGF_TRY(dalloc(&dSite_, (size_t)(B_ * nf_ * total), bytes_));
   NEGF_TRY(dalloc(&dSums_, (size_t)B_ * sums_blocks_ * 2, bytes_));
   NEGF_TRY(dalloc(&dTr_, (size_t)B_ * 4, bytes_));
@@ -224,20 +241,23 @@ int Engine::alloc() {
     for (int r = 0; r < 4; ++r)
       for (int c = 0; c < 4; ++c)
         if (p_.spin_ops[j][r][c][0] != 0.0 || p_.spin_ops[j][r][c][1] != 0.0) any = true;
-  const int no = p_.norb;
+  // the operators act on the nh electron orbitals of a site (Calculate_Observables.F90:14-15);
+  // with SC contacts the hole block of the BdG site stays zero
+  const int no = p_.norb, ne = nh_;
   if (any) {
     for (int j = 0; j < 3; ++j)
-      for (int r = 0; r < no; ++r)
-        for (int c = 0; c < no; ++c)
+      for (int r = 0; r < ne; ++r)
+        for (int c = 0; c < ne; ++c)
           spin[(j * no + r) * no + c] = make_double2(p_.spin_ops[j][r][c][0], p_.spin_ops[j][r][c][1]);
-  } else if (no == 4) {
+  } else if (ne == 4) {
     // sigma_x, sigma_y, sigma_z on the spin index (orbital = 2*tau + sigma)
     const double2 one = make_double2(1, 0), mi = make_double2(0, -1), pi_ = make_double2(0, 1), m1 = make_double2(-1, 0);
+    auto at = [&](int j, int r, int c) -> double2& { return spin[(j * no + r) * no + c]; };
     for (int blk = 0; blk < 2; ++blk) {
       const int o = 2 * blk;
-      spin[(0 * 4 + o) * 4 + o + 1] = one; spin[(0 * 4 + o + 1) * 4 + o] = one;
-      spin[(1 * 4 + o) * 4 + o + 1] = mi;  spin[(1 * 4 + o + 1) * 4 + o] = pi_;
-      spin[(2 * 4 + o) * 4 + o] = one;     spin[(2 * 4 + o + 1) * 4 + o + 1] = m1;
+      at(0, o, o + 1) = one; at(0, o + 1, o) = one;
+      at(1, o, o + 1) = mi;  at(1, o + 1, o) = pi_;
+      at(2, o, o) = one;     at(2, o + 1, o + 1) = m1;
     }
   }
   NEGF_CUDA_TRY(cudaMemcpy(dSpin_, spin.data(), sizeof(double2) * spin.size(), cudaMemcpyHostToDevice));
@@ -456,7 +476,8 @@ int Engine::invert_impl(double2* A, long long sA, int batch, int* status_dev) {
 int Engine::solve_sr(const std::vector<SrJob>& jobs, std::vector<int>& status, std::vector<int>& iters) {
   cudaEvent_t ph;
   timed_begin(st_, TK_PH_SR, 0.0, &ph);
-  const int rc = solve_sr_impl(jobs, status, iters);
+  const int rc = p_.contact_type == NEGF_CONTACT_LEADS ? solve_sr_impl(jobs, status, iters)
+                                                       : solve_contact_model(jobs, status, iters);
   timed_end(st_, TK_PH_SR, ph);
   return rc;
 }
@@ -485,15 +506,15 @@ int Engine::solve_sr_impl(const std::vector<SrJob>& jobs, std::vector<int>& stat
   auto inv_merge = [&](double2* A) -> int { return invert(A, sM, S, dSrStatus_); };
   cur_slices_ = s_sr_;
 
-  // alpha = (E + i eta) I - H_end (:117-120 / :129-132)
+  // alpha = (E + i eta) I - H_end (:71-74 / :83-86)
   NEGF_TRY(form_alpha(M_, S, dSrE_, dSrHend_, p_.eta, 0.0, buf(SR_ALPHA), sM, st_));
-  // g0 = inv(alpha + i eta I) (:187)
+  // g0 = inv(alpha + i eta I) (:141)
   NEGF_TRY(form_alpha(M_, S, dSrE_, dSrHend_, p_.eta, p_.eta, buf(SR_TMP), sM, st_));
   NEGF_TRY(inv_merge(buf(SR_TMP)));
-  // left lead beta = -H^H:  t = -g0 beta^H = g0 H,  t~ = -g0 beta = g0 H^H (:193-195)
+  // left lead beta = -H^H:  t = -g0 beta^H = g0 H,  t~ = -g0 beta = g0 H^H (:147-149)
   NEGF_TRY(hop_mul(0, OP_N, buf(SR_TMP), sM, buf(SR_T), sM, S));
   NEGF_TRY(hop_mul(0, OP_C, buf(SR_TMP), sM, buf(SR_TT), sM, S));
-  // T_L = t; the right lead (beta = -H) starts from t_R = t~, so T_R = t~ (:197)
+  // T_L = t; the right lead (beta = -H) starts from t_R = t~, so T_R = t~ (:151)
   NEGF_TRY(copy_blocks(M_, S, buf(SR_T), sM, buf(SR_TL), sM, st_));
   NEGF_TRY(copy_blocks(M_, S, buf(SR_TT), sM, buf(SR_TR), sM, st_));
   NEGF_TRY(set_identity(M_, S, buf(SR_TOLDL), sM, st_));
@@ -508,22 +529,22 @@ int Engine::solve_sr_impl(const std::vector<SrJob>& jobs, std::vector<int>& stat
   auto any_active = [&]() { return std::any_of(act.begin(), act.end(), [](int a) { return a != 0; }); };
   while (any_active() && it < p_.sr_max_iter) {
     ++it;
-    // Told_L <- Told_L t~ ; Told_R <- Told_R t  (:203-204, with t <-> t~ for the right lead)
+    // Told_L <- Told_L t~ ; Told_R <- Told_R t  (:157-158, with t <-> t~ for the right lead)
     NEGF_TRY(gemm(S, OP_N, buf(SR_TOLDL), sM, OP_N, buf(SR_TT), sM, buf(SR_W1), sM, one, zero));
     std::swap(role[SR_TOLDL], role[SR_W1]);
     NEGF_TRY(gemm(S, OP_N, buf(SR_TOLDR), sM, OP_N, buf(SR_T), sM, buf(SR_W1), sM, one, zero));
     std::swap(role[SR_TOLDR], role[SR_W1]);
-    // tmp = inv(I - t t~ - t~ t) (:206-209)
+    // tmp = inv(I - t t~ - t~ t) (:160-163)
     NEGF_TRY(set_identity(M_, S, buf(SR_TMP), sM, st_));
     NEGF_TRY(gemm(S, OP_N, buf(SR_T), sM, OP_N, buf(SR_TT), sM, buf(SR_TMP), sM, mone, one));
     NEGF_TRY(gemm(S, OP_N, buf(SR_TT), sM, OP_N, buf(SR_T), sM, buf(SR_TMP), sM, mone, one));
     NEGF_TRY(inv_merge(buf(SR_TMP)));
-    // t <- tmp t t ; t~ <- tmp t~ t~ (:216-222)
+    // t <- tmp t t ; t~ <- tmp t~ t~ (:170-176)
     NEGF_TRY(gemm(S, OP_N, buf(SR_TMP), sM, OP_N, buf(SR_T), sM, buf(SR_W1), sM, one, zero));
     NEGF_TRY(gemm(S, OP_N, buf(SR_W1), sM, OP_N, buf(SR_T), sM, buf(SR_TN), sM, one, zero));
     NEGF_TRY(gemm(S, OP_N, buf(SR_TMP), sM, OP_N, buf(SR_TT), sM, buf(SR_W1), sM, one, zero));
     NEGF_TRY(gemm(S, OP_N, buf(SR_W1), sM, OP_N, buf(SR_TT), sM, buf(SR_TTN), sM, one, zero));
-    // change = Told t ; T += change (:224-226)
+    // change = Told t ; T += change (:178-180)
     NEGF_TRY(gemm(S, OP_N, buf(SR_TOLDL), sM, OP_N, buf(SR_TN), sM, buf(SR_CHG), sM, one, zero));
     NEGF_TRY(sr_accumulate(M_, S, dSrActive_, buf(SR_CHG), sM, buf(SR_TL), sM, dSrCmax_, st_));
     NEGF_TRY(gemm(S, OP_N, buf(SR_TOLDR), sM, OP_N, buf(SR_TTN), sM, buf(SR_CHG), sM, one, zero));
@@ -536,10 +557,10 @@ int Engine::solve_sr_impl(const std::vector<SrJob>& jobs, std::vector<int>& stat
     for (int q = 0; q < 2 * S; ++q) {
       if (!act[q]) continue;
       const double c = hPin_[q];
-      if (std::isnan(c)) {               // :228-237
+      if (std::isnan(c)) {               // :182-191
         status[q % S] = NEGF_ENAN;
         act[q] = 0; iters[q] = it; changed = true;
-      } else if (!(c > p_.sr_tol)) {     // loop test of :200
+      } else if (!(c > p_.sr_tol)) {     // loop test of :154
         act[q] = 0; iters[q] = it; changed = true;
       }
     }
@@ -549,7 +570,7 @@ int Engine::solve_sr_impl(const std::vector<SrJob>& jobs, std::vector<int>& stat
   for (int q = 0; q < 2 * S; ++q)
     if (act[q]) { iters[q] = it; if (status[q % S] == 0) status[q % S] = NEGF_ESR_NOCONV; }
 
-  // g = inv(alpha + beta T), Sigma = beta g beta^H (:241-255) for each lead
+  // g = inv(alpha + beta T), Sigma = beta g beta^H (:195-209) for each lead
   for (int lead = 0; lead < 2; ++lead) {
     double2* T = buf(lead == 0 ? SR_TL : SR_TR);
     double2* W = buf(SR_TMP);
@@ -576,6 +597,61 @@ int Engine::solve_sr_impl(const std::vector<SrJob>& jobs, std::vector<int>& stat
   NEGF_CUDA_TRY(cudaStreamSynchronize(st_));
   for (int s = 0; s < S; ++s)
     if (status[s] == 0 && st[s] != 0) status[s] = st[s];
+  return NEGF_OK;
+}
+
+// Contacts with a closed-form self-energy (Source/Contact_Self_Energy.F90:19-67): the
+// per-energy scalars are formed here, the blocks on the device; Gamma and the contact DOS
+// follow from Sigma as for the decimated leads (:94-101).
+int Engine::solve_contact_model(const std::vector<SrJob>& jobs, std::vector<int>& status, std::vector<int>& iters) {
+  const int S = (int)jobs.size();
+  status.assign(S, 0);
+  iters.assign(2 * S, 0);
+  if (S == 0) return NEGF_OK;
+  if (S > S_) return NEGF_EINVAL;
+  const double rate = p_.tunneling_rate == 0.0 ? 1.0 : p_.tunneling_rate;   // :10
+  std::vector<double2> coef((size_t)S * 6, make_double2(0.0, 0.0));
+  for (int s = 0; s < S; ++s) {
+    double2* c = coef.data() + (size_t)s * 6;
+    if (p_.contact_type != NEGF_CONTACT_SC) {                 // :19-28, Sigma_R = Sigma_L
+      c[0] = c[3] = make_double2(0.0, -rate);
+      continue;
+    }
+    // :29-59: omega = 1/sqrt(DeltaSCL^2 - ce^2) for both contacts (the right one also uses
+    // DeltaSCL at :49), ce = E + i eta (:16)
+    const std::complex<double> ce(jobs[s].energy, p_.eta);
+    const std::complex<double> omega = 1.0 / std::sqrt(p_.delta_sc[0] * p_.delta_sc[0] - ce * ce);
+    const std::complex<double> m_alpha = -rate * omega * ce;
+    const std::complex<double> ph = std::exp(std::complex<double>(0.0, p_.chi_lr));
+    for (int lead = 0; lead < 2; ++lead) {
+      const std::complex<double> up = rate * omega * p_.delta_sc[lead];
+      const std::complex<double> lo = rate * omega * (-p_.delta_sc[lead]);
+      const std::complex<double> u = lead == 0 ? up * ph : up, l = lead == 0 ? lo * std::conj(ph) : lo;
+      c[lead * 3 + 0] = make_double2(m_alpha.real(), m_alpha.imag());
+      c[lead * 3 + 1] = make_double2(u.real(), u.imag());
+      c[lead * 3 + 2] = make_double2(l.real(), l.imag());
+    }
+  }
+  ContactGds g{};
+  bool any = false;
+  for (int r = 0; r < 4; ++r)
+    for (int c = 0; c < 4; ++c) {
+      g.m[r][c] = make_double2(p_.gds[r][c][0], p_.gds[r][c][1]);
+      if (p_.gds[r][c][0] != 0.0 || p_.gds[r][c][1] != 0.0) any = true;
+    }
+  if (!any && nh_ == 4) {   // the four-orbital models' gDS (Source/Read_In_Allocate.F90:199-202)
+    g.m[0][1] = make_double2(1, 0); g.m[1][0] = make_double2(-1, 0);
+    g.m[2][3] = make_double2(1, 0); g.m[3][2] = make_double2(-1, 0);
+  } else if (!any && nh_ == 2) {   // :214-215
+    g.m[0][1] = make_double2(1, 0); g.m[1][0] = make_double2(-1, 0);
+  }
+  NEGF_CUDA_TRY(cudaMemcpyAsync(dContactCoef_, coef.data(), sizeof(double2) * coef.size(), cudaMemcpyHostToDevice, st_));
+  const int ndiag = p_.contact_type == NEGF_CONTACT_PSMALL ? p_.npy * p_.norb : M_;   // :24-28: NN orbitals
+  const long long sM = MM_;
+  NEGF_TRY(contact_fill(M_, p_.norb, nh_, p_.contact_type, ndiag, S, dContactCoef_, g, dSrSigL_, dSrSigR_, sM, st_));
+  for (int lead = 0; lead < 2; ++lead)
+    NEGF_TRY(sr_sigma(HopBD{}, M_, S, -1, nullptr, 0, lead == 0 ? dSrSigL_ : dSrSigR_, sM,
+                      lead == 0 ? dSrGamL_ : dSrGamR_, sM, dSrDos_ + lead * S, st_));
   return NEGF_OK;
 }
 
@@ -650,6 +726,7 @@ int Engine::solve_rgf_impl(const std::vector<Item>& items, bool keep_columns) {
     double2* Yprev = (x & 1) ? dY_ : dYalt_;
     if (x == 0) {
       NEGF_TRY(copy_blocks(M_, B, Gx, sG, dC1_, sM, st_));                     // G(1,1) = gR_1
+      if (sc_()) NEGF_TRY(site_diag(M_, p_.norb, B, dC1_, sM, dG11_, (long long)M_ * p_.norb, st_));
     } else {
       NEGF_TRY(hop_mul(1, OP_C, dC1_, sM, dZ_, sM, B));                          // H^H G(x-1,1)
       NEGF_TRY(gemm(B, OP_N, Gx, sG, OP_N, dZ_, sM, dC1_, sM, one, zero));       // gR_x H^H G(x-1,1)
@@ -722,13 +799,14 @@ int Engine::densities_impl(const std::vector<Item>& items, std::vector<double>& 
   NEGF_CUDA_TRY(cudaMemcpyAsync(dItems_, items.data(), sizeof(Item) * B, cudaMemcpyHostToDevice, st_));
   DensityArgs a{};
   a.n = M_; a.norb = p_.norb; a.npx = p_.npx; a.npy = p_.npy; a.npz = p_.npz; a.batch = B;
-  a.calc_spin = p_.calc_spin; a.nf = nf_; a.items = dItems_;
+  a.calc_spin = p_.calc_spin; a.nf = nf_; a.items = dItems_; a.nh = nh_;
   a.P1 = dP1_; a.P2 = dP2_; a.sP = (long long)p_.npx * M_ * p_.norb;
   a.spin_ops = dSpin_; a.site_out = dSite_; a.sums = dSums_;
   NEGF_TRY(density_spin(a, st_));
   if (currents_) {
     CurrentArgs c{};
     c.n = M_; c.norb = p_.norb; c.npx = p_.npx; c.npy = p_.npy; c.npz = p_.npz; c.batch = B; c.nf = nf_;
+    c.nh = nh_;
     c.items = dItems_; c.Hall = dH_; c.Hop = dHop_;
     c.Px1 = dPx1_; c.Py1 = dPy1_; c.Pz1 = dPz1_; c.Px2 = dPx2_; c.Py2 = dPy2_; c.Pz2 = dPz2_;
     c.sP = a.sP;
@@ -737,6 +815,9 @@ int Engine::densities_impl(const std::vector<Item>& items, std::vector<double>& 
     c.P1 = dP1_; c.P2 = dP2_;
     NEGF_TRY(bond_currents(c, st_));
   }
+  if (sc_())   // supercurrent transmission from slice 1 (Calculate_Observables.F90:60-81)
+    NEGF_TRY(josephson(M_, p_.norb, B, dItems_, dP1_, dP2_, a.sP, dG11_, (long long)M_ * p_.norb, dSigL_, dGamL_, MM_,
+                       dTrJ_, st_));
   const size_t np = (size_t)B * sums_blocks_ * 2;
   NEGF_CUDA_TRY(cudaMemcpyAsync(hPin_, dSums_, sizeof(double) * np, cudaMemcpyDeviceToHost, st_));
   NEGF_CUDA_TRY(cudaStreamSynchronize(st_));
@@ -767,6 +848,7 @@ int Engine::resolved(int batch, bool er, bool orb, int nslots) {
   NEGF_TRY(ensure_resolved());
   CurrentArgs c{};
   c.n = M_; c.norb = p_.norb; c.npx = p_.npx; c.npy = p_.npy; c.npz = p_.npz; c.batch = batch; c.nf = nf_;
+  c.nh = nh_;
   c.items = dItems_; c.Hall = dH_; c.Hop = dHop_;
   c.Px1 = dPx1_; c.Py1 = dPy1_; c.Pz1 = dPz1_; c.Px2 = dPx2_; c.Py2 = dPy2_; c.Pz2 = dPz2_;
   c.sP = (long long)p_.npx * M_ * p_.norb;
@@ -815,12 +897,14 @@ int Engine::batch_solve(const negf_request* req, int n, negf_result* res, double
     std::vector<Item> items(nb);
     for (int i = 0; i < nb; ++i) {
       const negf_request& r = req[c0 + i];
-      const int rep = slot_rep_[r.slot];
+      // model contacts do not depend on the Hamiltonian: one problem per energy
+      const bool model = p_.contact_type != NEGF_CONTACT_LEADS;
+      const int rep = model ? 0 : slot_rep_[r.slot];
       auto key = std::make_pair(r.energy, rep);
       auto itk = key2job.find(key);
       std::pair<int, int> jl;
       if (itk == key2job.end()) {
-        if (slot_joint_[rep]) {
+        if (model || slot_joint_[rep]) {
           jobs.push_back(SrJob{r.energy, rep, 0, 1, 1});
           jl = {(int)jobs.size() - 1, (int)jobs.size() - 1};
         } else {
@@ -853,15 +937,16 @@ int Engine::batch_solve(const negf_request* req, int n, negf_result* res, double
     if (site_items)
       NEGF_CUDA_TRY(cudaMemcpyAsync(site_items + (size_t)c0 * nf_ * total, dSite_,
                                     sizeof(double) * nf_ * total * nb, cudaMemcpyDeviceToHost, st_));
-    std::vector<double> tr(4 * (size_t)nb);
+    std::vector<double> tr(4 * (size_t)nb), trj(sc_() ? nb : 0);
     std::vector<int> rst(nb);
     NEGF_CUDA_TRY(cudaMemcpyAsync(tr.data(), dTr_, sizeof(double) * 4 * nb, cudaMemcpyDeviceToHost, st_));
+    if (sc_()) NEGF_CUDA_TRY(cudaMemcpyAsync(trj.data(), dTrJ_, sizeof(double) * nb, cudaMemcpyDeviceToHost, st_));
     NEGF_CUDA_TRY(cudaMemcpyAsync(rst.data(), dStatus_, sizeof(int) * nb, cudaMemcpyDeviceToHost, st_));
     NEGF_CUDA_TRY(cudaStreamSynchronize(st_));
     for (int i = 0; i < nb; ++i) {
       negf_result& o = res[c0 + i];
       const Item& it = items[i];
-      o.T12 = tr[4 * i + 1];
+      o.T12 = sc_() ? trj[i] : tr[4 * i + 1];
       o.modes[0] = tr[4 * i + 0] + tr[4 * i + 1];
       o.modes[1] = tr[4 * i + 2] + tr[4 * i + 3];
       o.EDensity = ed[i];

@@ -90,6 +90,14 @@ class Engine {
   // bond currents (calc_currents): +x/+y/+z neighbour site blocks of each lead, and second
   // buffers for Y = G(:,1) Gamma_L and G(:,N) so that slices x and x+1 are both at hand
   bool currents_ = false;
+  int nh_ = 4;            // electron orbitals per site (norb, or norb / 2 with SC contacts)
+  // model contacts (contact_type 1..3): Sigma from closed forms instead of Sancho-Rubio;
+  // with SC contacts the G(1,1) site blocks are kept for the supercurrent trace
+  int solve_contact_model(const std::vector<SrJob>& jobs, std::vector<int>& status, std::vector<int>& iters);
+  double2* dContactCoef_ = nullptr;   // [S_][2][3]
+  double2* dG11_ = nullptr;           // [B_][M][norb], SC contacts only
+  double* dTrJ_ = nullptr;            // [B_] supercurrent transmission, SC contacts only
+  bool sc_() const { return p_.contact_type == NEGF_CONTACT_SC; }
   int nf_ = 5;   // site fields per item: RhoN, RhoP, SigX, SigY, SigZ (+ Jx, Jy, Jz)
   double2 *dPx1_ = nullptr, *dPy1_ = nullptr, *dPz1_ = nullptr;
   double2 *dPx2_ = nullptr, *dPy2_ = nullptr, *dPz2_ = nullptr;

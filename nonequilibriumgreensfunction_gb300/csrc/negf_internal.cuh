@@ -255,6 +255,7 @@ int sr_sigma(const HopBD& h, int n, int nprob, int lead, const double2* g, long 
 // sums: [item][2] = (EDensity, HDensity).
 struct DensityArgs {
   int n, norb, npx, npy, npz, batch, calc_spin, nf;
+  int nh;                   // electron orbitals per site: EDensity/HDensity sum over them
   const Item* items;
   const double2* P1; const double2* P2; long long sP;
   const double2* spin_ops;  // 3 * norb*norb (row-major)
@@ -268,6 +269,7 @@ int density_spin(const DensityArgs& a, cudaStream_t st);
 // Py/Pz as site_pairs writes them; Hall as FormW, Hop = HopX (dense, column-major).
 struct CurrentArgs {
   int n, norb, npx, npy, npz, batch, nf;
+  int nh;                   // bond sums run over orbital pairs ii, jj < nh (electrons)
   const Item* items;
   const double2* Hall;
   const double2* Hop;
@@ -286,6 +288,19 @@ struct CurrentArgs {
 int bond_currents(const CurrentArgs& a, cudaStream_t st);
 // or_acc[slot] += this batch's orbital-resolved sums for slots 0..nslots-1
 int orbital_resolved(const CurrentArgs& a, int nslots, cudaStream_t st);
+
+// model contacts: coef[job][lead][3] = (diag, up, lo), gds the nh x nh pairing structure
+struct ContactGds {
+  double2 m[4][4];
+};
+int contact_fill(int n, int no, int nh, int type, int ndiag, int njobs, const double2* coef, const ContactGds& g,
+                 double2* sigL, double2* sigR, long long sS, cudaStream_t st);
+// out[b][r][a] = X[b](r, site(r)*no + a)
+int site_diag(int n, int no, int batch, const double2* X, long long sX, double2* out, long long sO, cudaStream_t st);
+// supercurrent transmission per item (Calculate_Observables.F90:60-81), site-block-diagonal Sigma_L
+int josephson(int n, int no, int batch, const Item* items, const double2* P1, const double2* P2, long long sP,
+              const double2* G11, long long sG, const double2* sig, const double2* gam, long long sS, double* out,
+              cudaStream_t st);
 
 // acc[slot][f][i] += sum over items b with items[b].slot == slot (in order) of
 // site_out[b][f][i], f < nf

@@ -161,29 +161,32 @@ __global__ void hop_apply_kernel(HopBD h, int n, int left, int op, const double2
 // P[r][a] = sum_k Y(r,k) conj(X(site(r)*no + a, k)); one thread per row r, the k loop is
 // split over KSPLIT groups of threads and reduced in shared memory (fixed order).
 constexpr int SB_ROWS = 64, SB_KSPLIT = 4;
+// NOM bounds the orbitals per site (4, or 8 for the BdG form); no <= NOM
+template <int NOM>
 __global__ void __launch_bounds__(SB_ROWS* SB_KSPLIT) site_blocks_kernel(int n, int no, const double2* Y, long long sY,
                                                                          const double2* X, long long sX, double2* P,
                                                                          long long sP) {
-  __shared__ double2 part[SB_KSPLIT][SB_ROWS][4];
+  __shared__ double2 part[SB_KSPLIT][SB_ROWS][NOM];
   const int b = blockIdx.y;
   const int lr = threadIdx.x % SB_ROWS, kg = threadIdx.x / SB_ROWS;
   const int r = blockIdx.x * SB_ROWS + lr;
   const double2* Yb = Y + (long long)b * sY;
   const double2* Xb = X + (long long)b * sX;
-  double2 acc[4] = {make_double2(0, 0), make_double2(0, 0), make_double2(0, 0), make_double2(0, 0)};
+  double2 acc[NOM];
+  for (int a = 0; a < NOM; ++a) acc[a] = make_double2(0, 0);
   if (r < n) {
     const int base = (r / no) * no;
     const int k_per = (n + SB_KSPLIT - 1) / SB_KSPLIT;
     const int k_lo = kg * k_per, k_hi = min(n, k_lo + k_per);
     for (int k = k_lo; k < k_hi; ++k) {
       const double2 y = Yb[(long long)k * n + r];
-      for (int a = 0; a < no && a < 4; ++a) cfma(acc[a], y, cconj(Xb[(long long)k * n + base + a]));
+      for (int a = 0; a < no && a < NOM; ++a) cfma(acc[a], y, cconj(Xb[(long long)k * n + base + a]));
     }
   }
-  for (int a = 0; a < 4; ++a) part[kg][lr][a] = acc[a];
+  for (int a = 0; a < NOM; ++a) part[kg][lr][a] = acc[a];
   __syncthreads();
   if (kg == 0 && r < n) {
-    for (int a = 0; a < no && a < 4; ++a) {
+    for (int a = 0; a < no && a < NOM; ++a) {
       double2 s = part[0][lr][a];
       for (int q = 1; q < SB_KSPLIT; ++q) s = cadd(s, part[q][lr][a]);
       P[(long long)b * sP + (long long)r * no + a] = s;
@@ -198,19 +201,20 @@ __global__ void __launch_bounds__(SB_ROWS* SB_KSPLIT) site_blocks_kernel(int n, 
 //   P2[r][a] = same with site s + npy  (next z; zero when z = npz - 1)
 // One pass over Y serves all three; the k split is reduced in shared memory per output in a
 // fixed order, so P0 equals what site_blocks_kernel writes.
+template <int NOM>
 __global__ void __launch_bounds__(SB_ROWS* SB_KSPLIT) site_pairs_kernel(int n, int no, int npy, int npz,
                                                                         const double2* Y, long long sY,
                                                                         const double2* X, long long sX, double2* P0,
                                                                         double2* P1, double2* P2, long long sP) {
-  __shared__ double2 part[SB_KSPLIT][SB_ROWS][4];
+  __shared__ double2 part[SB_KSPLIT][SB_ROWS][NOM];
   const int b = blockIdx.y;
   const int lr = threadIdx.x % SB_ROWS, kg = threadIdx.x / SB_ROWS;
   const int r = blockIdx.x * SB_ROWS + lr;
   const double2* Yb = Y + (long long)b * sY;
   const double2* Xb = X + (long long)b * sX;
-  double2 acc[3][4];
+  double2 acc[3][NOM];
   for (int d = 0; d < 3; ++d)
-    for (int a = 0; a < 4; ++a) acc[d][a] = make_double2(0, 0);
+    for (int a = 0; a < NOM; ++a) acc[d][a] = make_double2(0, 0);
   int base[3] = {-1, -1, -1};
   if (r < n) {
     const int s = r / no;
@@ -225,16 +229,16 @@ __global__ void __launch_bounds__(SB_ROWS* SB_KSPLIT) site_pairs_kernel(int n, i
       const double2* xk = Xb + (long long)k * n;
       for (int d = 0; d < 3; ++d) {
         if (base[d] < 0) continue;
-        for (int a = 0; a < no && a < 4; ++a) cfma(acc[d][a], yv, cconj(xk[base[d] + a]));
+        for (int a = 0; a < no && a < NOM; ++a) cfma(acc[d][a], yv, cconj(xk[base[d] + a]));
       }
     }
   }
   double2* outs[3] = {P0, P1, P2};
   for (int d = 0; d < 3; ++d) {
-    for (int a = 0; a < 4; ++a) part[kg][lr][a] = acc[d][a];
+    for (int a = 0; a < NOM; ++a) part[kg][lr][a] = acc[d][a];
     __syncthreads();
     if (kg == 0 && r < n) {
-      for (int a = 0; a < no && a < 4; ++a) {
+      for (int a = 0; a < no && a < NOM; ++a) {
         double2 v = part[0][lr][a];
         for (int q = 1; q < SB_KSPLIT; ++q) v = cadd(v, part[q][lr][a]);
         outs[d][(long long)b * sP + (long long)r * no + a] = v;
@@ -427,12 +431,13 @@ __global__ void density_spin_kernel(DensityArgs a) {
     const int y = s % a.npy, z = s / a.npy;
     const double2* p1 = a.P1 + (long long)b * a.sP + ((long long)x * a.n + (long long)s * no) * no;
     const double2* p2 = a.P2 + (long long)b * a.sP + ((long long)x * a.n + (long long)s * no) * no;
-    double rn = 0.0, rp = 0.0;
+    double rn = 0.0, rp = 0.0, en = 0.0, ep = 0.0;
     double sp[3] = {0.0, 0.0, 0.0};
     for (int ia = 0; ia < no; ++ia) {
       const double2 q1 = p1[ia * no + ia], q2 = p2[ia * no + ia];
       rn += it.f1 * q1.x + it.f2 * q2.x;
       rp += (1.0 - it.f1) * q1.x + (1.0 - it.f2) * q2.x;
+      if (ia == a.nh - 1) { en = rn; ep = rp; }   // EDensity/HDensity: electron orbitals only
     }
     if (a.calc_spin) {
       // Re sum_{ia,ib} Gn(ia,ib) gM(ib,ia), P stored as P[row ia][col ib]
@@ -457,8 +462,8 @@ __global__ void density_spin_kernel(DensityArgs a) {
     so[2 * total + o] = sp[0] * w;
     so[3 * total + o] = sp[1] * w;
     so[4 * total + o] = sp[2] * w;
-    e_n = rn;
-    e_p = rp;
+    e_n = en;
+    e_p = ep;
   }
   // per-item EDensity/HDensity partial sums: written per thread block, summed by host-ordered kernel
   __shared__ double red_n[256], red_p[256];
@@ -543,8 +548,8 @@ __global__ void bond_currents_kernel(CurrentArgs a) {
   double j[3] = {0.0, 0.0, 0.0}, ju[3] = {0.0, 0.0, 0.0};
   for (int d = 0; d < 3; ++d) {
     if (!bond_inside(a, d, x, y, z)) continue;
-    for (int ii = 0; ii < no; ++ii)
-      for (int jj = 0; jj < no; ++jj) {
+    for (int ii = 0; ii < a.nh; ++ii)
+      for (int jj = 0; jj < a.nh; ++jj) {
         double2 p1, p2, hab, hba;
         bond_pair(a, H, prow, d, s, ii, jj, p1, p2, hab, hba);
         const double dum = (double)bond_dum(p1, p2, hab, hba, it.f1, it.f2, a.q2_over_hbar);
@@ -594,7 +599,7 @@ __global__ void orbital_resolved_kernel(CurrentArgs a) {
   double acc = 0.0;
   if (q < 3 * no * no) {
     const int d = q / (no * no), ii = (q % (no * no)) / no, jj = q % no;
-    if (bond_inside(a, d, x, y, z)) {
+    if (ii < a.nh && jj < a.nh && bond_inside(a, d, x, y, z)) {
       for (int b = 0; b < a.batch; ++b) {
         const Item it = a.items[b];
         if (it.slot != slot) continue;
@@ -618,6 +623,81 @@ __global__ void orbital_resolved_kernel(CurrentArgs a) {
   }
   const long long o = (long long)x + (long long)a.npx * (y + (long long)a.npy * z);
   a.or_acc[((long long)slot * nq + q) * total + o] += acc;
+}
+
+// ---- model contacts (Contact_Self_Energy.F90:19-67) ---------------------------------
+// Sigma of job s, lead l: coef[s][l] = (diag, up, lo).  Types 1/2: diag on the first ndiag
+// orbitals.  Type 3: the same norb x norb block on every site, diag on both nh x nh
+// diagonal blocks, up * gds in the electron-hole block, lo * gds in the hole-electron one.
+__global__ void contact_fill_kernel(int n, int no, int nh, int type, int ndiag, const double2* coef, ContactGds g,
+                                    double2* sigL, double2* sigR, long long sS) {
+  const int job = blockIdx.y;
+  const long long nn = (long long)n * n;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < 2 * nn;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int lead = (int)(e / nn);
+    const long long f = e % nn;
+    const int i = (int)(f % n), j = (int)(f / n);
+    const double2* c = coef + ((long long)job * 2 + lead) * 3;
+    double2 v = make_double2(0.0, 0.0);
+    if (type != 3) {
+      if (i == j && i < ndiag) v = c[0];
+    } else if (i / no == j / no) {
+      const int ai = i % no, aj = j % no;
+      const bool ei = ai < nh, ej = aj < nh;
+      if (ei == ej) {
+        if (ai == aj) v = c[0];
+      } else if (ei) {
+        v = cmul(c[1], g.m[ai][aj - nh]);
+      } else {
+        v = cmul(c[2], g.m[ai - nh][aj]);
+      }
+    }
+    (lead == 0 ? sigL : sigR)[(long long)job * sS + f] = v;
+  }
+}
+
+// out[b][r][a] = X[b](r, site(r)*no + a): the diagonal site blocks of a column-major block
+__global__ void site_diag_kernel(int n, int no, const double2* X, long long sX, double2* out, long long sO) {
+  const int b = blockIdx.y;
+  const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (e >= (long long)n * no) return;
+  const int r = (int)(e / no), a = (int)(e % no);
+  out[(long long)b * sO + e] = X[(long long)b * sX + (long long)((r / no) * no + a) * n + r];
+}
+
+// Supercurrent transmission of Calculate_Observables.F90:60-81 for site-block-diagonal
+// SigmaL / GammaL: T = sum_r sz(r) Re[(i Gn11 SigmaL^H)(r,r) - (G11 GammaL)(r,r)], sz = +1
+// on electron orbitals, with Gn11 = f1 P1 + f2 P2 on slice 1 and G11 its diagonal site
+// blocks.  One CTA per item, fixed reduction order.
+__global__ void josephson_kernel(int n, int no, const Item* items, const double2* P1, const double2* P2, long long sP,
+                                 const double2* G11, long long sG, const double2* sig, const double2* gam,
+                                 long long sS, double* out) {
+  __shared__ double red[EW_THREADS];
+  const int b = blockIdx.x;
+  const Item it = items[b];
+  double t = 0.0;
+  for (int r = threadIdx.x; r < n; r += blockDim.x) {
+    const int base = (r / no) * no;
+    double2 s1 = make_double2(0.0, 0.0), s2 = make_double2(0.0, 0.0);
+    for (int a = 0; a < no; ++a) {
+      const long long q = (long long)r * no + a;
+      const double2 p1 = P1[(long long)b * sP + q], p2 = P2[(long long)b * sP + q];
+      const double2 gn = make_double2(it.f1 * p1.x + it.f2 * p2.x, it.f1 * p1.y + it.f2 * p2.y);
+      const long long c = (long long)(base + a);
+      cfma(s1, gn, cconj(sig[(long long)b * sS + c * n + r]));           // Gn(r,c) conj(Sigma(r,c))
+      cfma(s2, G11[(long long)b * sG + q], gam[(long long)b * sS + (long long)r * n + c]);  // G(r,c) Gamma(c,r)
+    }
+    const double v = -s1.y - s2.x;                                       // Re(i s1) - Re(s2)
+    t += (r % no < no / 2) ? v : -v;
+  }
+  red[threadIdx.x] = t;
+  __syncthreads();
+  for (int k = blockDim.x / 2; k > 0; k >>= 1) {
+    if (threadIdx.x < k) red[threadIdx.x] += red[threadIdx.x + k];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[b] = red[0];
 }
 
 __global__ void reduce_sites_kernel(int batch, int total, int nf, int nslots, const Item* items,
@@ -660,9 +740,12 @@ int hop_apply(const HopBD& h, int n, int batch, int left, Op op, const double2* 
 
 int site_blocks(int n, int norb, int batch, const double2* Y, long long sY, const double2* X, long long sX, double2* P,
                 long long sP, cudaStream_t st) {
-  if (norb > 4) return NEGF_EINVAL;
+  if (norb < 1 || norb > 8) return NEGF_EINVAL;
   dim3 grid((n + SB_ROWS - 1) / SB_ROWS, batch);
-  site_blocks_kernel<<<grid, SB_ROWS * SB_KSPLIT, 0, st>>>(n, norb, Y, sY, X, sX, P, sP);
+  if (norb <= 4)
+    site_blocks_kernel<4><<<grid, SB_ROWS * SB_KSPLIT, 0, st>>>(n, norb, Y, sY, X, sX, P, sP);
+  else
+    site_blocks_kernel<8><<<grid, SB_ROWS * SB_KSPLIT, 0, st>>>(n, norb, Y, sY, X, sX, P, sP);
   NEGF_CUDA_TRY(cudaGetLastError());
   count_launch();
   return NEGF_OK;
@@ -670,16 +753,19 @@ int site_blocks(int n, int norb, int batch, const double2* Y, long long sY, cons
 
 int site_pairs(int n, int norb, int npy, int npz, int batch, const double2* Y, long long sY, const double2* X,
                long long sX, double2* P, double2* Py, double2* Pz, long long sP, cudaStream_t st) {
-  if (norb > 4 || n != norb * npy * npz) return NEGF_EINVAL;
+  if (norb < 1 || norb > 8 || n != norb * npy * npz) return NEGF_EINVAL;
   dim3 grid((n + SB_ROWS - 1) / SB_ROWS, batch);
-  site_pairs_kernel<<<grid, SB_ROWS * SB_KSPLIT, 0, st>>>(n, norb, npy, npz, Y, sY, X, sX, P, Py, Pz, sP);
+  if (norb <= 4)
+    site_pairs_kernel<4><<<grid, SB_ROWS * SB_KSPLIT, 0, st>>>(n, norb, npy, npz, Y, sY, X, sX, P, Py, Pz, sP);
+  else
+    site_pairs_kernel<8><<<grid, SB_ROWS * SB_KSPLIT, 0, st>>>(n, norb, npy, npz, Y, sY, X, sX, P, Py, Pz, sP);
   NEGF_CUDA_TRY(cudaGetLastError());
   count_launch();
   return NEGF_OK;
 }
 
 int bond_currents(const CurrentArgs& a, cudaStream_t st) {
-  if (a.norb > 4 || a.nf < 8) return NEGF_EINVAL;
+  if (a.norb > 8 || a.nh < 1 || a.nh > a.norb || a.nf < 8) return NEGF_EINVAL;
   const int total = a.npx * a.npy * a.npz;
   dim3 grid((total + 127) / 128, a.batch);
   bond_currents_kernel<<<grid, 128, 0, st>>>(a);
@@ -689,10 +775,37 @@ int bond_currents(const CurrentArgs& a, cudaStream_t st) {
 }
 
 int orbital_resolved(const CurrentArgs& a, int nslots, cudaStream_t st) {
-  if (a.norb > 4 || !a.or_acc || nslots < 1) return NEGF_EINVAL;
+  if (a.norb > 8 || a.nh < 1 || a.nh > a.norb || !a.or_acc || nslots < 1) return NEGF_EINVAL;
   const long long work = (long long)a.npx * a.npy * a.npz * (3 * a.norb * a.norb + a.norb);
   dim3 grid((unsigned)((work + 255) / 256), nslots);
   orbital_resolved_kernel<<<grid, 256, 0, st>>>(a);
+  NEGF_CUDA_TRY(cudaGetLastError());
+  count_launch();
+  return NEGF_OK;
+}
+
+int contact_fill(int n, int no, int nh, int type, int ndiag, int njobs, const double2* coef, const ContactGds& g,
+                 double2* sigL, double2* sigR, long long sS, cudaStream_t st) {
+  if (njobs < 1) return NEGF_OK;
+  contact_fill_kernel<<<ew_grid(2LL * n * n, njobs), EW_THREADS, 0, st>>>(n, no, nh, type, ndiag, coef, g, sigL, sigR,
+                                                                          sS);
+  NEGF_CUDA_TRY(cudaGetLastError());
+  count_launch();
+  return NEGF_OK;
+}
+
+int site_diag(int n, int no, int batch, const double2* X, long long sX, double2* out, long long sO, cudaStream_t st) {
+  const long long work = (long long)n * no;
+  site_diag_kernel<<<dim3((unsigned)((work + 255) / 256), batch), 256, 0, st>>>(n, no, X, sX, out, sO);
+  NEGF_CUDA_TRY(cudaGetLastError());
+  count_launch();
+  return NEGF_OK;
+}
+
+int josephson(int n, int no, int batch, const Item* items, const double2* P1, const double2* P2, long long sP,
+              const double2* G11, long long sG, const double2* sig, const double2* gam, long long sS, double* out,
+              cudaStream_t st) {
+  josephson_kernel<<<batch, EW_THREADS, 0, st>>>(n, no, items, P1, P2, sP, G11, sG, sig, gam, sS, out);
   NEGF_CUDA_TRY(cudaGetLastError());
   count_launch();
   return NEGF_OK;

@@ -30,6 +30,10 @@ MODULE negf_gpu_shim
         INTEGER(C_INT32_T) :: residual_slices, sr_slices, calc_currents
         INTEGER(C_INT32_T) :: reserved(3)
         REAL(C_DOUBLE)     :: spin_ops(2, 4, 4, 3)   ! C order [3][4][4][2]
+        INTEGER(C_INT32_T) :: contact_type, reserved1
+        REAL(C_DOUBLE)     :: tunneling_rate, delta_sc(2), chi_lr
+        REAL(C_DOUBLE)     :: gds(2, 4, 4)           ! C order [4][4][2]
+        INTEGER(C_INT32_T) :: reserved2(8)
     END TYPE
 
     TYPE(C_PTR), SAVE :: negf_h = C_NULL_PTR
@@ -113,6 +117,12 @@ CONTAINS
             p%mixed_slices = 0; p%keep_g_columns = 0; p%reserved = 0
             p%residual_slices = 0; p%sr_slices = 0; p%calc_currents = 1
             p%spin_ops = 0D0
+            ! contacts (Source/Read_In_Allocate.F90:19,69-76); gds = 0 selects the model's gDS
+            p%contact_type = contactType; p%reserved1 = 0; p%reserved2 = 0
+            p%tunneling_rate = 1D0; p%delta_sc = 0D0; p%chi_lr = 0D0; p%gds = 0D0
+            IF (contactType == 3) THEN
+                p%delta_sc(1) = DeltaSCL; p%delta_sc(2) = DeltaSCR; p%chi_lr = chiLR
+            ENDIF
             st = negf_create(p, negf_h)
             IF (st /= 0) STOP "negf_create failed"
         ENDIF

@@ -200,3 +200,24 @@ def build_from_model(npx, npy, npz, model):
     idx = np.arange(m)
     htotd[:, idx, idx] = (htotd[:, idx, idx].real + diag) + 1j * htotd[:, idx, idx].imag
     return htotd, hopx
+
+
+def bdg(htotd, hopx, npy, npz, nh=NORB):
+    """BdG form of a wire for superconducting contacts: every nh x nh site-pair block H_e
+    of Htotd and HopX becomes [[H_e, 0], [0, -conj(H_e)]] on 2 nh orbitals per site, electron
+    orbitals first (Source/Read_In_Allocate.F90:69-71, Build_Hamiltonian.F90:52-56,
+    162-163, 199-200).  Returns (htotd[npx, 2M, 2M], hopx[2M, 2M])."""
+    htotd = np.asarray(htotd, dtype=np.complex128)
+    hopx = np.asarray(hopx, dtype=np.complex128)
+    nsite = npy * npz
+    no = 2 * nh
+    e_idx = (np.arange(nsite)[:, None] * no + np.arange(nh)[None, :]).ravel()   # electron rows
+    h_idx = e_idx + nh                                                           # their holes
+    m2 = nsite * no
+
+    def one(blk):
+        out = np.zeros((m2, m2), dtype=np.complex128)
+        out[np.ix_(e_idx, e_idx)] = blk
+        out[np.ix_(h_idx, h_idx)] = -np.conj(blk)
+        return out
+    return np.stack([one(b) for b in htotd]), one(hopx)

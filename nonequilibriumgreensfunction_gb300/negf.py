@@ -44,7 +44,13 @@ def _to_fortran_blocks(htotd):
 class Solver:
     def __init__(self, npx, npy, npz, norb=4, n_hamiltonians=1, max_batch=1, eta=1e-4, sr_tol=1e-8,
                  sr_max_iter=20000, calc_spin=False, precision="fp64", device=0, keep_g_columns=False,
-                 spin_ops=None, mixed_slices=0, residual_slices=0, sr_slices=0, calc_currents=False):
+                 spin_ops=None, mixed_slices=0, residual_slices=0, sr_slices=0, calc_currents=False,
+                 contact_type=0, tunneling_rate=1.0, delta_sc=(1e-3, 1e-3), chi_lr=0.8, gds=None):
+        """``contact_type`` is the reference's contactType: 0 semi-infinite leads, 1 / 2
+        phenomenological contacts, 3 superconducting contacts on a BdG Hamiltonian (norb =
+        2 x the electron orbitals; see hamiltonian.bdg).  ``tunneling_rate``, ``delta_sc``
+        (DeltaSCL, DeltaSCR), ``chi_lr`` and ``gds`` (None = the four-orbital model's) are
+        the contact parameters of Read_In_Allocate.F90:69-76,199-202."""
         self.lib = capi.load()
         p = NegfParams()
         p.npx, p.npy, p.npz, p.norb = npx, npy, npz, norb
@@ -58,13 +64,25 @@ class Solver:
         p.sr_slices = sr_slices
         p.keep_g_columns = 1 if keep_g_columns else 0
         p.calc_currents = 1 if calc_currents else 0
+        nh = norb // 2 if contact_type == capi.NEGF_CONTACT_SC else norb
         if spin_ops is not None:
             ops = np.asarray(spin_ops, dtype=np.complex128)
             buf = np.zeros((3, 4, 4, 2))
-            buf[:, :norb, :norb, 0] = ops.real
-            buf[:, :norb, :norb, 1] = ops.imag
+            buf[:, :nh, :nh, 0] = ops.real
+            buf[:, :nh, :nh, 1] = ops.imag
             for i, v in enumerate(buf.ravel()):
                 p.spin_ops[i] = v
+        p.contact_type = contact_type
+        p.tunneling_rate = tunneling_rate
+        p.delta_sc[0], p.delta_sc[1] = delta_sc
+        p.chi_lr = chi_lr
+        if gds is not None:
+            g = np.asarray(gds, dtype=np.complex128)
+            buf = np.zeros((4, 4, 2))
+            buf[:g.shape[0], :g.shape[1], 0] = g.real
+            buf[:g.shape[0], :g.shape[1], 1] = g.imag
+            for i, v in enumerate(buf.ravel()):
+                p.gds[i] = v
         self.params = p
         self.npx, self.npy, self.npz, self.norb = npx, npy, npz, norb
         self.M = norb * npy * npz
@@ -72,6 +90,8 @@ class Solver:
         self.n_hamiltonians = n_hamiltonians
         self.calc_spin = bool(calc_spin)
         self.calc_currents = bool(calc_currents)
+        self.contact_type = contact_type
+        self.nh = nh
         h = ctypes.c_void_p()
         check(self.lib.negf_create(ctypes.byref(p), ctypes.byref(h)), "negf_create")
         self._h = h

@@ -15,6 +15,7 @@ reference calls through MKL), the reference's per-energy path:
     Source/Calculate_Gnp.F90:1-136          calculate_gnp()
     Source/Calculate_Observables.F90:2-169  calculate_observables()
     Source/Build_Hamiltonian.F90:1-207      build_hamiltonian_reference() (model 0 only)
+    Source/Build_Hamiltonian.F90:52-56,162-163,199-200   bdg_hamiltonian()
     Source/Read_In_Allocate.F90:161-197     gamma matrices
 
 The algorithm follows the reference step by step: the backward GRd/GRu/GRl recursion
@@ -65,6 +66,13 @@ def reference_gamma_matrices():
     gMy = np.array([[c0, -ci, c0, c0], [ci, c0, c0, c0], [c0, c0, c0, -ci], [c0, c0, ci, c0]])
     gMz = np.diag([c1, -c1, c1, -c1])
     return g0, g1, g2, g3, gMx, gMy, gMz
+
+
+def reference_gds():
+    """gDS, the pairing structure of the superconducting contacts for Nh == 4
+    (Read_In_Allocate.F90:199-202)."""
+    c0, c1 = 0j, 1 + 0j
+    return np.array([[c0, c1, c0, c0], [-c1, c0, c0, c0], [c0, c0, c0, c1], [c0, c0, -c1, c0]])
 
 
 # ---------------------------------------------------------------------------
@@ -147,6 +155,25 @@ def build_hamiltonian_reference(npx, npy, npz, a0=1.0, mu_t=0.0, ab_phi=0.0, bcy
     return htotd, hopx
 
 
+def bdg_hamiltonian(htotd, hopx, npy, npz, nh=4):
+    """The BdG form of an Nh-orbital Hamiltonian for superconducting contacts
+    (Read_In_Allocate.F90:69-71: Norb = 2 Nh): every Nh x Nh site-pair block H_e of Htotd
+    and HopX becomes the Norb x Norb block [[H_e, 0], [0, -conj(H_e)]]
+    (Build_Hamiltonian.F90:52-56 for the unit-cell blocks, :162-163 after an impurity,
+    :199-200 after the Aharonov-Bohm phase).  Site blocks keep the in-slice order
+    orb + y Norb + z Npy Norb with the electron orbitals first."""
+    nsite = npy * npz
+    no = 2 * nh
+
+    def conv(blk):
+        e = blk.reshape(nsite, nh, nsite, nh)
+        out = np.zeros((nsite, no, nsite, no), dtype=complex)
+        out[:, :nh, :, :nh] = e
+        out[:, nh:, :, nh:] = -np.conj(e)
+        return out.reshape(nsite * no, nsite * no)
+    return np.stack([conv(b) for b in htotd]), conv(hopx)
+
+
 # ---------------------------------------------------------------------------
 # Options (reference quirks as switches)
 # ---------------------------------------------------------------------------
@@ -159,6 +186,19 @@ class SolveOptions:
     kT: float = 0.0                          # 0 -> T=0 step, Source/Energy_Sweep.F90:11-21
     calc_spin: bool = False                  # calcSigExp, Source/Read_In_Allocate.F90:93
     norb: int = 4
+    # contactType (Source/Read_In_Allocate.F90:19): 0 semi-infinite leads, 1/2 phenomenological
+    # (Contact_Self_Energy.F90:19-28), 3 superconducting with a BdG Hamiltonian (:29-67)
+    contact_type: int = 0
+    tunneling_rate: float = 1.0              # Contact_Self_Energy.F90:10
+    delta_sc: tuple = (1e-3, 1e-3)           # DeltaSCL, DeltaSCR, Read_In_Allocate.F90:74-75
+    chi_lr: float = 0.8                      # Read_In_Allocate.F90:72
+    gds: Optional[np.ndarray] = None         # None -> reference_gds()
+
+    @property
+    def nh(self) -> int:
+        """Electron orbitals per site: Norb, or half of it for the BdG Hamiltonian
+        (Read_In_Allocate.F90:67-71)."""
+        return self.norb // 2 if self.contact_type == 3 else self.norb
 
 
 def fermi(energy: float, mu_c: float, kT: float) -> float:
@@ -231,22 +271,66 @@ def sancho_rubio(alpha: np.ndarray, beta: np.ndarray, eta: float, tol: float, ma
 # ---------------------------------------------------------------------------
 # Contact_Self_Energy (contactType 0), Source/Contact_Self_Energy.F90:1-106
 # ---------------------------------------------------------------------------
-def contact_self_energy(htotd, hopx, energy, opt: SolveOptions):
-    """Returns dict with SigmaL, SigmaR, GammaL, GammaR, dosc (2,), sr_err (2,), sr_iters (2,)."""
+def contact_self_energy(htotd, hopx, energy, opt: SolveOptions, npy=None):
+    """Returns dict with SigmaL, SigmaR, GammaL, GammaR, dosc (2,), sr_err (2,), sr_iters (2,).
+    ``npy`` is needed by contact type 2 only."""
     npx, m, _ = htotd.shape
     ident = np.eye(m, dtype=complex)
     ce = complex(energy, opt.eta)                           # :16
+    if opt.contact_type in (1, 2, 3):
+        if opt.contact_type == 2 and npy is None:
+            raise ValueError("contact type 2 needs npy")
+        sig_l, sig_r = model_contact_self_energy(m, npy, ce, opt)
+        return _finish_contacts(sig_l, sig_r, np.zeros(2, dtype=int), np.zeros(2, dtype=int))
     alpha = -htotd[0] + ident * ce                          # :71-74
     sig_l, err_l, it_l = sancho_rubio(alpha, -hopx.conj().T, opt.eta, opt.sr_tol, opt.sr_max_iter)
     alpha = -htotd[npx - 1] + ident * ce                    # :83-86
     sig_r, err_r, it_r = sancho_rubio(alpha, -hopx, opt.eta, opt.sr_tol, opt.sr_max_iter)
     if sig_l is None or sig_r is None:
         raise FloatingPointError("Sancho_Rubio produced NaN")
+    return _finish_contacts(sig_l, sig_r, np.array([err_l, err_r]), np.array([it_l, it_r]))
+
+
+def _finish_contacts(sig_l, sig_r, err, iters):
     dosc = np.array([-np.imag(np.trace(sig_l)) / PI, -np.imag(np.trace(sig_r)) / PI])  # :94-97
     gam_l = 1j * (sig_l - sig_l.conj().T)                   # :100
     gam_r = 1j * (sig_r - sig_r.conj().T)                   # :101
-    return dict(SigmaL=sig_l, SigmaR=sig_r, GammaL=gam_l, GammaR=gam_r, dosc=dosc,
-                sr_err=np.array([err_l, err_r]), sr_iters=np.array([it_l, it_r]))
+    return dict(SigmaL=sig_l, SigmaR=sig_r, GammaL=gam_l, GammaR=gam_r, dosc=dosc, sr_err=err, sr_iters=iters)
+
+
+def model_contact_self_energy(m, npy, ce, opt: SolveOptions):
+    """Self-energies of the contact models that need no decimation
+    (Contact_Self_Energy.F90:19-67); ce = E + i eta_sigma (:16).
+      1: -i rate on every orbital of the end slice (:19-23);
+      2: the same on the first NN = Npy*Norb orbitals only (:24-28);
+      3: superconducting contacts on a BdG Hamiltonian, the same Norb x Norb block on every
+         site (:29-67): omega = 1/sqrt(DeltaSCL^2 - ce^2) (the right contact also uses
+         DeltaSCL here, :49), -rate omega ce on both diagonal Nh x Nh blocks,
+         rate omega (+-Delta) gDS off the diagonal, times exp(+-i chi) on the left contact
+         only."""
+    rate = opt.tunneling_rate
+    if opt.contact_type in (1, 2):
+        sig = np.zeros((m, m), dtype=complex)
+        k = m if opt.contact_type == 1 else npy * opt.norb
+        sig[np.arange(k), np.arange(k)] = -1j * rate
+        return sig, sig.copy()
+    nh, no = opt.nh, opt.norb
+    gds = reference_gds() if opt.gds is None else np.asarray(opt.gds, dtype=complex)
+    ident = np.eye(nh, dtype=complex)
+    out = []
+    for side in (0, 1):
+        omega = 1.0 / np.sqrt(complex(opt.delta_sc[0]) ** 2 - ce ** 2)      # :33, :49
+        m_alpha = -rate * omega * ce                                         # :35, :51
+        d_up = rate * omega * opt.delta_sc[side]                             # :36, :52
+        d_lo = rate * omega * (-opt.delta_sc[side])                          # :37, :53
+        ph = np.exp(1j * opt.chi_lr) if side == 0 else 1.0                   # :43-44
+        blk = np.zeros((no, no), dtype=complex)
+        blk[:nh, :nh] = m_alpha * ident                                      # :40-41
+        blk[nh:, nh:] = m_alpha * ident
+        blk[:nh, nh:] = d_up * gds * ph                                      # :43
+        blk[nh:, :nh] = d_lo * gds * np.conj(ph)                             # :44
+        out.append(np.kron(np.eye(m // no), blk))                            # :63-67
+    return out[0], out[1]
 
 
 # ---------------------------------------------------------------------------
@@ -331,39 +415,58 @@ def site_density(gd, npy, npz, norb=4):
 
 
 # ---------------------------------------------------------------------------
-# Calculate_Observables, Source/Calculate_Observables.F90:2-169 (non-BdG branch)
+# Calculate_Observables, Source/Calculate_Observables.F90:2-169
 # ---------------------------------------------------------------------------
 def calculate_observables(gnp, grrgt, gam_l, gam_r, htotd, hopx, f1, f2, de, npy, npz,
-                          calc_spin=False, calc_currents=True, norb=4, calc_resolved=False):
+                          calc_spin=False, calc_currents=True, norb=4, calc_resolved=False, nh=None,
+                          bdg=False, sig_l=None, grd1=None):
+    """``nh``: electron orbitals per site (Norb, or Norb/2 on a BdG Hamiltonian); the spin,
+    EDensity/HDensity and current sums run over them only, as the reference's loops do.
+    ``bdg``: the supercurrent transmission (:60-81) from Gnd(:,:,1), SigmaL, GRd(:,:,1) =
+    ``grd1`` and GammaL instead of the Landauer trace."""
     npx = htotd.shape[0]
     nn = npy * norb
+    nh = norb if nh is None else nh
+    nsite = npy * npz
     res = {}
     gnd, gpd = gnp["Gnd"], gnp["Gpd"]
     _, _, _, _, gmx, gmy, gmz = reference_gamma_matrices()
     if calc_spin:                                           # :10-30
-        # site blocks Gnd(idx+ii, idx+jj) with idx = y*Norb + z*NN, summed against gM(jj, ii)
-        nsite = npy * npz
+        # site blocks Gnd(idx+ii, idx+jj), ii, jj <= Nh, idx = y*Norb + z*NN, against gM(jj, ii)
         blocks = gnd.reshape(npx, nsite, norb, nsite, norb)
-        diag_blocks = blocks[:, np.arange(nsite), :, np.arange(nsite), :]   # (nsite, npx, norb, norb)
+        diag_blocks = blocks[:, np.arange(nsite), :nh, np.arange(nsite), :nh]   # (nsite, npx, nh, nh)
         sig = np.zeros((3, npx, npy, npz))
         for j, gm in enumerate((gmx, gmy, gmz)):
-            v = de / (2.0 * PI) * np.real(np.einsum("sxab,ba->xs", diag_blocks, gm))
+            v = de / (2.0 * PI) * np.real(np.einsum("sxab,ba->xs", diag_blocks, gm[:nh, :nh]))
             sig[j] = v.reshape(npx, npz, npy).transpose(0, 2, 1)
         res["SigExp"] = sig
-    # :33-43 electron/hole DOS at this energy
-    res["EDensity"] = float(np.real(np.trace(gnd, axis1=1, axis2=2)).sum() / (2.0 * PI))
-    res["HDensity"] = float(np.real(np.trace(gpd, axis1=1, axis2=2)).sum() / (2.0 * PI))
+    # :33-43 electron/hole DOS at this energy (orbitals ii <= Nh of every site)
+    dn = np.real(np.diagonal(gnd, axis1=1, axis2=2)).reshape(npx, nsite, norb)[:, :, :nh]
+    dp = np.real(np.diagonal(gpd, axis1=1, axis2=2)).reshape(npx, nsite, norb)[:, :, :nh]
+    res["EDensity"] = float(dn.sum() / (2.0 * PI))
+    res["HDensity"] = float(dp.sum() / (2.0 * PI))
     # :46-53 injected modes
     res["Modec1"] = float(np.real(np.sum(gam_l * (gnd[0] + gpd[0]).T)))
     res["Modec2"] = float(np.real(np.sum(gam_r * (gnd[npx - 1] + gpd[npx - 1]).T)))
-    # :85-100 transmission
-    g1n = grrgt[0]
-    cmat1 = gam_l @ g1n
-    cmat2 = gam_r @ g1n.conj().T
-    t12 = float(np.real(np.sum(cmat1 * cmat2.T)))
-    res["T12"] = t12
-    res["ContactCurrent"] = np.array([Q_E * de / H_PLANCK * (t12 * (f2 - f1)),
-                                      Q_E * de / H_PLANCK * (t12 * (f1 - f2))])  # :102-103
+    if bdg:
+        # :60-81 supercurrent transmission, PRB 62, 648 (2000) Eq. 14:
+        # cmat1 = (i Gnd(:,:,1)) SigmaL^H, cmat2 = GRd(:,:,1) (-GammaL),
+        # T12 = sum_ii sigma_z(ii) Re (cmat1 + cmat2)(ii, ii), +1 on electron orbitals
+        cmat1 = (1j * gnd[0]) @ sig_l.conj().T
+        cmat2 = grd1 @ (-gam_l)
+        sz = np.where(np.arange(gnd.shape[1]) % norb < norb // 2, 1.0, -1.0)
+        t12 = float(np.sum(sz * np.real(np.diagonal(cmat1 + cmat2))))
+        res["T12"] = t12
+        res["ContactCurrent"] = np.array([Q_E * de / H_PLANCK * t12, Q_E * de / H_PLANCK * (-t12)])  # :79-80
+    else:
+        # :85-100 transmission
+        g1n = grrgt[0]
+        cmat1 = gam_l @ g1n
+        cmat2 = gam_r @ g1n.conj().T
+        t12 = float(np.real(np.sum(cmat1 * cmat2.T)))
+        res["T12"] = t12
+        res["ContactCurrent"] = np.array([Q_E * de / H_PLANCK * (t12 * (f2 - f1)),
+                                          Q_E * de / H_PLANCK * (t12 * (f1 - f2))])  # :102-103
     if calc_currents and "Gnu" in gnp:                      # :110-169, dumVar is REAL(4)
         j = np.zeros((3, npx, npy, npz))                    # Jx, Jy, Jz
         er = np.zeros((3, npx, npy, npz))                   # ERJx/y/z at this energy (:124-157)
@@ -376,14 +479,14 @@ def calculate_observables(gnp, grrgt, gam_l, gam_r, htotd, hopx, f1, f2, de, npy
             for yy in range(npy):
                 for zz in range(npz):
                     idx = yy * norb + zz * nn
-                    a = slice(idx, idx + norb)
+                    a = slice(idx, idx + nh)                # orbitals ii <= Nh (:114-115)
                     terms = [None, None, None]
                     if yy < npy - 1:
-                        b = slice(idx + norb, idx + 2 * norb)
+                        b = slice(idx + norb, idx + norb + nh)
                         terms[1] = (h[a, b] * gnd[xx][b, a].T - gnd[xx][a, b] * h[b, a].T
                                     - h[a, b] * gpd[xx][b, a].T + gpd[xx][a, b] * h[b, a].T)
                     if zz < npz - 1:
-                        b = slice(idx + nn, idx + nn + norb)
+                        b = slice(idx + nn, idx + nn + nh)
                         terms[2] = (h[a, b] * gnd[xx][b, a].T - gnd[xx][a, b] * h[b, a].T
                                     - h[a, b] * gpd[xx][b, a].T + gpd[xx][a, b] * h[b, a].T)
                     if xx < npx - 1:
@@ -396,7 +499,9 @@ def calculate_observables(gnp, grrgt, gam_l, gam_r, htotd, hopx, f1, f2, de, npy
                         dum = np.float32(np.real(pref * v)).astype(np.float64)   # [ii, jj]
                         j[d, xx, yy, zz] = np.sum(dum * w)
                         er[d, xx, yy, zz] = np.sum(dum)
-                        orj[d, xx, yy, zz] = (dum * w).ravel()
+                        pairs = np.zeros((norb, norb))
+                        pairs[:nh, :nh] = dum * w
+                        orj[d, xx, yy, zz] = pairs.ravel()
         res["Jx"], res["Jy"], res["Jz"] = j
         if calc_resolved:
             res["ERJx"], res["ERJy"], res["ERJz"] = er
@@ -423,7 +528,7 @@ def energy_sweep(htotd, hopx, energy, mu_lead, de, npy, npz, opt: SolveOptions,
     npx, m, _ = htotd.shape
     f1 = fermi(energy, mu_lead[0], opt.kT)
     f2 = fermi(energy, mu_lead[1], opt.kT)
-    cse = contact_self_energy(htotd, hopx, energy, opt)
+    cse = contact_self_energy(htotd, hopx, energy, opt, npy=npy)
     ident = np.eye(m, dtype=complex)
     inv_grd = -htotd + ident[None] * complex(energy, opt.eta)   # :31-36
     inv_grd[0] = inv_grd[0] - cse["SigmaL"]                     # :37
@@ -437,7 +542,8 @@ def energy_sweep(htotd, hopx, energy, mu_lead, de, npy, npz, opt: SolveOptions,
     out["RhoP"] = site_density(gnp["Gpd"], npy, npz, opt.norb) * (de / (2.0 * PI))
     obs = calculate_observables(gnp, rg["GRRgt"], cse["GammaL"], cse["GammaR"], htotd, hopx,
                                 f1, f2, de, npy, npz, calc_spin=opt.calc_spin,
-                                calc_currents=calc_currents, norb=opt.norb, calc_resolved=calc_resolved)
+                                calc_currents=calc_currents, norb=opt.norb, calc_resolved=calc_resolved,
+                                nh=opt.nh, bdg=opt.contact_type == 3, sig_l=cse["SigmaL"], grd1=rg["GRd"][0])
     out.update(obs)
     if calc_resolved:                                           # Calculate_Gnp.F90:125-129
         on = orbital_density(gnp["Gnd"], npy, npz, opt.norb)

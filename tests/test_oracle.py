@@ -215,3 +215,42 @@ def test_resolved_currents_decompose_the_totals():
     assert np.abs(r["ORRhon"].sum(axis=3) - r["RhoN"]).max() <= 1e-13 * np.abs(r["RhoN"]).max()
     diff = r["RhoN"] - r["RhoP"]
     assert np.abs(r["ERRhon"] * w - diff).max() <= 1e-12 * np.abs(diff).max()
+
+
+def test_bdg_builders_agree():
+    """The package's BdG conversion equals the oracle's restatement of the reference's BdG
+    blocks (Build_Hamiltonian.F90:52-56, 162-163, 199-200) on a disordered flux wire."""
+    npx, npy, npz = 3, 3, 2
+    h, x = HB.ti_wire(npx, npy, npz, W=0.3, seed=2, flux=0.4, zeeman=0.02)
+    hb, xb = HB.bdg(h, x, npy, npz)
+    ho, xo = O.bdg_hamiltonian(h, x, npy, npz, 4)
+    assert hb.shape == (npx, 8 * npy * npz, 8 * npy * npz)
+    assert np.array_equal(hb, ho) and np.array_equal(xb, xo)
+    assert np.abs(hb - hb.conj().transpose(0, 2, 1)).max() == 0.0
+
+
+def test_model_contact_self_energies():
+    """Contact types 1-3 (Contact_Self_Energy.F90:19-67): the phenomenological contacts give
+    -Im Tr Sigma / pi = rate x (number of contacted orbitals), and the superconducting
+    contacts give the BCS density of states rate M |E| / (pi sqrt(E^2 - Delta^2)) outside the
+    gap, a positive semidefinite Gamma, and Sigma_L = Sigma_R at chi = 0."""
+    npx, npy, npz = 2, 3, 2
+    h, x = HB.ti_wire(npx, npy, npz)
+    m = h.shape[1]
+    for ct, k in ((1, m), (2, npy * 4)):
+        c = O.contact_self_energy(h, x, 0.05, O.SolveOptions(contact_type=ct, tunneling_rate=0.7), npy=npy)
+        assert np.allclose(c["dosc"], 0.7 * k / O.PI, rtol=1e-14)
+        assert np.allclose(np.diag(c["GammaL"])[:k], 1.4) and np.all(np.diag(c["GammaL"])[k:] == 0)
+    hb, xb = O.bdg_hamiltonian(h, x, npy, npz, 4)
+    mb = hb.shape[1]
+    delta = 1e-3
+    for e in (-3e-3, -1.5e-3, 1.2e-3, 4e-3):
+        opt = O.SolveOptions(norb=8, contact_type=3, eta=1e-9, delta_sc=(delta, delta), chi_lr=0.8)
+        c = O.contact_self_energy(hb, xb, e, opt)
+        want = mb * abs(e) / (O.PI * np.sqrt(e * e - delta * delta))
+        assert np.allclose(c["dosc"], want, rtol=1e-6), (e, c["dosc"], want)
+        for g in (c["GammaL"], c["GammaR"]):
+            assert np.linalg.eigvalsh(g).min() >= -1e-9 * np.abs(g).max()
+    c = O.contact_self_energy(hb, xb, 0.4e-3, O.SolveOptions(norb=8, contact_type=3, chi_lr=0.0, eta=1e-9))
+    assert np.array_equal(c["SigmaL"], c["SigmaR"])
+    assert abs(c["dosc"][0]) < 1e-3 * mb                     # inside the gap: eta-broadened only
