@@ -126,6 +126,19 @@ __device__ __forceinline__ void tc_commit(uint64_t* bar) {
                : "memory");
 }
 
+// An integer-valued FP32 accumulator as an int, with integer operations only.  Every TMEM
+// accumulator holds a sum of products of 7-bit integers, |sum| <= S K' 2^12 < 2^31, and is
+// integer-valued even where it rounded (an FP32 of magnitude >= 2^24 is an even integer),
+// so value = mantissa * 2^(exponent - 150) is exact in an int.  The FP32 -> int64
+// conversion instruction would run on the FP64 pipe, which on this part issues about two
+// operations per clock per SM and otherwise bounds the epilogue.
+__device__ __forceinline__ int acc_to_int(uint32_t bits) {
+  const int e = (int)((bits >> 23) & 0xFFu) - 150;
+  const int mant = (int)((bits & 0x7FFFFFu) | 0x800000u);
+  const int mag = e >= 0 ? (mant << e) : (e > -24 ? (mant >> -e) : 0);
+  return (bits >> 31) ? -mag : mag;
+}
+
 // v * 2^scale as a double, rounded to nearest even, built from integer operations only
 // (results below the normal range flush to zero)
 __device__ __forceinline__ double scaled_int_to_double(long long v, int scale) {
@@ -536,7 +549,7 @@ __global__ void __launch_bounds__(TC_THREADS, MINB)
         for (int d = 0; d < S; ++d) {
 #pragma unroll
           for (int i = 0; i < CW; ++i) {
-            const long long q = (long long)__float2ll_rn(__uint_as_float(raw[d][i]));
+            const long long q = (long long)acc_to_int(raw[d][i]);
             if (d < DH) hi[i] += q * (1LL << (7 * (DH - 1 - d)));
             else lo[i] += q * (1LL << (7 * (S - 1 - d)));
           }
@@ -794,7 +807,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         for (int d = 0; d < S; ++d) {
 #pragma unroll
           for (int i = 0; i < CW; ++i) {
-            const long long q = (long long)__float2ll_rn(__uint_as_float(raw[d][i]));
+            const long long q = (long long)acc_to_int(raw[d][i]);
             if (d < DH) hi[i] += q * (1LL << (7 * (DH - 1 - d)));
             else lo[i] += q * (1LL << (7 * (S - 1 - d)));
           }
