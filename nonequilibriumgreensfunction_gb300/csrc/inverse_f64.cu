@@ -23,7 +23,10 @@ namespace {
 constexpr int PANEL_THREADS = 512;
 constexpr size_t kPanelSmemMax = 200 * 1024;
 
-__device__ __forceinline__ void argmax_combine(double& v, int& i, double v2, int i2) {
+// V is the real type of the matrix: the FP32 inverse compares floats, so its pivot search
+// stays off the FP64 pipe (comparing the floats orders them as their doubles would)
+template <typename V>
+__device__ __forceinline__ void argmax_combine(V& v, int& i, V v2, int i2) {
   // larger value wins; on ties the lower row index wins (izamax returns the first max)
   if (v2 > v || (v2 == v && i2 < i)) { v = v2; i = i2; }
 }
@@ -34,11 +37,11 @@ __global__ void __launch_bounds__(PANEL_THREADS) gj_panel_kernel(T* A, long long
                                                                  int* ipiv, int* info) {
   extern __shared__ __align__(16) unsigned char panel_raw[];
   T* Ps = reinterpret_cast<T*>(panel_raw);
-  __shared__ double red_v[PANEL_THREADS / 32];
+  using R = typename CplxTraits<T>::R;
+  __shared__ R red_v[PANEL_THREADS / 32];
   __shared__ int red_i[PANEL_THREADS / 32];
   __shared__ int s_piv;
   __shared__ T s_d;
-  using R = typename CplxTraits<T>::R;
   const int b = blockIdx.x;
   T* Ab = A + (long long)b * sA;
   int* ip = ipiv + (long long)b * n;
@@ -53,19 +56,19 @@ __global__ void __launch_bounds__(PANEL_THREADS) gj_panel_kernel(T* A, long long
     const int r = k0 + c;
     T* col = Ps + (long long)c * n;
     // ---- pivot search over rows r..n-1
-    double bv = -1.0;
+    R bv = -1;
     int bi = n;
-    for (int i = r + t; i < n; i += PANEL_THREADS) argmax_combine(bv, bi, (double)cabs1(col[i]), i);
+    for (int i = r + t; i < n; i += PANEL_THREADS) argmax_combine(bv, bi, (R)cabs1(col[i]), i);
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
-      double ov = __shfl_down_sync(0xffffffffu, bv, off);
+      R ov = __shfl_down_sync(0xffffffffu, bv, off);
       int oi = __shfl_down_sync(0xffffffffu, bi, off);
       argmax_combine(bv, bi, ov, oi);
     }
     if (lane == 0) { red_v[warp] = bv; red_i[warp] = bi; }
     __syncthreads();
     if (t == 0) {
-      double v = red_v[0];
+      R v = red_v[0];
       int i = red_i[0];
       for (int w = 1; w < PANEL_THREADS / 32; ++w) argmax_combine(v, i, red_v[w], red_i[w]);
       if (i >= n) i = r;

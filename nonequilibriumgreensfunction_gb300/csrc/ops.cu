@@ -23,6 +23,27 @@ __device__ __forceinline__ double2 hbe(const HopBD& h, int s, int a, int c) {
   return h.hb[((long long)s * h.norb + a) * h.norb + c];
 }
 
+// acc += a b (complex) with the same fma sequence as cfma, leaving out the terms whose
+// factor from b (cfma_sb) or a (cfma_sa) is an exact zero.  The HopX site blocks of the
+// wire models are half zeros and their nonzeros purely real or imaginary, so this takes a
+// quarter of the FP64 fmas; a skipped term fma(x, 0, acc) would have returned acc, so the
+// sums are unchanged (up to the sign of an exact zero).  When every site has the same
+// block, the branches are uniform across a warp.
+__device__ __forceinline__ void cfma_sb(double2& acc, double2 a, double2 b) {
+  if (b.x != 0.0) acc.x = fma(a.x, b.x, acc.x);
+  if (b.y != 0.0) {
+    acc.x = fma(-a.y, b.y, acc.x);
+    acc.y = fma(a.x, b.y, acc.y);
+  }
+  if (b.x != 0.0) acc.y = fma(a.y, b.x, acc.y);
+}
+__device__ __forceinline__ void cfma_sa(double2& acc, double2 a, double2 b) {
+  if (a.x != 0.0) acc.x = fma(a.x, b.x, acc.x);
+  if (a.y != 0.0) acc.x = fma(-a.y, b.y, acc.x);
+  if (a.x != 0.0) acc.y = fma(a.x, b.y, acc.y);
+  if (a.y != 0.0) acc.y = fma(a.y, b.x, acc.y);
+}
+
 // ---- W assembly (Energy_Sweep.F90:31-38 + Recursive_Greens.F90:18-20 / :70-72) ----------
 __global__ void form_w_kernel(FormW a) {
   const int b = blockIdx.y;
@@ -69,8 +90,9 @@ __global__ void form_w_kernel(FormW a) {
 // The same W when HopX is block diagonal with 4 x 4 site blocks: one thread per 4 x 4 site
 // block (si, sj) of W.  The coupling term of the block is L_si G(si, sj) R_sj (side 0:
 // L = H^H, R = H; side 1: L = H, R = H^H), formed as T = G R and then L T: 8 complex FMAs
-// per element instead of the 20 of the element-wise form.  GB300's FP64 pipe runs at 1/64
-// of its FP32 rate, so this FP64 arithmetic, not memory, bounds the kernel.  Each thread
+// per element instead of the 20 of the element-wise form, and a quarter of those with the
+// zero terms of the hop blocks left out.  GB300's FP64 pipe runs at 1/64 of its FP32 rate,
+// so this FP64 arithmetic, not memory, bounds the kernel.  Each thread
 // reads and writes its block as four 64-byte column pieces; consecutive threads take
 // consecutive row blocks, so a warp's accesses to a column are contiguous.
 __global__ void form_w_blocks_kernel(FormW a) {
@@ -103,7 +125,7 @@ __global__ void form_w_blocks_kernel(FormW a) {
       for (int r = 0; r < 4; ++r) {
         double2 acc = make_double2(0.0, 0.0);
 #pragma unroll
-        for (int q = 0; q < 4; ++q) cfma(acc, g[r][q], rc[q]);
+        for (int q = 0; q < 4; ++q) cfma_sb(acc, g[r][q], rc[q]);
         tm[r][c] = acc;
       }
     }
@@ -115,7 +137,7 @@ __global__ void form_w_blocks_kernel(FormW a) {
         double2 acc = make_double2(0.0, 0.0);
 #pragma unroll
         for (int p = 0; p < 4; ++p)   // L(r, p): side 0: L = H^H, side 1: L = H
-          cfma(acc, a.side == 0 ? cconj(hbe(a.hop, si, p, r)) : hbe(a.hop, si, r, p), tm[p][c]);
+          cfma_sa(acc, a.side == 0 ? cconj(hbe(a.hop, si, p, r)) : hbe(a.hop, si, r, p), tm[p][c]);
         const long long e = e0 + r;
         double2 v = make_double2(-Hx[e].x, -Hx[e].y);
         if (si == sj && r == c) { v.x += it.energy; v.y += a.eta; }
@@ -946,29 +968,46 @@ __global__ void to_f64_kernel(int n, const float2* src, long long sS, double2* d
 // R = I - T in place; rnorm[b] = max over rows of sum_j |R_ij| (the infinity norm, the
 // Newton-Schulz contraction factor).  A CTA covers 32 rows; its 8 thread rows stride over
 // the columns (coalesced) and the row sums are reduced in shared memory in fixed order.
+// |x| of a double as a float, truncated, from its bits with integer operations (below
+// the float range -> 0, above -> inf, NaN -> NaN): the residual norm only decides whether
+// a matrix takes more steps or an FP64 inverse, so float accuracy is enough, and the
+// conversion instruction would run on the FP64 pipe
+__device__ __forceinline__ float abs_to_float(double x) {
+  const unsigned long long a = (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFULL;
+  const int E = (int)(a >> 52) - 1023 + 127;
+  const unsigned int m = (unsigned int)(a >> 29) & 0x7FFFFFu;
+  if ((a >> 52) == 0x7FF) return __uint_as_float(0x7F800000u | (m ? 0x400000u : 0u));
+  if (E <= 0) return 0.0f;
+  if (E >= 255) return __uint_as_float(0x7F800000u);
+  return __uint_as_float(((unsigned int)E << 23) | m);
+}
+
 __global__ void ns_residual_kernel(int n, double2* T, long long sT, unsigned long long* rnorm) {
-  __shared__ double part[8][32];
+  __shared__ float part[8][32];
   const int b = blockIdx.y;
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int i = blockIdx.x * 32 + tx;
-  double s = 0.0;
+  float s = 0.0f;
   if (i < n) {
     double2* Tb = T + (long long)b * sT;
     for (int j = ty; j < n; j += 8) {
       double2 v = Tb[(long long)j * n + i];
-      v = make_double2((i == j ? 1.0 : 0.0) - v.x, -v.y);
+      // R = I - T: a subtraction on the diagonal only, a sign flip elsewhere
+      const double re = i == j ? 1.0 - v.x : __longlong_as_double(__double_as_longlong(v.x) ^ (long long)(1ULL << 63));
+      v = make_double2(re, __longlong_as_double(__double_as_longlong(v.y) ^ (long long)(1ULL << 63)));
       Tb[(long long)j * n + i] = v;
-      s += fabs(v.x) + fabs(v.y);
+      s += abs_to_float(v.x) + abs_to_float(v.y);
     }
   }
   part[ty][tx] = s;
   __syncthreads();
   if (ty == 0) {
     for (int q = 1; q < 8; ++q) s += part[q][tx];
-    if (isnan(s)) s = 1e300;
-    // warp max, then one atomicMax per CTA on the bit pattern (non-negative doubles order as integers)
-    for (int off = 16; off > 0; off >>= 1) s = fmax(s, __shfl_xor_sync(0xffffffffu, s, off));
-    if (tx == 0) atomicMax(rnorm + b, (unsigned long long)__double_as_longlong(s));
+    if (isnan(s)) s = 1e30f;
+    // warp max, then one atomicMax per CTA on the bit pattern of the double (non-negative
+    // doubles order as integers)
+    for (int off = 16; off > 0; off >>= 1) s = fmaxf(s, __shfl_xor_sync(0xffffffffu, s, off));
+    if (tx == 0) atomicMax(rnorm + b, (unsigned long long)__double_as_longlong((double)s));
   }
 }
 

@@ -241,31 +241,45 @@ __device__ __forceinline__ void slice_value(double x, int e, __nv_bfloat16 (&out
   }
 }
 
-__device__ __forceinline__ int scale_exponent(double m) {
-  if (!(m > 0.0) || isinf(m)) return 0;
-  int e;
-  frexp(m, &e);   // m = f 2^e, f in [0.5, 1)
-  return e;
+// Row and column maxima are taken on bit patterns: |x| as an unsigned integer orders like
+// |x| itself, NaN maps to 0 as fmax would ignore it, and the exponent of the maximum is
+// read from its bits -- all integer operations, none on GB300's slow FP64 pipe.
+__device__ __forceinline__ unsigned long long abs_bits(double x) {
+  const unsigned long long a = (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFULL;
+  return a > 0x7FF0000000000000ULL ? 0ULL : a;
+}
+
+// e with m = f 2^e, f in [0.5, 1) (frexp), for m = the double with bit pattern a >= 0;
+// 0 for zero and infinity
+__device__ __forceinline__ int scale_exponent(unsigned long long a) {
+  const int E = (int)(a >> 52);
+  if (a == 0 || E == 0x7FF) return 0;
+  if (E == 0) {   // subnormal maximum: its row slices to zero whatever e is
+    int e;
+    frexp(__longlong_as_double((long long)a), &e);
+    return e;
+  }
+  return E - 1022;
 }
 
 // row exponents of A (M x K complex, column-major): a CTA covers 32 rows, its 8 thread
 // rows stride over the columns (coalesced 512-byte row segments), reduced in shared memory
 __global__ void row_exp_kernel(const double2* A, int lda, long long sA, int m, int k, int* ea) {
-  __shared__ double part[8][32];
+  __shared__ unsigned long long part[8][32];
   const int b = blockIdx.y;
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int i = blockIdx.x * 32 + tx;
   const double2* Ab = A + (long long)b * sA;
-  double mx = 0.0;
+  unsigned long long mx = 0;
   if (i < m)
     for (int kk = ty; kk < k; kk += 8) {
       const double2 v = Ab[(long long)kk * lda + i];
-      mx = fmax(mx, fmax(fabs(v.x), fabs(v.y)));
+      mx = max(mx, max(abs_bits(v.x), abs_bits(v.y)));
     }
   part[ty][tx] = mx;
   __syncthreads();
   if (ty == 0 && i < m) {
-    for (int q = 1; q < 8; ++q) mx = fmax(mx, part[q][tx]);
+    for (int q = 1; q < 8; ++q) mx = max(mx, part[q][tx]);
     ea[(long long)b * m + i] = scale_exponent(mx);
   }
 }
@@ -325,10 +339,10 @@ __global__ void __launch_bounds__(256) slice_b_kernel(const double2* B, int ldb,
   const int j = blockIdx.x * 8 + warp;
   if (j >= n) return;   // whole warps leave together; no block-wide barrier below
   const double2* col = B + (long long)b * sB + (long long)j * ldb;
-  double mx = 0.0;
-  for (int kk = lane; kk < k; kk += 32) mx = fmax(mx, fmax(fabs(col[kk].x), fabs(col[kk].y)));
+  unsigned long long mx = 0;
+  for (int kk = lane; kk < k; kk += 32) mx = max(mx, max(abs_bits(col[kk].x), abs_bits(col[kk].y)));
 #pragma unroll
-  for (int off = 16; off > 0; off >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+  for (int off = 16; off > 0; off >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, off));
   const int e = scale_exponent(mx);
   if (lane == 0) fb[(long long)b * n + j] = e;
   const long long n2 = 2LL * n;
