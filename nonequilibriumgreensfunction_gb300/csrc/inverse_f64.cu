@@ -182,29 +182,50 @@ __global__ void __launch_bounds__(SWAP_WARPS * 32) gj_swap_kernel(T* A, long lon
 // panel [k0, k0 + kb), P = A(:, k0:k0+kb) (n x kb), R (kb x n) from gj_swap.  K = kb <= 32,
 // so each CTA stages its whole P and R slabs in shared memory with one barrier and then
 // runs the kb rank-1 steps from there: 80 x 80 output tiles, 256 threads of 5 x 5 complex
-// accumulators (25 FMAs per 10 shared loads).  The k order and the final A + sum equal
-// those of the general GEMM kernel, so results are bitwise the same.
-constexpr int UPD_T = 80, UPD_R = 5;
+// accumulators (25 FMAs per 10 shared loads).  The R slab's rows are padded to 81 entries:
+// its loads walk k fastest, and an 80-entry stride would put every thread of a warp on the
+// same bank.  In the FP32 form the 25 values of A a thread updates are loaded before the k
+// loop, so their latency overlaps the slab loads and the FMAs instead of serialising 25
+// load/store round trips at the end (the FP64 form, with twice the registers per value,
+// loads them a column of five at a time).  The k order and the final A + sum equal those of
+// the general GEMM kernel, so results are bitwise the same.
+constexpr int UPD_T = 80, UPD_R = 5, UPD_RS = UPD_T + 1;
 template <typename T>
-__global__ void __launch_bounds__(256) gj_update_kernel(T* A, long long sA, int n, int k0, int kb, const T* R,
+__global__ void __launch_bounds__(256, sizeof(T) == 8 ? 2 : 1) gj_update_kernel(T* A, long long sA, int n, int k0, int kb, const T* R,
                                                         long long sR) {
   extern __shared__ __align__(16) unsigned char upd_raw[];
   T* Ps = reinterpret_cast<T*>(upd_raw);              // [kb][UPD_T]
-  T* Rs = Ps + 32 * UPD_T;                              // [kb][UPD_T]
+  T* Rs = Ps + 32 * UPD_T;                              // [kb][UPD_RS]
+  constexpr bool kPrefetch = sizeof(T) == 8;            // float2
   const int b = blockIdx.z;
   const int m0 = blockIdx.x * UPD_T, n0 = blockIdx.y * UPD_T;
   if (n0 >= k0 && n0 + UPD_T <= k0 + kb) return;        // tile inside the panel columns
   T* Ab = A + (long long)b * sA;
   const T* Rb = R + (long long)b * sR;
   const int t = threadIdx.x;
+  const int tx = t & 15, ty = t >> 4;
+  auto updated = [&](int i, int j) -> T* {              // nullptr: outside A or in the panel
+    const int row = m0 + tx + 16 * i, col = n0 + ty + 16 * j;
+    if (row >= n || col >= n || (col >= k0 && col < k0 + kb)) return nullptr;
+    return Ab + (long long)col * n + row;
+  };
+  T cin[kPrefetch ? UPD_R : 1][kPrefetch ? UPD_R : 1];
+  if constexpr (kPrefetch) {
+#pragma unroll
+    for (int j = 0; j < UPD_R; ++j)
+#pragma unroll
+      for (int i = 0; i < UPD_R; ++i) {
+        const T* cp = updated(i, j);
+        cin[i][j] = cp ? *cp : CplxTraits<T>::make(0, 0);
+      }
+  }
   for (int e = t; e < kb * UPD_T; e += 256) {
     const int k = e / UPD_T, i = e % UPD_T;
     Ps[k * UPD_T + i] = (m0 + i < n) ? Ab[(long long)(k0 + k) * n + m0 + i] : CplxTraits<T>::make(0, 0);
     const int j = e / kb, kk = e % kb;                  // R slab: contiguous kb x UPD_T
-    Rs[kk * UPD_T + j] = (n0 + j < n) ? Rb[(long long)(n0 + j) * kb + kk] : CplxTraits<T>::make(0, 0);
+    Rs[kk * UPD_RS + j] = (n0 + j < n) ? Rb[(long long)(n0 + j) * kb + kk] : CplxTraits<T>::make(0, 0);
   }
   __syncthreads();
-  const int tx = t & 15, ty = t >> 4;
   T acc[UPD_R][UPD_R];
 #pragma unroll
   for (int i = 0; i < UPD_R; ++i)
@@ -215,7 +236,7 @@ __global__ void __launch_bounds__(256) gj_update_kernel(T* A, long long sA, int 
 #pragma unroll
     for (int i = 0; i < UPD_R; ++i) av[i] = Ps[k * UPD_T + tx + 16 * i];
 #pragma unroll
-    for (int j = 0; j < UPD_R; ++j) bv[j] = Rs[k * UPD_T + ty + 16 * j];
+    for (int j = 0; j < UPD_R; ++j) bv[j] = Rs[k * UPD_RS + ty + 16 * j];
 #pragma unroll
     for (int i = 0; i < UPD_R; ++i)
 #pragma unroll
@@ -223,14 +244,20 @@ __global__ void __launch_bounds__(256) gj_update_kernel(T* A, long long sA, int 
   }
 #pragma unroll
   for (int j = 0; j < UPD_R; ++j) {
-    const int col = n0 + ty + 16 * j;
-    if (col >= n || (col >= k0 && col < k0 + kb)) continue;
+    T c[UPD_R];
+    if constexpr (!kPrefetch) {   // the column's five loads before its five stores
+#pragma unroll
+      for (int i = 0; i < UPD_R; ++i) {
+        const T* cp = updated(i, j);
+        c[i] = cp ? *cp : CplxTraits<T>::make(0, 0);
+      }
+    }
 #pragma unroll
     for (int i = 0; i < UPD_R; ++i) {
-      const int row = m0 + tx + 16 * i;
-      if (row >= n) continue;
-      T* cp = Ab + (long long)col * n + row;
-      *cp = cadd(acc[i][j], *cp);
+      T* cp = updated(i, j);
+      if (!cp) continue;
+      if constexpr (kPrefetch) *cp = cadd(acc[i][j], cin[i][j]);
+      else *cp = cadd(acc[i][j], c[i]);
     }
   }
 }
@@ -297,7 +324,7 @@ int gj_invert(T* A, long long sA, int n, int batch, InvWork& w, cudaStream_t st)
   const size_t smem = sizeof(T) * (size_t)n * nb;
   if (smem > kPanelSmemMax) return NEGF_EINVAL;
   NEGF_CUDA_TRY(cudaFuncSetAttribute(gj_panel_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPanelSmemMax));
-  const size_t upd_smem = sizeof(T) * 2 * 32 * UPD_T;
+  const size_t upd_smem = sizeof(T) * 32 * (UPD_T + UPD_RS);
   NEGF_CUDA_TRY(cudaFuncSetAttribute(gj_update_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)upd_smem));
   if (nb > 32 || batch > 65535) return NEGF_EINVAL;
   NEGF_CUDA_TRY(cudaMemsetAsync(w.info, 0, sizeof(int) * batch, st));
