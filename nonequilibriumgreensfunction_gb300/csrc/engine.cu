@@ -288,6 +288,34 @@ int Engine::set_hopx(const double2* hx) {
       for (int a = 0; a < no; ++a)
         for (int c = 0; c < no; ++c) hb[((size_t)s * no + a) * no + c] = hx[(long long)(s * no + c) * M_ + s * no + a];
     NEGF_CUDA_TRY(cudaMemcpy(dHopBD_, hb.data(), sizeof(double2) * hb.size(), cudaMemcpyHostToDevice));
+    hop_uniform_ = no == 4;
+    for (size_t e = 16; e < hb.size() && hop_uniform_; ++e)
+      if (hb[e].x != hb[e % 16].x || hb[e].y != hb[e % 16].y) hop_uniform_ = false;
+    if (hop_uniform_) {
+      // op(H)(a, p) from the site block H(a, p) = hb[a * 4 + p]
+      auto opH = [&](int opc, int a, int p) {
+        const double2 v = opc ? hb[p * 4 + a] : hb[a * 4 + p];
+        return opc ? make_double2(v.x, -v.y) : v;
+      };
+      for (int left = 0; left < 2; ++left)
+        for (int opc = 0; opc < 2; ++opc) {
+          HopRows& r = hop_rows_[left][opc];
+          for (int a = 0; a < 4; ++a) {
+            int cnt = 0;
+            for (int kind = 0; kind < 3; ++kind)
+              for (int p = 0; p < 4; ++p) {
+                // left: Y_a = sum_p op(H)(a, p) x_p; right: Y_a = sum_p x_p op(H)(p, a)
+                const double2 c = left ? opH(opc, a, p) : opH(opc, p, a);
+                const int k = (c.x != 0.0 && c.y != 0.0) ? 2 : (c.x != 0.0 ? 0 : (c.y != 0.0 ? 1 : -1));
+                if (k != kind) continue;
+                r.p[a][cnt] = p; r.kind[a][cnt] = k; r.c[a][cnt] = c; ++cnt;
+              }
+            r.cnt[a] = cnt;
+          }
+        }
+    }
+  } else {
+    hop_uniform_ = false;
   }
   hop_set_ = true;
   return NEGF_OK;
@@ -359,7 +387,9 @@ int Engine::gemm(int batch, Op opA, const double2* A, long long sA, Op opB, cons
 }
 
 int Engine::hop_mul(int left, Op op, const double2* X, long long sX, double2* Y, long long sY, int batch) {
-  if (hop_bd_) return hop_apply(hop(), M_, batch, left, op, X, sX, Y, sY, st_);
+  if (hop_bd_)
+    return hop_apply(hop(), hop_uniform_ ? &hop_rows_[left ? 1 : 0][op == OP_C ? 1 : 0] : nullptr, M_, batch, left, op,
+                     X, sX, Y, sY, st_);
   const double2 one = make_double2(1, 0), zero = make_double2(0, 0);
   if (left) return gemm(batch, op, dHop_, 0, OP_N, X, sX, Y, sY, one, zero);
   return gemm(batch, OP_N, X, sX, op, dHop_, 0, Y, sY, one, zero);
@@ -701,6 +731,11 @@ int Engine::solve_rgf_impl(const std::vector<Item>& items, bool keep_columns) {
       if (hop_bd_) {
         fw.gprev = gprev;
         fw.hop = hop();
+        if (hop_uniform_) {   // side 0: L = H^H, R = H; side 1: L = H, R = H^H
+          fw.use_rows = 1;
+          fw.lrow = hop_rows_[1][side == 0 ? 1 : 0];
+          fw.rrow = hop_rows_[0][side == 0 ? 0 : 1];
+        }
       } else {
         // side 0: H^H g H ; side 1: H g H^H  (dense HopX)
         NEGF_TRY(hop_mul(1, side == 0 ? OP_C : OP_N, gprev, sG, dZ_, sM, B));

@@ -70,6 +70,10 @@ class Engine {
   double2* dHop_ = nullptr;
   double2* dHopBD_ = nullptr;
   bool hop_bd_ = false;
+  // every site's HopX block is the same 4 x 4 block: compact terms of op(H) for each side,
+  // hop_rows_[left][op == OP_C]
+  bool hop_uniform_ = false;
+  HopRows hop_rows_[2][2]{};
   bool hop_set_ = false;
   std::vector<int> slot_set_;
   // Slots whose end slices H_1 / H_N are bitwise identical share the Sancho-Rubio

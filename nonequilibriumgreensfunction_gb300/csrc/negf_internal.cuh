@@ -189,6 +189,19 @@ struct HopBD {
 //          side 0:  H^H gprev[b] H    (left-connected sweep, Recursive_Greens.F90:18-20)
 //          side 1:  H gprev[b] H^H    (right-connected sweep, Recursive_Greens.F90:70-72)
 //        using the block-diagonal H, or, if zsub != nullptr, zsub[b] (dense path).
+// A 4 x 4 hop block shared by every site, as compact terms per output index a: cnt[a]
+// terms (p[a][t], c[a][t]) with Y_a = sum_t c x_p (left: c = op(H)(a, p); right:
+// Y(i, a) = sum_t x_p c with c = op(H)(p, a)); kind 0 = real c, 1 = imaginary c,
+// 2 = general.  Each list is sorted by kind, so that lanes of different rows take the same
+// branches; the order of two terms can then differ from the dense fma sequence, which moves
+// the last bit of a sum at most.
+struct HopRows {
+  int cnt[4];
+  int p[4][4];
+  int kind[4][4];
+  double2 c[4][4];
+};
+
 struct FormW {
   int n, batch, npx, x;
   double eta;
@@ -201,11 +214,17 @@ struct FormW {
   HopBD hop;
   const double2* zsub; long long sZ;
   double2* W; long long sW;
+  // every site shares one 4 x 4 hop block: the coupling term L G R from compact terms,
+  // lrow = L by rows (left form), rrow = R by columns (right form)
+  int use_rows = 0;
+  HopRows lrow{}, rrow{};
 };
 int form_w(const FormW& a, cudaStream_t st);
 
-// Y[b] = op(H) X[b] (left == 1) or X[b] op(H) (left == 0), H block diagonal; op in {N, C}
-int hop_apply(const HopBD& h, int n, int batch, int left, Op op, const double2* X, long long sX,
+// Y[b] = op(H) X[b] (left == 1) or X[b] op(H) (left == 0), H block diagonal; op in {N, C}.
+// rows (may be null): the compact form of op(H) for that side when every site has the same
+// 4 x 4 block.
+int hop_apply(const HopBD& h, const HopRows* rows, int n, int batch, int left, Op op, const double2* X, long long sX,
               double2* Y, long long sY, cudaStream_t st);
 
 // Site blocks of P = X Gamma X^H: P[b][r][a] = sum_k Y[b](r,k) conj(X[b](site(r)*norb + a, k)),

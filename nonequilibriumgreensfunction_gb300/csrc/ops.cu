@@ -87,6 +87,55 @@ __global__ void form_w_kernel(FormW a) {
   }
 }
 
+// acc += x c (right) or c x (left) for one compact hop term of the given kind
+__device__ __forceinline__ void term_fma(double2& acc, double2 x, double2 c, int kind, bool c_left) {
+  if (kind == 0) {
+    acc.x = fma(c.x, x.x, acc.x);
+    acc.y = fma(c.x, x.y, acc.y);
+  } else if (kind == 1) {
+    acc.x = fma(-c.y, x.y, acc.x);
+    acc.y = fma(c.y, x.x, acc.y);
+  } else if (c_left) {
+    cfma(acc, c, x);
+  } else {
+    cfma(acc, x, c);
+  }
+}
+
+// W with the coupling term from the compact terms of a hop block shared by every site:
+// W(i, j) -= sum_p L(a, p) sum_q G(4 si + p, 4 sj + q) R(q, c) over the nonzero terms only
+// (i = 4 si + a, j = 4 sj + c), the nesting of form_w_blocks_kernel.  Lanes of a warp share
+// j and take the same kinds of terms, so they branch together; the G elements come from L1.
+__global__ void form_w_rows_kernel(FormW a) {
+  const int b = blockIdx.y;
+  const int n = a.n;
+  const long long nn = (long long)n * n;
+  const Item it = a.items[b];
+  const double2* Hx = a.Hall + ((long long)it.slot * a.npx + a.x) * nn;
+  const double2* gp = a.gprev + (long long)b * a.sG;
+  const double2* sl = (a.x == 0 && a.sigL) ? a.sigL + (long long)b * a.sSig : nullptr;
+  const double2* sr = (a.x == a.npx - 1 && a.sigR) ? a.sigR + (long long)b * a.sSig : nullptr;
+  double2* W = a.W + (long long)b * a.sW;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nn; e += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(e % n), j = (int)(e / n);
+    double2 v = make_double2(-Hx[e].x, -Hx[e].y);
+    if (i == j) { v.x += it.energy; v.y += a.eta; }
+    if (sl) v = csub(v, sl[e]);
+    if (sr) v = csub(v, sr[e]);
+    const int ra = i & 3, ca = j & 3;
+    const double2* gb = gp + (long long)(j - ca) * n + (i - ra);   // G(4 si + p, 4 sj + q) = gb[q n + p]
+    double2 acc = make_double2(0.0, 0.0);
+    for (int tl = 0; tl < a.lrow.cnt[ra]; ++tl) {
+      const int p = a.lrow.p[ra][tl];
+      double2 t = make_double2(0.0, 0.0);
+      for (int tr = 0; tr < a.rrow.cnt[ca]; ++tr)
+        term_fma(t, gb[(long long)a.rrow.p[ca][tr] * n + p], a.rrow.c[ca][tr], a.rrow.kind[ca][tr], false);
+      term_fma(acc, t, a.lrow.c[ra][tl], a.lrow.kind[ra][tl], true);
+    }
+    W[e] = csub(v, acc);
+  }
+}
+
 // The same W when HopX is block diagonal with 4 x 4 site blocks: one thread per 4 x 4 site
 // block (si, sj) of W.  The coupling term of the block is L_si G(si, sj) R_sj (side 0:
 // L = H^H, R = H; side 1: L = H, R = H^H), formed as T = G R and then L T: 8 complex FMAs
@@ -173,6 +222,43 @@ __global__ void hop_apply_kernel(HopBD h, int n, int left, int op, const double2
       for (int qa = 0; qa < no; ++qa) {
         const double2 hv = (op == OP_C) ? cconj(hbe(h, s, aj, qa)) : hbe(h, s, qa, aj);
         cfma(acc, Xb[(long long)(s * no + qa) * n + i], hv);
+      }
+    }
+    Yb[e] = acc;
+  }
+}
+
+// The same products when every site shares one 4 x 4 block, from its compact terms: the
+// wire models' HopX blocks are half zeros with purely real or imaginary nonzeros, so each
+// output takes two terms of two FP64 fmas instead of four complex fmas (16 fmas).  The term
+// lists are kernel parameters sorted by kind, so every lane runs the same kinds of terms;
+// the skipped terms are exact zeros of hop_apply_kernel's sequence.
+__global__ void hop_rows_kernel(HopRows r, int n, int left, const double2* X, long long sX, double2* Y, long long sY) {
+  const int b = blockIdx.y;
+  const long long nn = (long long)n * n;
+  const double2* Xb = X + (long long)b * sX;
+  double2* Yb = Y + (long long)b * sY;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nn; e += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(e % n), j = (int)(e / n);
+    // left: x_p = X(4s + p, j), a = i % 4; right: x_p = X(i, 4s + p), a = j % 4
+    const int a = left ? (i & 3) : (j & 3);
+    const double2* xb = left ? Xb + (long long)j * n + (i - a) : Xb + (long long)(j - a) * n + i;
+    const long long xs = left ? 1 : n;
+    double2 acc = make_double2(0.0, 0.0);
+    for (int t = 0; t < r.cnt[a]; ++t) {
+      const double2 x = xb[r.p[a][t] * xs];
+      const double2 c = r.c[a][t];
+      const int k = r.kind[a][t];
+      if (k == 0) {
+        acc.x = fma(c.x, x.x, acc.x);
+        acc.y = fma(c.x, x.y, acc.y);
+      } else if (k == 1) {
+        acc.x = fma(-c.y, x.y, acc.x);
+        acc.y = fma(c.y, x.x, acc.y);
+      } else if (left) {
+        cfma(acc, c, x);
+      } else {
+        cfma(acc, x, c);
       }
     }
     Yb[e] = acc;
@@ -739,6 +825,12 @@ __global__ void reduce_sites_kernel(int batch, int total, int nf, int nslots, co
 
 // =====================================================================================
 int form_w(const FormW& a, cudaStream_t st) {
+  if (a.gprev && a.use_rows && a.hop.norb == 4 && !a.zsub && a.n % 4 == 0) {
+    form_w_rows_kernel<<<ew_grid((long long)a.n * a.n, a.batch), EW_THREADS, 0, st>>>(a);
+    NEGF_CUDA_TRY(cudaGetLastError());
+    count_launch();
+    return NEGF_OK;
+  }
   if (a.gprev && a.hop.hb && a.hop.norb == 4 && !a.zsub && a.n % 4 == 0) {
     const long long nblk = (long long)(a.n / 4) * (a.n / 4);
     form_w_blocks_kernel<<<ew_grid(nblk, a.batch), 128, 0, st>>>(a);
@@ -752,8 +844,14 @@ int form_w(const FormW& a, cudaStream_t st) {
   return NEGF_OK;
 }
 
-int hop_apply(const HopBD& h, int n, int batch, int left, Op op, const double2* X, long long sX, double2* Y,
-              long long sY, cudaStream_t st) {
+int hop_apply(const HopBD& h, const HopRows* rows, int n, int batch, int left, Op op, const double2* X, long long sX,
+              double2* Y, long long sY, cudaStream_t st) {
+  if (rows && h.norb == 4 && n % 4 == 0 && X != Y) {
+    hop_rows_kernel<<<ew_grid((long long)n * n, batch), EW_THREADS, 0, st>>>(*rows, n, left, X, sX, Y, sY);
+    NEGF_CUDA_TRY(cudaGetLastError());
+    count_launch();
+    return NEGF_OK;
+  }
   hop_apply_kernel<<<ew_grid((long long)n * n, batch), EW_THREADS, 0, st>>>(h, n, left, (int)op, X, sX, Y, sY);
   NEGF_CUDA_TRY(cudaGetLastError());
   count_launch();
