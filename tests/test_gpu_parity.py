@@ -189,6 +189,37 @@ def test_dense_hopx_and_asymmetric_leads(need_gpu):
     assert_close(rn[..., 0], want, "RhoN")
 
 
+@pytest.mark.parametrize("precision,rtol", [("fp64", RTOL), ("mixed", 1e-6)])
+def test_uniform_hop_block_with_general_entries(need_gpu, precision, rtol):
+    """Every site shares one HopX block whose nonzeros are general complex numbers, with
+    rows of different kinds (one real extra entry): the compact term lists of the HopX
+    products and of the W assembly take their general and mixed branches."""
+    npx, npy, npz = 6, 2, 2
+    htotd, hopx = HB.ti_wire(npx, npy, npz, W=0.1, seed=4, flux=0.3)
+    blk = hopx[:4, :4] * np.exp(0.3j)
+    blk[0, 1] = 0.04                                # a real entry beside general ones
+    nsite = npy * npz
+    hopx = np.kron(np.eye(nsite), blk)
+    opt = O.SolveOptions(eta=1e-5, sr_tol=1e-10, kT=0.025, calc_spin=True)
+    mu = (0.05, -0.05)
+    es = np.array([-0.6, -0.4, 0.45])               # in the bands of the 2 x 2 cross-section
+    f1 = [O.fermi(x, mu[0], opt.kT) for x in es]
+    f2 = [O.fermi(x, mu[1], opt.kT) for x in es]
+    with Solver(npx, npy, npz, eta=opt.eta, sr_tol=opt.sr_tol, calc_spin=True, max_batch=3,
+                precision=precision) as s:
+        s.set_hamiltonian(htotd, hopx)
+        rn = s.new_site_array(1)
+        r = s.solve_batch(es, f1, f2, 1e-3, rho_n=rn)
+    assert (r["status"] == 0).all()
+    want = np.zeros((npx, npy, npz))
+    for i, e in enumerate(es):
+        ref = O.energy_sweep(htotd, hopx, float(e), mu, 1e-3, npy, npz, opt)
+        for k in ("T12", "Modec1", "EDensity", "HDensity"):
+            assert_close(r[k][i], ref[k], "%s[%d]" % (k, i), rtol=rtol, floor=1e-6)
+        want += ref["RhoN"]
+    assert_close(rn[..., 0], want, "RhoN", rtol=rtol)
+
+
 def test_result_is_the_same_alone_and_in_a_batch(need_gpu):
     """Each item's arithmetic is independent of what else is in the batch: bitwise equal."""
     npx, npy, npz = 8, 3, 3
