@@ -23,70 +23,6 @@ __device__ __forceinline__ double2 hbe(const HopBD& h, int s, int a, int c) {
   return h.hb[((long long)s * h.norb + a) * h.norb + c];
 }
 
-// acc += a b (complex) with the same fma sequence as cfma, leaving out the terms whose
-// factor from b (cfma_sb) or a (cfma_sa) is an exact zero.  The HopX site blocks of the
-// wire models are half zeros and their nonzeros purely real or imaginary, so this takes a
-// quarter of the FP64 fmas; a skipped term fma(x, 0, acc) would have returned acc, so the
-// sums are unchanged (up to the sign of an exact zero).  When every site has the same
-// block, the branches are uniform across a warp.
-__device__ __forceinline__ void cfma_sb(double2& acc, double2 a, double2 b) {
-  if (b.x != 0.0) acc.x = fma(a.x, b.x, acc.x);
-  if (b.y != 0.0) {
-    acc.x = fma(-a.y, b.y, acc.x);
-    acc.y = fma(a.x, b.y, acc.y);
-  }
-  if (b.x != 0.0) acc.y = fma(a.y, b.x, acc.y);
-}
-__device__ __forceinline__ void cfma_sa(double2& acc, double2 a, double2 b) {
-  if (a.x != 0.0) acc.x = fma(a.x, b.x, acc.x);
-  if (a.y != 0.0) acc.x = fma(-a.y, b.y, acc.x);
-  if (a.x != 0.0) acc.y = fma(a.x, b.y, acc.y);
-  if (a.y != 0.0) acc.y = fma(a.y, b.x, acc.y);
-}
-
-// ---- W assembly (Energy_Sweep.F90:31-38 + Recursive_Greens.F90:18-20 / :70-72) ----------
-__global__ void form_w_kernel(FormW a) {
-  const int b = blockIdx.y;
-  const int n = a.n;
-  const long long nn = (long long)n * n;
-  const Item it = a.items[b];
-  const double2* Hx = a.Hall + ((long long)it.slot * a.npx + a.x) * nn;
-  const double2* gp = a.gprev ? a.gprev + (long long)b * a.sG : nullptr;
-  const double2* zs = a.zsub ? a.zsub + (long long)b * a.sZ : nullptr;
-  const double2* sl = (a.x == 0 && a.sigL) ? a.sigL + (long long)b * a.sSig : nullptr;
-  const double2* sr = (a.x == a.npx - 1 && a.sigR) ? a.sigR + (long long)b * a.sSig : nullptr;
-  double2* W = a.W + (long long)b * a.sW;
-  const int no = a.hop.norb;
-  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nn; e += (long long)gridDim.x * blockDim.x) {
-    const int i = (int)(e % n), j = (int)(e / n);
-    double2 v = make_double2(-Hx[e].x, -Hx[e].y);
-    if (i == j) { v.x += it.energy; v.y += a.eta; }
-    if (sl) v = csub(v, sl[e]);
-    if (sr) v = csub(v, sr[e]);
-    if (zs) v = csub(v, zs[e]);
-    if (gp && a.hop.hb) {
-      // sum_{p in site(i), q in site(j)} L(i,p) g(p,q) R(q,j)
-      const int si = i / no, ai = i % no, sj = j / no, aj = j % no;
-      double2 acc = make_double2(0.0, 0.0);
-      for (int pa = 0; pa < no; ++pa) {
-        // side 0: L = H^H -> L(i,p) = conj(H(p,i));  side 1: L = H -> H(i,p)
-        const double2 l = a.side == 0 ? cconj(hbe(a.hop, si, pa, ai)) : hbe(a.hop, si, ai, pa);
-        double2 row = make_double2(0.0, 0.0);
-        const int p = si * no + pa;
-        for (int qa = 0; qa < no; ++qa) {
-          // side 0: R = H -> H(q,j);  side 1: R = H^H -> conj(H(j,q))
-          const double2 r = a.side == 0 ? hbe(a.hop, sj, qa, aj) : cconj(hbe(a.hop, sj, aj, qa));
-          const int q = sj * no + qa;
-          cfma(row, gp[(long long)q * n + p], r);
-        }
-        cfma(acc, l, row);
-      }
-      v = csub(v, acc);
-    }
-    W[e] = v;
-  }
-}
-
 // acc += x c (right) or c x (left) for one compact hop term of the given kind
 __device__ __forceinline__ void term_fma(double2& acc, double2 x, double2 c, int kind, bool c_left) {
   if (kind == 0) {
@@ -139,9 +75,9 @@ __global__ void form_w_rows_kernel(FormW a) {
 // The same W when HopX is block diagonal with 4 x 4 site blocks: one thread per 4 x 4 site
 // block (si, sj) of W.  The coupling term of the block is L_si G(si, sj) R_sj (side 0:
 // L = H^H, R = H; side 1: L = H, R = H^H), formed as T = G R and then L T: 8 complex FMAs
-// per element instead of the 20 of the element-wise form, and a quarter of those with the
-// zero terms of the hop blocks left out.  GB300's FP64 pipe runs at 1/64 of its FP32 rate,
-// so this FP64 arithmetic, not memory, bounds the kernel.  Each thread
+// per element instead of the 20 of the element-wise form.  GB300's FP64 pipe runs at 1/64
+// of its FP32 rate, so this FP64 arithmetic, not memory, bounds the kernel.  Used when the
+// sites' blocks differ; a block shared by every site takes form_w_rows_kernel.  Each thread
 // reads and writes its block as four 64-byte column pieces; consecutive threads take
 // consecutive row blocks, so a warp's accesses to a column are contiguous.
 __global__ void form_w_blocks_kernel(FormW a) {
@@ -174,7 +110,7 @@ __global__ void form_w_blocks_kernel(FormW a) {
       for (int r = 0; r < 4; ++r) {
         double2 acc = make_double2(0.0, 0.0);
 #pragma unroll
-        for (int q = 0; q < 4; ++q) cfma_sb(acc, g[r][q], rc[q]);
+        for (int q = 0; q < 4; ++q) cfma(acc, g[r][q], rc[q]);
         tm[r][c] = acc;
       }
     }
@@ -186,7 +122,7 @@ __global__ void form_w_blocks_kernel(FormW a) {
         double2 acc = make_double2(0.0, 0.0);
 #pragma unroll
         for (int p = 0; p < 4; ++p)   // L(r, p): side 0: L = H^H, side 1: L = H
-          cfma_sa(acc, a.side == 0 ? cconj(hbe(a.hop, si, p, r)) : hbe(a.hop, si, r, p), tm[p][c]);
+          cfma(acc, a.side == 0 ? cconj(hbe(a.hop, si, p, r)) : hbe(a.hop, si, r, p), tm[p][c]);
         const long long e = e0 + r;
         double2 v = make_double2(-Hx[e].x, -Hx[e].y);
         if (si == sj && r == c) { v.x += it.energy; v.y += a.eta; }
