@@ -23,6 +23,49 @@ __device__ __forceinline__ double2 hbe(const HopBD& h, int s, int a, int c) {
   return h.hb[((long long)s * h.norb + a) * h.norb + c];
 }
 
+// ---- W assembly (Energy_Sweep.F90:31-38 + Recursive_Greens.F90:18-20 / :70-72) ----------
+__global__ void form_w_kernel(FormW a) {
+  const int b = blockIdx.y;
+  const int n = a.n;
+  const long long nn = (long long)n * n;
+  const Item it = a.items[b];
+  const double2* Hx = a.Hall + ((long long)it.slot * a.npx + a.x) * nn;
+  const double2* gp = a.gprev ? a.gprev + (long long)b * a.sG : nullptr;
+  const double2* zs = a.zsub ? a.zsub + (long long)b * a.sZ : nullptr;
+  const double2* sl = (a.x == 0 && a.sigL) ? a.sigL + (long long)b * a.sSig : nullptr;
+  const double2* sr = (a.x == a.npx - 1 && a.sigR) ? a.sigR + (long long)b * a.sSig : nullptr;
+  double2* W = a.W + (long long)b * a.sW;
+  const int no = a.hop.norb;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nn; e += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(e % n), j = (int)(e / n);
+    double2 v = make_double2(-Hx[e].x, -Hx[e].y);
+    if (i == j) { v.x += it.energy; v.y += a.eta; }
+    if (sl) v = csub(v, sl[e]);
+    if (sr) v = csub(v, sr[e]);
+    if (zs) v = csub(v, zs[e]);
+    if (gp && a.hop.hb) {
+      // sum_{p in site(i), q in site(j)} L(i,p) g(p,q) R(q,j)
+      const int si = i / no, ai = i % no, sj = j / no, aj = j % no;
+      double2 acc = make_double2(0.0, 0.0);
+      for (int pa = 0; pa < no; ++pa) {
+        // side 0: L = H^H -> L(i,p) = conj(H(p,i));  side 1: L = H -> H(i,p)
+        const double2 l = a.side == 0 ? cconj(hbe(a.hop, si, pa, ai)) : hbe(a.hop, si, ai, pa);
+        double2 row = make_double2(0.0, 0.0);
+        const int p = si * no + pa;
+        for (int qa = 0; qa < no; ++qa) {
+          // side 0: R = H -> H(q,j);  side 1: R = H^H -> conj(H(j,q))
+          const double2 r = a.side == 0 ? hbe(a.hop, sj, qa, aj) : cconj(hbe(a.hop, sj, aj, qa));
+          const int q = sj * no + qa;
+          cfma(row, gp[(long long)q * n + p], r);
+        }
+        cfma(acc, l, row);
+      }
+      v = csub(v, acc);
+    }
+    W[e] = v;
+  }
+}
+
 // acc += x c (right) or c x (left) for one compact hop term of the given kind
 __device__ __forceinline__ void term_fma(double2& acc, double2 x, double2 c, int kind, bool c_left) {
   if (kind == 0) {
