@@ -25,6 +25,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 REPO = os.path.dirname(os.path.abspath(__file__))
@@ -355,6 +356,9 @@ def main():
                          "--slices slices, twice) and exit")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--clocks-csv", default=None,
+                    help="where the nvidia-smi samples of the timed region go (%%d = rank); "
+                         "default: the temporary directory")
     ap.add_argument("--serving-seconds", type=float, default=30.0,
                     help="length of the Poisson-arrival serving run (0 = skip); rank 0 of a 1-GPU run only")
     args = ap.parse_args()
@@ -424,8 +428,9 @@ def main():
     sr_iters = int(np.max(r["sr_iters"]))
     timed_results = []
 
-    clocks_path = os.path.join(REPO, "gpurun_out", "bench_clocks_rank%d.csv" % rank)
-    os.makedirs(os.path.dirname(clocks_path), exist_ok=True)
+    clocks_path = (args.clocks_csv % rank) if args.clocks_csv else os.path.join(
+        tempfile.gettempdir(), "negf_bench_clocks_rank%d.csv" % rank)
+    os.makedirs(os.path.dirname(os.path.abspath(clocks_path)), exist_ok=True)
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize()
