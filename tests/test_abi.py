@@ -62,6 +62,33 @@ int main(void) {
     assert vals == want
 
 
+def test_field_offsets_match_header():
+    """Every field of the parameter and output structures the bindings fill sits where the C
+    compiler puts it (contact parameters, resolved-output pointers, stats counters)."""
+    structs = {
+        "negf_params": capi.NegfParams, "negf_batch_outputs": capi.NegfBatchOutputs,
+        "negf_stats": capi.NegfStats, "negf_result": capi.NegfResult, "negf_request": capi.NegfRequest,
+        "negf_wire_model": capi.NegfWireModel, "negf_serve_params": capi.NegfServeParams,
+        "negf_wire_request": capi.NegfWireRequest, "negf_wire_status": capi.NegfWireStatus,
+    }
+    lines = []
+    for cname, cls in structs.items():
+        for fname, _ in cls._fields_:
+            lines.append('  printf("%%s.%%s %%zu\\n", "%s", "%s", offsetof(%s, %s));' % (cname, fname, cname, fname))
+    src = "#include <stdio.h>\n#include <stddef.h>\n#include \"negf.h\"\nint main(void) {\n" + "\n".join(lines) + \
+        "\n  return 0;\n}\n"
+    with tempfile.TemporaryDirectory() as d:
+        c = os.path.join(d, "t.c")
+        exe = os.path.join(d, "t")
+        open(c, "w").write(src)
+        subprocess.run(["gcc", "-I", os.path.join(REPO, "include"), c, "-o", exe], check=True)
+        got = dict(line.split() for line in subprocess.run([exe], capture_output=True, text=True,
+                                                           check=True).stdout.splitlines())
+    for cname, cls in structs.items():
+        for fname, _ in cls._fields_:
+            assert int(got["%s.%s" % (cname, fname)]) == getattr(cls, fname).offset, (cname, fname)
+
+
 def test_strerror_covers_codes():
     capi.load()
     for code in range(-12, 1):
