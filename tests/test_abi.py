@@ -112,3 +112,40 @@ def test_c_driver_compiles_against_header():
         exe = os.path.join(d, "drv")
         subprocess.run(["gcc", "-O1", "-I", os.path.join(REPO, "include"), drv, "-o", exe,
                         "-L", os.path.dirname(capi.library_path()), "-lnegf_gb300", "-lm"], check=True)
+
+
+def test_fortran_shim_params_type_matches_header():
+    """The shim's BIND(C) negf_params_t (no Fortran compiler here) lays out like negf_params:
+    its fields, parsed from the source and placed with C alignment, have the header's
+    offsets and total size."""
+    shim = os.path.join(REPO, "nonequilibriumgreensfunction_gb300", "fortran", "negf_gpu_shim.F90")
+    txt = open(shim).read()
+    body = txt[txt.index("TYPE, BIND(C) :: negf_params_t"):txt.index("END TYPE")]
+    sizes = {"INTEGER(C_INT32_T)": 4, "REAL(C_DOUBLE)": 8}
+    fields, off = [], 0
+    for line in body.splitlines()[1:]:
+        line = line.split("!")[0].strip()
+        if not line:
+            continue
+        kind, names = [p.strip() for p in line.split("::")]
+        size = sizes[kind]
+        for m in re.finditer(r"(\w+)(?:\(([\d,\s]+)\))?", names):
+            count = 1
+            if m.group(2):
+                for d in m.group(2).split(","):
+                    count *= int(d)
+            off = (off + size - 1) // size * size
+            fields.append((m.group(1), off))
+            off += size * count
+    total = (off + 7) // 8 * 8
+    src = "#include <stdio.h>\n#include <stddef.h>\n#include \"negf.h\"\nint main(void) {\n"
+    src += "\n".join('  printf("%%zu\\n", offsetof(negf_params, %s));' % f for f, _ in fields)
+    src += '\n  printf("%zu\\n", sizeof(negf_params));\n  return 0;\n}\n'
+    with tempfile.TemporaryDirectory() as d:
+        c = os.path.join(d, "t.c")
+        exe = os.path.join(d, "t")
+        open(c, "w").write(src)
+        subprocess.run(["gcc", "-I", os.path.join(REPO, "include"), c, "-o", exe], check=True)
+        vals = [int(v) for v in subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()]
+    assert vals[:-1] == [o for _, o in fields], list(zip([f for f, _ in fields], vals, [o for _, o in fields]))
+    assert vals[-1] == total
