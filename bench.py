@@ -76,6 +76,17 @@ def max_over_ranks(value, dist, device):
     return float(t.item())
 
 
+def survey_flops_per_solve(m, npx, n_sr, n_leads=2):
+    """The work model of the hot-path scope table (real flops per energy point):
+    F = 96 M^3 Npx + n_leads (72 n_SR + 56) M^3 + 16 M^3 -- per slice 12 complex M^3
+    products or inverses of 8 M^3 each (both sweeps, both column propagations, the two
+    G Gamma products), per decimation iteration 8 products and 1 inverse per lead, the
+    transmission's 2 products.  It counts dense HopX products that the site-local HopX
+    of these wires makes O(M^2) and does not share the decimation between seeds."""
+    m3 = float(m) ** 3
+    return 96.0 * m3 * npx + n_leads * (72.0 * n_sr + 56.0) * m3 + 16.0 * m3
+
+
 def algorithmic_flops_per_solve(m, npx, n_sr, n_seeds_sharing=SEEDS):
     """Work model of the solve (real flops), per energy point:
     RGF: per slice 2 inverses + 4 complex GEMMs (column 1, column N, G Gamma_L, G Gamma_R),
@@ -345,8 +356,11 @@ def main():
     ap.add_argument("--sr-slices", type=int, default=0, help="mixed form: slices of the Sancho-Rubio products")
     ap.add_argument("--fp64-steps", type=int, default=1,
                     help="mixed form: timed FP64 steps on the same requests (T error and FP64 rate)")
-    ap.add_argument("--fp64-batch", type=int, default=32,
-                    help="mixed form: requests of each compared step solved in FP64 (a prefix of the step)")
+    ap.add_argument("--fp64-batch", type=int, default=0,
+                    help="mixed form: requests of each compared step solved in FP64 (a prefix of the "
+                         "step; 0 = the whole step)")
+    ap.add_argument("--e2e-steps", type=int, default=5,
+                    help="steps of the end-to-end leg (each re-uploads the Hamiltonians); at most --steps")
     ap.add_argument("--npx", type=int, default=NPX,
                     help="slices of the wire; the benchmark workload is 100, shorter wires only for profiling")
     ap.add_argument("--workload", default="wire", choices=["wire", "scf"],
@@ -428,7 +442,7 @@ def main():
     sr_iters = int(np.max(r["sr_iters"]))
     timed_results = []
 
-    clocks_path = (args.clocks_csv % rank) if args.clocks_csv else os.path.join(
+    clocks_path = (args.clocks_csv.replace("%d", str(rank))) if args.clocks_csv else os.path.join(
         tempfile.gettempdir(), "negf_bench_clocks_rank%d.csv" % rank)
     os.makedirs(os.path.dirname(os.path.abspath(clocks_path)), exist_ok=True)
     if world > 1:
@@ -458,9 +472,10 @@ def main():
         torch.cuda.synchronize()
         if world > 1:
             dist.barrier()
+        n_e2e = max(1, min(args.e2e_steps, args.steps))
         ev2, ev3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         ev2.record(stream)
-        for s in range(args.steps):
+        for s in range(n_e2e):
             for k, (hf, xf) in enumerate(pinned):
                 solver.set_hamiltonian_fortran(hf, xf, slot=k)
             one_step(args.warmup + s)
@@ -471,18 +486,19 @@ def main():
             el2 = max_over_ranks(el2, dist, dev)
         h2d = sum(hf.nbytes + xf.nbytes for hf, xf in pinned) + args.batch * 40
         d2h = args.batch * 64 + 5 * nsites * SEEDS * 8
-        e2e = {"value": args.batch * args.steps * world / el2, "unit": "solves/s",
-               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)}
+        e2e = {"value": args.batch * n_e2e * world / el2, "unit": "solves/s",
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "steps": n_e2e}
 
     # FP64 form on the same requests: its rate, and the T error of the mixed form
     fp64 = None
     if args.form == "mixed" and args.fp64_steps > 0:
         st_mixed = st
         solver.close()
-        nfb = max(SEEDS, min(args.fp64_batch, args.batch))
+        nfb = args.batch if args.fp64_batch <= 0 else max(SEEDS, min(args.fp64_batch, args.batch))
         ref = Solver(NPX, NPY, NPZ, n_hamiltonians=SEEDS, max_batch=nfb, eta=ETA, sr_tol=SR_TOL,
                      calc_spin=True, precision="fp64", device=local_rank)
         ref.set_stream(stream.cuda_stream)
+        ref.profile(True)
         for k, (hf, xf) in enumerate(pinned):
             ref.set_hamiltonian_fortran(hf, xf, slot=k)
         n_fp = min(args.fp64_steps, args.steps)
@@ -497,19 +513,34 @@ def main():
         ev5.record(stream)
         torch.cuda.synchronize()
         el64 = ev4.elapsed_time(ev5) * 1e-3
+        st64 = ref.stats()
         t_err = 0.0
+        rho_err = 0.0
         worst = []
         for s_i, (a, b) in enumerate(zip(timed_results[:n_fp], outs)):
             rel = np.abs(a["T12"][:nfb] - b["T12"]) / np.maximum(np.abs(b["T12"]), 1e-3)
             t_err = max(t_err, float(np.max(rel)))
+            for k in ("EDensity", "HDensity"):
+                den = np.maximum(np.abs(b[k]), 1e-3 * np.abs(b[k]).max())
+                rho_err = max(rho_err, float(np.max(np.abs(a[k][:nfb] - b[k]) / den)))
             e_s, _, _, sl_s = step_requests(args.warmup + s_i, args.batch, rank, world)
             for i in np.argsort(rel)[-3:]:
                 worst.append((float(rel[i]), float(e_s[i]), int(sl_s[i]), float(b["T12"][i]), float(a["T12"][i])))
         worst = sorted(worst)[-3:]
+        fp64_peak = fp64_zgemm_peak_tflops(torch, dev)
+        gemm_tf = st64["gemm_flops"] / (st64["gemm_ms"] * 1e-3) / 1e12 if st64["gemm_ms"] > 0 else None
         fp64 = {"value": nfb * n_fp / el64, "unit": "solves/s", "steps": n_fp, "batch": nfb,
-                "t_rel_err_max": t_err, "t_err_gate": 1e-6, "gate_ok": t_err <= 1e-6,
-                "t_err_floor": "denominator max(|T_fp64|, 1e-3)",
-                "worst": [{"rel": w[0], "E": w[1], "seed": w[2], "T_fp64": w[3], "T_mixed": w[4]} for w in worst]}
+                "compared_solves": nfb * n_fp, "t_rel_err_max": t_err, "t_err_gate": 1e-6,
+                "gate_ok": t_err <= 1e-6, "t_err_floor": "denominator max(|T_fp64|, 1e-3)",
+                "density_rel_err_max": rho_err,
+                "density_err_floor": "EDensity/HDensity, denominator max(|x|, 1e-3 max|x|)",
+                "worst": [{"rel": w[0], "E": w[1], "seed": w[2], "T_fp64": w[3], "T_mixed": w[4]} for w in worst],
+                "roofline": {"bound": "fp64", "kernel": "zgemm_kernel<double2> (FP64 complex GEMM, DFMA)",
+                             "achieved": gemm_tf, "peak": fp64_peak, "unit": "TFLOP/s",
+                             "frac": (gemm_tf / fp64_peak) if gemm_tf else None,
+                             "peak_source": "cuBLAS ZGEMM 4096^3 complex128 measured live (of measured)",
+                             "launches": st64["gemm_launches"], "gemm_s": st64["gemm_ms"] * 1e-3,
+                             "gauss_jordan_panel_s": st64["panel_ms"] * 1e-3, "step_s": el64 / n_fp}}
         ref.close()
         solver = None
         st = st_mixed
@@ -533,8 +564,13 @@ def main():
     else:
         # tensor work actually issued: the slice-pair products, counted from the stats'
         # complex-equivalent flops; achieved = issued BF16 tensor flops / kernel time
+        # achieved: the algorithmic work of the scope table's convention, 3 BF16 MMAs per
+        # split real product, i.e. 3 x 8 m n k real flops per complex product the launches
+        # compute; issued: every slice-pair MMA the kernel actually runs, S (S + 1) / 2 of
+        # them per real product (the precision cost of the integer slicing)
         tc_issued = st.get("tc_flops") or None
-        tc_tf = (tc_issued / (st["tc_ms"] * 1e-3) / 1e12) if (tc_issued and st["tc_ms"] > 0) else None
+        tc_tf = (3.0 * st["tc_complex_flops"] / (st["tc_ms"] * 1e-3) / 1e12) if st["tc_ms"] > 0 else None
+        issued_tf = (tc_issued / (st["tc_ms"] * 1e-3) / 1e12) if (tc_issued and st["tc_ms"] > 0) else None
         bf16_peak = peaks.get("bf16_tflops")
         # DRAM traffic of one 5-slice RGF product launch (M = 400): an ncu capture of 16
         # products (dram__bytes_read.sum + dram__bytes_write.sum = 153.8 + 25.8 MB) scaled
@@ -551,15 +587,19 @@ def main():
             "traffic_source": "ncu capture of 16 products, scaled in proportion to the batch",
             "traffic_algorithmic_bytes": algo_bytes,
             "peak_source": "MEASURED_PEAKS.json bf16_tflops (of measured, burst)",
+            "achieved_convention": "3 BF16 MMAs (3 x 8 m n k flops) per complex product computed",
+            "issued_tflops": issued_tf, "issued_frac": (issued_tf / bf16_peak) if (issued_tf and bf16_peak) else None,
             "launches": st["tc_launches"], "share_of_step": st["tc_ms"] * 1e-3 / elapsed,
             "complex_equiv_tflops": (st["tc_complex_flops"] / (st["tc_ms"] * 1e-3) / 1e12) if st["tc_ms"] > 0 else None,
             "fallbacks": st["fallbacks"], "ns_residual_max": st["ns_residual_max"],
-            "ns_extra_steps": st["ns_extra_steps"],
+            "ns_extra_steps": st["ns_extra_steps"], "ns_unconverged": st["ns_unconverged"],
+            "ns_final_residual_max": st["ns_final_residual_max"],
         }
     roofline["breakdown_s_per_step"] = {
         k: st[k] * 1e-3 / args.steps for k in ("phase_sr_ms", "phase_rgf_ms", "phase_inv_ms", "phase_dens_ms",
                                                "tc_ms", "gemm_ms", "panel_ms", "f32_gemm_ms", "slice_ms")}
     flops_solve = algorithmic_flops_per_solve(m, NPX, sr_iters)
+    flops_survey = survey_flops_per_solve(m, NPX, sr_iters)
     serving = None
     if args.serving_seconds > 0 and world == 1:
         if solver is not None:
@@ -581,6 +621,10 @@ def main():
         "roofline": roofline,
         "solve_tflops": flops_solve * value / 1e12 / world,
         "algorithmic_flops_per_solve": flops_solve,
+        "algorithmic_model": "48 M^3 Npx + (88 n_SR + 24) M^3 / seeds + 32 M^3 (the work this solver "
+                             "does: site-local HopX, decimation shared by the seeds of an energy)",
+        "solve_tflops_survey_model": flops_survey * value / 1e12 / world,
+        "survey_flops_per_solve": flops_survey,
         "sr_iters": sr_iters,
         "cpu_baseline": cpu,
         "fp64_form": fp64,

@@ -150,10 +150,27 @@ typedef struct negf_stats {
     double  phase_inv_ms;    /* all inverses (Sancho-Rubio and RGF)                        */
     double  phase_dens_ms;   /* density / spin reductions                                  */
     int64_t ns_extra_steps;  /* mixed form: Newton-Schulz matrix-steps beyond the two fixed
-                                ones (matrices whose residual was still above 1e-6)        */
+                                ones (matrices whose residual was still above ns_tol)      */
+    int64_t ns_unconverged;  /* mixed form: matrices still above ns_tol after ns_max_steps
+                                steps; each was inverted again in FP64 (also counted in
+                                fallbacks)                                                  */
+    double  ns_final_residual_max; /* mixed form: largest residual norm before the last
+                                update among the accepted inverses (<= ns_tol; the last
+                                update squares it)                                          */
 } negf_stats;
 NEGF_API int negf_profile(negf_handle* h, int enable);
 NEGF_API int negf_get_stats(negf_handle* h, negf_stats* out);
+
+/* Newton-Schulz policy of the mixed form's inverses (no reference counterpart: the
+ * reference's Invert_Matrix, Source/MKL_Routines_Cluster.F90:2-33, is a direct LU; its
+ * errorFlag contract is kept by redoing in FP64 any inverse this policy cannot certify).
+ * Each block is inverted in FP32 and refined by X <- X + X (I - W X); two steps always,
+ * more (up to ns_max_steps in all, 2..16) while the row-sum norm of I - W X before the
+ * latest update is above ns_tol.  A block is inverted again in FP64 when its first
+ * residual norm is above ns_accept (< 1), its FP32 factorisation met a zero pivot, or it
+ * is still above ns_tol after ns_max_steps steps.  Values <= 0 select the defaults
+ * (4, 1e-5, 0.5).  NEGF_ESTATE on an FP64 handle.                                      */
+NEGF_API int negf_set_refinement(negf_handle* h, int32_t ns_max_steps, double ns_tol, double ns_accept);
 
 /* ---- Hamiltonian upload ------------------------------------------------------------
  * Replaces the broadcast of Build_Hamiltonian's output to the solvers
@@ -402,10 +419,14 @@ NEGF_API int negf_zinv(int32_t n, const double* G, double* invG, int32_t batch);
  * cudaMalloc/cudaFree.  It calls no allocating routine; its scratch is one static device
  * array of NEGF_NOALLOC_SCRATCH_BYTES that every GPU loading the library holds until
  * exit, which limits m, n, k to NEGF_NOALLOC_MAX_DIM (larger sizes: NEGF_ESCRATCH).
- * The first call on each device looks up the array's device address (make it before any
- * stream capture).  All calls share the scratch: calls that overlap on the GPU race, so
- * the caller must order them.  Runs on `stream` (cudaStream_t, NULL = default stream) and
- * returns after the product is complete.                                               */
+ * A GPU holds the array from the first call on it (or from library load, when CUDA loads
+ * modules eagerly); that first call looks up the array's device address.  All calls
+ * share the scratch: calls that overlap on the GPU race, so the caller must order them.
+ * Runs on `stream` (cudaStream_t, NULL = default stream), then reads the device error
+ * flag and synchronises `stream`: it returns after the product is complete and cannot be
+ * captured into a CUDA graph.  The first beta = 0 call of each shape with 2k <= 800 also
+ * times the tensor-core kernel variants: it launches the product six times and waits for
+ * them before returning.                                                               */
 #define NEGF_NOALLOC_MAX_DIM      512
 #define NEGF_NOALLOC_MAX_SLICES   8
 #define NEGF_NOALLOC_SCRATCH_BYTES (26u * 1024u * 1024u)

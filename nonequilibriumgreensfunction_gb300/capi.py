@@ -33,7 +33,7 @@ NEGF_CONTACT_LEADS, NEGF_CONTACT_PBIG, NEGF_CONTACT_PSMALL, NEGF_CONTACT_SC = 0,
 # every symbol include/negf.h declares
 EXPORTED_SYMBOLS = (
     "negf_create", "negf_destroy", "negf_strerror", "negf_device_bytes",
-    "negf_set_stream", "negf_profile", "negf_get_stats",
+    "negf_set_stream", "negf_profile", "negf_get_stats", "negf_set_refinement",
     "negf_set_hamiltonian", "negf_build_hamiltonian", "negf_contact_self_energy", "negf_get_retarded_greens",
     "negf_copy_g_columns", "negf_calculate_gnp", "negf_calculate_observables",
     "negf_calculate_currents", "negf_calculate_resolved", "negf_solve_batch", "negf_solve_batch_ex",
@@ -113,7 +113,8 @@ class NegfStats(ctypes.Structure):
                 ("tc_complex_flops", c_double),
                 ("fallbacks", c_int64), ("ns_residual_max", c_double), ("f32_gemm_ms", c_double),
                 ("slice_ms", c_double), ("phase_sr_ms", c_double), ("phase_rgf_ms", c_double),
-                ("phase_inv_ms", c_double), ("phase_dens_ms", c_double), ("ns_extra_steps", c_int64)]
+                ("phase_inv_ms", c_double), ("phase_dens_ms", c_double), ("ns_extra_steps", c_int64),
+                ("ns_unconverged", c_int64), ("ns_final_residual_max", c_double)]
 
 
 class NegfServeParams(ctypes.Structure):
@@ -155,6 +156,7 @@ def _declare(lib):
         "negf_set_stream": (c_int, [h, c_void_p]),
         "negf_profile": (c_int, [h, c_int]),
         "negf_get_stats": (c_int, [h, POINTER(NegfStats)]),
+        "negf_set_refinement": (c_int, [h, c_int32, c_double, c_double]),
         "negf_set_hamiltonian": (c_int, [h, c_int32, _dp, _dp]),
         "negf_build_hamiltonian": (c_int, [h, c_int32, POINTER(NegfWireModel)]),
         "negf_contact_self_energy": (c_int, [h, c_double, _dp, _dp, _dp, _dp, _dp]),

@@ -164,8 +164,15 @@ int negf_profile(negf_handle* h, int enable) {
   }
   h->eng.fallbacks_ = 0;
   h->eng.ns_extra_ = 0;
+  h->eng.ns_unconverged_ = 0;
   h->eng.last_rnorm_max_ = 0.0;
+  h->eng.last_rk_max_ = 0.0;
   return NEGF_OK;
+}
+
+int negf_set_refinement(negf_handle* h, int32_t ns_max_steps, double ns_tol, double ns_accept) {
+  if (!h) return NEGF_EINVAL;
+  return h->eng.set_refinement(ns_max_steps, ns_tol, ns_accept);
 }
 
 int negf_get_stats(negf_handle* h, negf_stats* out) {
@@ -193,6 +200,8 @@ int negf_get_stats(negf_handle* h, negf_stats* out) {
   out->fallbacks = h->eng.fallbacks_;
   out->ns_residual_max = h->eng.last_rnorm_max_;
   out->ns_extra_steps = h->eng.ns_extra_;
+  out->ns_unconverged = h->eng.ns_unconverged_;
+  out->ns_final_residual_max = h->eng.last_rk_max_;
   return NEGF_OK;
 }
 

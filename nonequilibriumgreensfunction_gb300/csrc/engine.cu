@@ -114,7 +114,8 @@ int Engine::init(const negf_params& p) {
   if (p.precision != NEGF_PREC_FP64 && p.precision != NEGF_PREC_MIXED) return NEGF_EINVAL;
   if (p.precision == NEGF_PREC_MIXED && p.mixed_slices != 0 && !tc_supported_slices(p.mixed_slices))
     return NEGF_EINVAL;
-  if (p.precision == NEGF_PREC_MIXED && 2 * p.norb * p.npy * p.npz >= 4096) return NEGF_EINVAL;
+  // the tensor-core products keep exact accumulators up to K' = 2 M = 1600
+  if (p.precision == NEGF_PREC_MIXED && 2 * padded_k(p.norb * p.npy * p.npz) > 1600) return NEGF_EINVAL;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return NEGF_ENODEV;
   if (p.device < 0 || p.device >= ndev) return NEGF_EINVAL;
@@ -400,8 +401,10 @@ int Engine::merge_info(int batch) { return merge_info_kernel_launch(batch, inv_.
 // In-place inverse of `batch` matrices at stride sA; INFO of singular ones merged into
 // status_dev.  FP64 form: blocked Gauss-Jordan.  Mixed form: FP32 Gauss-Jordan, then
 // ns_steps_ Newton-Schulz steps X <- X + X (I - W X) with W X formed at s_res_ slices
-// (FP64-class) and X R at s_upd_ slices; a matrix whose first residual norm is above
-// ns_accept_ (or whose FP32 factorisation met a zero pivot) is inverted again in FP64.
+// (FP64-class) and X R at s_upd_ slices, and up to ns_max_steps_ in all for a matrix whose
+// residual norm before its last update is above ns_tol_.  A matrix is inverted again in
+// FP64 when its first residual norm is above ns_accept_, its FP32 factorisation met a zero
+// pivot, or it is still above ns_tol_ after ns_max_steps_ steps.
 int Engine::invert(double2* A, long long sA, int batch, int* status_dev) {
   cudaEvent_t ph;
   timed_begin(st_, TK_PH_INV, 0.0, &ph);
@@ -447,10 +450,13 @@ int Engine::invert_impl(double2* A, long long sA, int batch, int* status_dev) {
   // proportional to the matrices that need it, and each matrix's result depends only on
   // its own residuals, never on the rest of the batch.
   std::vector<int> act;
+  // rlast[b]: matrix b's residual norm before its last update (the update squares it)
+  std::vector<double> rlast(batch);
   for (int b = 0; b < batch; ++b) {
+    rlast[b] = __longlong_as_double_host(rk[b]);
     const double r = __longlong_as_double_host(r0[b]);
     if (info32[b] != 0 || !(r <= ns_accept_)) continue;     // redone in FP64 below
-    if (__longlong_as_double_host(rk[b]) > ns_tol_) act.push_back(b);
+    if (!(rlast[b] <= ns_tol_)) act.push_back(b);
   }
   for (int step = ns_steps_; step < ns_max_steps_ && !act.empty(); ++step) {
     const int na = (int)act.size();
@@ -470,17 +476,29 @@ int Engine::invert_impl(double2* A, long long sA, int batch, int* status_dev) {
     NEGF_TRY(scatter_strided(M_, na, dNsX_, MM_, dNsIdx_, A, sA, st_));
     NEGF_CUDA_TRY(cudaStreamSynchronize(st_));
     std::vector<int> next;
-    for (int i = 0; i < na; ++i)
-      if (__longlong_as_double_host(rk[i]) > ns_tol_) next.push_back(act[i]);
+    for (int i = 0; i < na; ++i) {
+      rlast[act[i]] = __longlong_as_double_host(rk[i]);
+      if (!(rlast[act[i]] <= ns_tol_)) next.push_back(act[i]);
+    }
     act.swap(next);
   }
   NEGF_CUDA_TRY(cudaStreamSynchronize(st_));
-  double worst = 0.0;
+  // A matrix still in `act` took ns_max_steps_ steps and its residual norm before the last
+  // update stayed above ns_tol_: its inverse is not FP64-class, so it joins the FP64 redo
+  // with the matrices that failed the first test, and never leaves this call unflagged.
+  std::vector<char> unconv(batch, 0);
+  for (int b : act) unconv[b] = 1;
+  ns_unconverged_ += (long long)act.size();
+  double worst = 0.0, worst_last = 0.0;
   std::vector<int> bad;
   for (int b = 0; b < batch; ++b) {
     const double r = __longlong_as_double_host(r0[b]);
-    if (info32[b] != 0 || !(r <= ns_accept_)) bad.push_back(b);
-    else if (r > worst) worst = r;
+    if (info32[b] != 0 || !(r <= ns_accept_) || unconv[b]) {
+      bad.push_back(b);
+    } else {
+      worst = std::max(worst, r);
+      worst_last = std::max(worst_last, rlast[b]);
+    }
   }
   if (!bad.empty()) {
     // FP64 inverses of the saved matrices, all failures of this call in one batched call
@@ -497,6 +515,21 @@ int Engine::invert_impl(double2* A, long long sA, int batch, int* status_dev) {
     fallbacks_ += nb;
   }
   last_rnorm_max_ = std::max(last_rnorm_max_, worst);
+  last_rk_max_ = std::max(last_rk_max_, worst_last);
+  return NEGF_OK;
+}
+
+int Engine::set_refinement(int max_steps, double tol, double accept) {
+  if (!mixed_) return NEGF_ESTATE;
+  // the two fixed steps stay; at most 16 in all.  A residual norm below 1 is what makes
+  // the Newton-Schulz iteration converge, so the acceptance bound must stay below it.
+  const int ms = max_steps <= 0 ? 4 : max_steps;
+  const double t = tol <= 0.0 ? 1e-5 : tol;
+  const double a = accept <= 0.0 ? 0.5 : accept;
+  if (ms < ns_steps_ || ms > 16 || !(t < 1.0) || !(a < 1.0)) return NEGF_EINVAL;
+  ns_max_steps_ = ms;
+  ns_tol_ = t;
+  ns_accept_ = a;
   return NEGF_OK;
 }
 

@@ -160,9 +160,13 @@ class Engine {
   int* dNsIdx_ = nullptr;     // matrices still taking Newton-Schulz steps beyond ns_steps_
   double2 *dNsX_ = nullptr, *dNsW_ = nullptr;   // their X and W, gathered into a compact batch
   long long ns_extra_ = 0;    // matrix-steps taken beyond ns_steps_ (statistics)
+  long long ns_unconverged_ = 0;   // matrices still above ns_tol_ after ns_max_steps_ (redone in FP64)
+  double last_rk_max_ = 0.0;       // largest residual norm before the last update of an accepted matrix
   int* dTcErr_ = nullptr;
   long long fallbacks_ = 0;
   double last_rnorm_max_ = 0.0;
+  // Newton-Schulz policy of the mixed form (negf_set_refinement); <= 0 restores a default
+  int set_refinement(int max_steps, double tol, double accept);
   int invert(double2* A, long long sA, int batch, int* status_dev);
   int invert_impl(double2* A, long long sA, int batch, int* status_dev);
   int solve_sr_impl(const std::vector<SrJob>& jobs, std::vector<int>& status, std::vector<int>& iters);

@@ -7,18 +7,24 @@
 // synchronise the whole device.  negf_zgemm allocates its slice planes on every call; this
 // variant keeps them in one static device array instead.
 //
-// The scratch is a file-scope __device__ array of NEGF_NOALLOC_SCRATCH_BYTES (about 26 MB):
-// every GPU that loads the library holds it until the process exits.  It bounds the
-// problem size: m, n, k <= NEGF_NOALLOC_MAX_DIM and slices <= NEGF_NOALLOC_MAX_SLICES.
-// All calls share it and it keeps the previous call's contents, so calls that overlap on
-// the GPU (different streams or host threads without ordering) race on it; calls must be
+// The scratch is a file-scope __device__ array of NEGF_NOALLOC_SCRATCH_BYTES (about 26 MB).
+// A GPU holds it from the first negf_zgemm_noalloc call on that device (or from library
+// load, when CUDA loads modules eagerly) until the process exits.  It bounds the problem
+// size: m, n, k <= NEGF_NOALLOC_MAX_DIM and slices <= NEGF_NOALLOC_MAX_SLICES.  All calls
+// share it and it keeps the previous call's contents, so calls that overlap on the GPU
+// (different streams or host threads without ordering) race on it; calls must be
 // serialised by the caller.  The slicing kernels overwrite every scratch byte a call reads,
 // and the device error flag is cleared at the start of each call.
 //
 // Host code may not use the array's name as a device address (on the host it names a
 // shadow object): the first call on each device, with that device current, resolves the
-// device address with cudaGetSymbolAddress and caches it.  That first call should
-// therefore be made before any stream capture begins.
+// device address with cudaGetSymbolAddress and caches it.
+//
+// Every call ends by copying the device error flag to the host and synchronising
+// `stream`, so it blocks until the product is complete and cannot be recorded into a CUDA
+// graph.  The first beta = 0 call of each shape with K' = 2k <= 800 also runs the kernel
+// variant choice of the tensor-core GEMM: it launches the product six times on `stream`
+// and waits for their events before it returns.
 #include <mutex>
 
 #include "engine.h"

@@ -10,8 +10,11 @@
 //     [Cr | Ci] = [Ar  Ai] [[Br, Bi], [-Bi, Br]]      (K' = 2K, N' = 2N),
 // the slice products S_p T_q are integer matrices with |entries| <= K' * 2^12.  The MMAs
 // of one anti-diagonal d = p + q (at most S pairs) accumulate into one FP32 TMEM
-// accumulator; for d < 5 and K' <= 800 every partial sum stays below 2^24, so those
-// accumulators are EXACT (products of 7-bit integers and their sums are representable).
+// accumulator; for d < 5 and K' <= 800 every partial sum stays below (d+1) 800 2^12 < 2^24,
+// so those accumulators are EXACT (products of 7-bit integers and their sums are
+// representable).  For 800 < K' <= 1600 (M up to 800) the K blocks are split in two halves
+// of at most 800, each accumulated into its own set of TMEM accumulators and summed in
+// int64 by the epilogue, so the same argument holds per half; K' > 1600 is refused.
 // Higher diagonals carry weight <= 2^-35 and their rounding is far below FP64 epsilon of
 // the leading term.  The epilogue recombines sum_d acc_d 2^(7(S-1-d)) in int64 (two words
 // for S >= 7, each converted and then added), converts to FP64 and scales by
@@ -403,8 +406,9 @@ __global__ void __launch_bounds__(256) slice_b_kernel(const double2* B, int ldb,
 // ---------------------------------------------------------------------------------
 // MINB = CTAs resident per SM: 1 (deep pipeline, up to 200 KB of stages) or 2 (two CTAs
 // share an SM, so one's prologue/epilogue overlaps the other's MMAs; <= 110 KB of stages
-// and <= 256 TMEM columns each)
-template <int S, int NT, int MINB = 1>
+// and <= 256 TMEM columns each).  KS = accumulator sets along K: 2 splits the K blocks in
+// two halves of at most 800 K' each (exact accumulators for 800 < K' <= 1600).
+template <int S, int NT, int MINB = 1, int KS = 1>
 struct TcCfg {
   static constexpr int A_TILE = TILE_M * ROW_BYTES;            // bytes of one A slice tile
   static constexpr int B_TILE = NT * ROW_BYTES;                // bytes of one B slice tile
@@ -415,12 +419,13 @@ struct TcCfg {
 #endif
   static constexpr int STAGES = BUDGET / STAGE > TC_MAX_STAGES ? TC_MAX_STAGES : BUDGET / STAGE;
   static constexpr int SMEM = STAGES * STAGE + 1024 + 256 + 4 * (NT / 2);   // + alignment, barriers, exponents
-  static constexpr int TMEM_COLS_USED = S * NT;
+  static constexpr int TMEM_COLS_USED = KS * S * NT;
   static constexpr int TMEM_COLS = TMEM_COLS_USED <= 32 ? 32 : TMEM_COLS_USED <= 64 ? 64
                                  : TMEM_COLS_USED <= 128 ? 128 : TMEM_COLS_USED <= 256 ? 256 : 512;
   static_assert(STAGES >= 2, "at least two stages");
   static_assert(TMEM_COLS_USED <= 512 / MINB, "TMEM holds 512 columns per SM");
   static_assert(NT % 16 == 0 && NT >= 16 && NT <= 256, "UMMA N");
+  static_assert(KS == 1 || KS == 2, "one or two accumulator sets along K");
 };
 
 struct TcArgs {
@@ -438,10 +443,10 @@ struct TcArgs {
   int* err;
 };
 
-template <int S, int NT, int MINB>
+template <int S, int NT, int MINB, int KS>
 __global__ void __launch_bounds__(TC_THREADS, MINB)
     zgemm_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, TcArgs a) {
-  using Cfg = TcCfg<S, NT, MINB>;
+  using Cfg = TcCfg<S, NT, MINB, KS>;
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + Cfg::STAGES * Cfg::STAGE);
@@ -454,6 +459,9 @@ __global__ void __launch_bounds__(TC_THREADS, MINB)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int tm = blockIdx.x, tn = blockIdx.y, b = blockIdx.z;
   const int nk = (a.kp + BK - 1) / BK;
+  // K blocks [0, ksplit) accumulate into set 0, [ksplit, nk) into set 1 (KS = 2 only)
+  const int ksplit = KS == 1 ? nk : (nk + 1) / 2;
+  const int nsets = (KS == 2 && ksplit < nk) ? 2 : 1;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < Cfg::STAGES; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
@@ -521,6 +529,9 @@ __global__ void __launch_bounds__(TC_THREADS, MINB)
         // address field (bits 0-13, address >> 4), and shared addresses stay below 2^18,
         // so a tile's descriptor is the base plus its byte offset >> 4
         const uint64_t da0 = make_desc(sa), db0 = make_desc(sb);
+        const bool second = KS == 2 && kb >= ksplit;
+        const uint32_t acc_base = tmem + (second ? (uint32_t)(S * NT) : 0u);
+        const bool first_kb = kb == (second ? ksplit : 0);   // the set's first K block overwrites it
 #pragma unroll
         for (int d = 0; d < S; ++d) {
 #pragma unroll
@@ -530,8 +541,8 @@ __global__ void __launch_bounds__(TC_THREADS, MINB)
             for (int kk = 0; kk < BK / 16; ++kk) {
               const uint64_t da = da0 + (uint64_t)((p * Cfg::A_TILE + kk * 32) >> 4);
               const uint64_t db = db0 + (uint64_t)((q * Cfg::B_TILE + kk * 32) >> 4);
-              const uint32_t acc = (kb > 0 || p > 0 || kk > 0) ? 1u : 0u;
-              tc_mma(tmem + d * NT, da, db, idesc, acc);
+              const uint32_t acc = (!first_kb || p > 0 || kk > 0) ? 1u : 0u;
+              tc_mma(acc_base + d * NT, da, db, idesc, acc);
             }
           }
         }
@@ -565,25 +576,29 @@ __global__ void __launch_bounds__(TC_THREADS, MINB)
 #pragma unroll
       for (int i = 0; i < CW; ++i) { hi[i] = 0; lo[i] = 0; }
       if (ok) {
-        // all S accumulator reads of this chunk in flight together, one wait
-        uint32_t raw[S][CW];
+        // all S accumulator reads of this chunk (per K set) in flight together, one wait;
+        // the sets' exact integer values add in int64
+#pragma unroll 1
+        for (int set = 0; set < nsets; ++set) {
+          uint32_t raw[S][CW];
 #pragma unroll
-        for (int d = 0; d < S; ++d) {
-          const uint32_t ta = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(d * NT + c0);
+          for (int d = 0; d < S; ++d) {
+            const uint32_t ta = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(set * S * NT + d * NT + c0);
 #pragma unroll
-          for (int h = 0; h < CW / 8; ++h) {
-            uint32_t (&r8)[8] = *reinterpret_cast<uint32_t(*)[8]>(&raw[d][8 * h]);
-            tmem_ld8_nowait(ta + 8 * h, r8);
+            for (int h = 0; h < CW / 8; ++h) {
+              uint32_t (&r8)[8] = *reinterpret_cast<uint32_t(*)[8]>(&raw[d][8 * h]);
+              tmem_ld8_nowait(ta + 8 * h, r8);
+            }
           }
-        }
-        tmem_wait_ld();
+          tmem_wait_ld();
 #pragma unroll
-        for (int d = 0; d < S; ++d) {
+          for (int d = 0; d < S; ++d) {
 #pragma unroll
-          for (int i = 0; i < CW; ++i) {
-            const long long q = (long long)acc_to_int(raw[d][i]);
-            if (d < DH) hi[i] += q * (1LL << (7 * (DH - 1 - d)));
-            else lo[i] += q * (1LL << (7 * (S - 1 - d)));
+            for (int i = 0; i < CW; ++i) {
+              const long long q = (long long)acc_to_int(raw[d][i]);
+              if (d < DH) hi[i] += q * (1LL << (7 * (DH - 1 - d)));
+              else lo[i] += q * (1LL << (7 * (S - 1 - d)));
+            }
           }
         }
       }
@@ -925,19 +940,22 @@ int make_map(CUtensorMap* map, const void* base, int kp, long long rows, int box
 #define TC_MINB7 1
 #endif
 
-template <int S, int NT, int MINB>
+template <int S, int NT, int MINB, int KS = 1>
 int launch_mma(const SlicedOperand& A, const SlicedOperand& B, const TcArgs& args, cudaStream_t st) {
-  using Cfg = TcCfg<S, NT, MINB>;
+  using Cfg = TcCfg<S, NT, MINB, KS>;
+  // one set of accumulators holds at most 800 K' exactly (two sets: 1600)
+  if (args.kp > 800 * KS) return NEGF_EINVAL;
   CUtensorMap ma, mb;
   NEGF_TRY(make_map(&ma, A.data, args.kp, (long long)args.batch * args.planesA * args.rowsA, TILE_M));
   NEGF_TRY(make_map(&mb, B.data, args.kp, (long long)args.batch * args.planesB * args.rowsB, NT));
-  NEGF_CUDA_TRY(cudaFuncSetAttribute(zgemm_tc_kernel<S, NT, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM));
+  NEGF_CUDA_TRY(
+      cudaFuncSetAttribute(zgemm_tc_kernel<S, NT, MINB, KS>, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM));
   dim3 grid((args.m + TILE_M - 1) / TILE_M, (unsigned)((2LL * args.n + NT - 1) / NT), args.batch);
   cudaEvent_t ev;
   const double cflops = 8.0 * args.m * (double)args.n * (args.kp / 2) * args.batch;
   add_tc_complex_flops(cflops);
   timed_begin(st, TK_TC, cflops * (S * (S + 1) / 2), &ev);
-  zgemm_tc_kernel<S, NT, MINB><<<grid, TC_THREADS, Cfg::SMEM, st>>>(ma, mb, args);
+  zgemm_tc_kernel<S, NT, MINB, KS><<<grid, TC_THREADS, Cfg::SMEM, st>>>(ma, mb, args);
   NEGF_CUDA_TRY(cudaGetLastError());
   timed_end(st, TK_TC, ev);
   count_launch();
@@ -1098,7 +1116,8 @@ int choose_variant(int S, const SlicedOperand& A, const SlicedOperand& B, const 
     auto it = g_tune.find(key);
     if (it != g_tune.end()) return it->second;
   }
-  if (args.beta_kind != 0) return 0;
+  // beyond K' = 800 only the per-tile kernel splits its accumulators along K
+  if (args.beta_kind != 0 || args.kp > 800) return 0;
   // two timings each, after a first run of each that pays one-time costs
   float best[2] = {1e30f, 1e30f};
   for (int rep = 0; rep < 3; ++rep)
@@ -1120,9 +1139,9 @@ int zgemm_tc(const SlicedOperand& A, const SlicedOperand& B, double2 alpha, doub
   const int S = slices ? slices : A.slices;
   if (S > A.slices || S > B.slices || (!slices && A.slices != B.slices)) return NEGF_EINVAL;
   if (A.k != B.k || A.batch != B.batch) return NEGF_EINVAL;
-  // the leading accumulator (one pair) is exact for K' * 2^12 < 2^24; larger K would
-  // round it and lose the FP64-class tail
-  if (2 * A.k >= 4096) return NEGF_EINVAL;
+  // every accumulator is exact for K' <= 800 per accumulator set, and the per-tile kernel
+  // has at most two sets along K
+  if (2 * A.k > 1600) return NEGF_EINVAL;
   TcArgs args{};
   args.m = A.rows; args.n = B.rows / 2; args.kp = 2 * A.k; args.batch = A.batch;
   args.rowsA = A.rows; args.rowsB = B.rows;
@@ -1133,7 +1152,7 @@ int zgemm_tc(const SlicedOperand& A, const SlicedOperand& B, double2 alpha, doub
   args.alpha_one = (alpha.x == 1.0 && alpha.y == 0.0) ? 1 : 0;
   args.beta_kind = (beta.x == 0.0 && beta.y == 0.0) ? 0 : (beta.x == 1.0 && beta.y == 0.0) ? 1 : 2;
 #if TC_PERSIST
-  switch (S) {
+  if (args.kp <= 800) switch (S) {
     case 2: return launch_persistent<2, 128>(A, B, args, st);
     case 3: return launch_persistent<3, 80>(A, B, args, st);
     case 4: return launch_persistent<4, 64>(A, B, args, st);
@@ -1142,7 +1161,7 @@ int zgemm_tc(const SlicedOperand& A, const SlicedOperand& B, double2 alpha, doub
     case 7: return launch_persistent<7, 32>(A, B, args, st);
     case 8: return launch_persistent<8, 32>(A, B, args, st);
   }
-  return NEGF_EINVAL;
+  if (args.kp <= 800) return NEGF_EINVAL;
 #endif
   const int variant = choose_variant(S, A, B, args, st);
   if (variant == -2) return NEGF_OK;        // the tuning runs computed C
@@ -1165,6 +1184,18 @@ int launch_persistent_s(int S, const SlicedOperand& A, const SlicedOperand& B, c
 }
 
 int launch_per_tile_s(int S, const SlicedOperand& A, const SlicedOperand& B, const TcArgs& args, cudaStream_t st) {
+  if (args.kp > 800) {
+    // two accumulator sets along K, one CTA per SM: 2 S NT <= 512 TMEM columns
+    switch (S) {
+      case 3: return launch_mma<3, 80, 1, 2>(A, B, args, st);
+      case 4: return launch_mma<4, 64, 1, 2>(A, B, args, st);
+      case 5: return launch_mma<5, 48, 1, 2>(A, B, args, st);
+      case 6: return launch_mma<6, 32, 1, 2>(A, B, args, st);
+      case 7: return launch_mma<7, 32, 1, 2>(A, B, args, st);
+      case 8: return launch_mma<8, 32, 1, 2>(A, B, args, st);
+    }
+    return NEGF_EINVAL;
+  }
   switch (S) {
     case 2: return launch_mma<2, 128, 2>(A, B, args, st);   // internal: small corrections
     case 3: return launch_mma<3, TC_NT3, TC_MINB3>(A, B, args, st);

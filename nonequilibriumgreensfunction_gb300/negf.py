@@ -128,6 +128,15 @@ class Solver:
     def profile(self, enable=True):
         check(self.lib.negf_profile(self._h, 1 if enable else 0), "negf_profile")
 
+    def set_refinement(self, ns_max_steps=0, ns_tol=0.0, ns_accept=0.0):
+        """Newton-Schulz policy of the mixed form (negf_set_refinement): at most
+        ``ns_max_steps`` refinement steps per inverse, more than the two fixed ones while
+        the residual norm before the latest update is above ``ns_tol``; an inverse whose
+        first residual norm is above ``ns_accept``, or that is still above ``ns_tol`` after
+        the last step, is redone in FP64.  0 selects a default (4, 1e-5, 0.5)."""
+        check(self.lib.negf_set_refinement(self._h, int(ns_max_steps), float(ns_tol), float(ns_accept)),
+              "negf_set_refinement")
+
     def stats(self):
         st = capi.NegfStats()
         check(self.lib.negf_get_stats(self._h, ctypes.byref(st)), "negf_get_stats")

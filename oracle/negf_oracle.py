@@ -193,12 +193,33 @@ class SolveOptions:
     delta_sc: tuple = (1e-3, 1e-3)           # DeltaSCL, DeltaSCR, Read_In_Allocate.F90:74-75
     chi_lr: float = 0.8                      # Read_In_Allocate.F90:72
     gds: Optional[np.ndarray] = None         # None -> reference_gds()
+    # The reference's Sancho-Rubio iteration counter is an implicitly SAVEd local,
+    # ``INTEGER(4) :: counter=1`` (Contact_Self_Energy.F90:119): it is initialised once per
+    # process and every iteration of every call increments it (:155), so the loop test
+    # ``counter <= 20000`` (:154) caps the iterations of the whole process, not of one call.
+    # None (default): a counter per call, the cap sr_max_iter per call.  An SrCounter:
+    # the reference's process-wide counter, shared by every call given the same object.
+    sr_counter: Optional["SrCounter"] = None
 
     @property
     def nh(self) -> int:
         """Electron orbitals per site: Norb, or half of it for the BdG Hamiltonian
         (Read_In_Allocate.F90:67-71)."""
         return self.norb // 2 if self.contact_type == 3 else self.norb
+
+
+@dataclasses.dataclass
+class SrCounter:
+    """The reference's SAVEd Sancho-Rubio counter (Contact_Self_Energy.F90:119,154-155).
+
+    ``value`` starts at 1 as in the reference and keeps its value between calls.  Once the
+    iterations of all calls so far have taken it past 20000, the loop body of every later
+    call is skipped: CapT stays t (the first term of Eq. 16, :151) and Sigma is formed from
+    it without decimation.  A single-process run reaches this after about 20000 / (2 n_SR)
+    energies (about 400-500 at n_SR = 20-25); the reference's 72-rank production run gives
+    each rank about 9 energies and never does.  The cap test ``counter == 20000`` (:202)
+    can fire only when a call converges exactly at that count."""
+    value: int = 1
 
 
 def fermi(energy: float, mu_c: float, kT: float) -> float:
@@ -227,12 +248,14 @@ def invert_matrix(g: np.ndarray):
 # ---------------------------------------------------------------------------
 # Sancho-Rubio, Source/Contact_Self_Energy.F90:110-223
 # ---------------------------------------------------------------------------
-def sancho_rubio(alpha: np.ndarray, beta: np.ndarray, eta: float, tol: float, max_iter: int):
+def sancho_rubio(alpha: np.ndarray, beta: np.ndarray, eta: float, tol: float, max_iter: int,
+                 counter_state: Optional[SrCounter] = None):
     """Lopez-Sancho/Rubio decimation.  Returns (Sigma, error_flag, iterations).
 
-    The iteration counter is local to the call; in the reference it is an implicitly
-    SAVEd ``INTEGER :: counter=1`` (Contact_Self_Energy.F90:119) shared by all calls, a
-    difference that only matters when the 20000-iteration cap is hit.
+    Without ``counter_state`` the iteration counter is local to the call and max_iter caps
+    each call.  With it, the counter is the reference's SAVEd one (Contact_Self_Energy.F90:
+    119): it starts from ``counter_state.value``, is stored back at the end, and the cap
+    max_iter applies to the sum over all calls sharing the state (see SrCounter).
     """
     nn = alpha.shape[0]
     ident = np.eye(nn, dtype=complex)
@@ -244,7 +267,8 @@ def sancho_rubio(alpha: np.ndarray, beta: np.ndarray, eta: float, tol: float, ma
     cap_t = t.copy()                    # :151
     toldt = ident.copy()                # :152
     change_max = 1.0                    # change initialised to c1, :135
-    counter = 1
+    counter = 1 if counter_state is None else counter_state.value
+    counter0 = counter
     while counter <= max_iter and change_max > tol:       # :154
         counter += 1
         toldt = toldt @ tt                                  # :157-158
@@ -258,14 +282,18 @@ def sancho_rubio(alpha: np.ndarray, beta: np.ndarray, eta: float, tol: float, ma
         cap_t = cap_t + change                              # :180
         abs_change = np.abs(change)
         if np.isnan(abs_change).any():                      # :182-191
-            return None, 1, counter - 1
+            if counter_state is not None:
+                counter_state.value = counter
+            return None, 1, counter - counter0
         change_max = float(abs_change.max())
+    if counter_state is not None:
+        counter_state.value = counter
     cmat1 = beta @ cap_t + alpha                            # :195-196
     gfinal, err = invert_matrix(cmat1)                      # :197
     if counter == max_iter:                                 # :202-205
         err = 1
     sigma = (beta @ gfinal) @ beta.conj().T                 # :208-209
-    return sigma, err, counter - 1
+    return sigma, err, counter - counter0
 
 
 # ---------------------------------------------------------------------------
@@ -283,9 +311,10 @@ def contact_self_energy(htotd, hopx, energy, opt: SolveOptions, npy=None):
         sig_l, sig_r = model_contact_self_energy(m, npy, ce, opt)
         return _finish_contacts(sig_l, sig_r, np.zeros(2, dtype=int), np.zeros(2, dtype=int))
     alpha = -htotd[0] + ident * ce                          # :71-74
-    sig_l, err_l, it_l = sancho_rubio(alpha, -hopx.conj().T, opt.eta, opt.sr_tol, opt.sr_max_iter)
+    sig_l, err_l, it_l = sancho_rubio(alpha, -hopx.conj().T, opt.eta, opt.sr_tol, opt.sr_max_iter,
+                                      opt.sr_counter)
     alpha = -htotd[npx - 1] + ident * ce                    # :83-86
-    sig_r, err_r, it_r = sancho_rubio(alpha, -hopx, opt.eta, opt.sr_tol, opt.sr_max_iter)
+    sig_r, err_r, it_r = sancho_rubio(alpha, -hopx, opt.eta, opt.sr_tol, opt.sr_max_iter, opt.sr_counter)
     if sig_l is None or sig_r is None:
         raise FloatingPointError("Sancho_Rubio produced NaN")
     return _finish_contacts(sig_l, sig_r, np.array([err_l, err_r]), np.array([it_l, it_r]))

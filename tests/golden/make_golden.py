@@ -54,6 +54,16 @@ CASES = {
     "c2_sub": dict(npx=100, npy=10, npz=10, basis="tau_sigma", zeeman=0.01, flux=0.5, W=0.1, seed=1,
                    eta=1e-5, sr_tol=1e-10, kT=0.025, mu_lead=(0.005, -0.005),
                    energies=[-0.1, 0.0037], dE=0.6 / 511, calc_spin=True),
+    # BASELINE config 5 cross-section (Npy = Npz = 12, M = 576) on a short wire: products
+    # with K' = 2M = 1152 > 800, where the tensor-core GEMM splits its accumulators along K
+    "m576": dict(npx=8, npy=12, npz=12, basis="tau_sigma", zeeman=0.01, flux=0.5, W=0.1, seed=5,
+                 eta=1e-5, sr_tol=1e-10, kT=0.025, mu_lead=(0.025, -0.025),
+                 energies=[-0.262, 0.0021, 0.147], dE=0.6 / 1023, calc_spin=True),
+    # the largest cross-section of BASELINE config 4 (Npy = Npz = 14, M = 784, K' = 1568),
+    # the strongest disorder and flux of that mix
+    "m784": dict(npx=6, npy=14, npz=14, basis="tau_sigma", zeeman=0.01, flux=1.0, W=0.2, seed=7,
+                 eta=1e-5, sr_tol=1e-10, kT=0.025, mu_lead=(0.005, -0.005),
+                 energies=[-0.213, 0.0513], dE=0.6 / 1023, calc_spin=True),
 }
 
 

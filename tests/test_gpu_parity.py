@@ -85,7 +85,7 @@ def test_per_energy_interface_matches_oracle(need_gpu):
             assert_close(np.stack(spin), ref["SigExp"], "spin", floor=np.abs(ref["RhoN"]).max())
 
 
-@pytest.mark.parametrize("case", ["ref_debug", "flux_zeeman", "c1"])
+@pytest.mark.parametrize("case", ["ref_debug", "flux_zeeman", "c1", "m576", "m784"])
 def test_batch_matches_golden(case, need_gpu):
     mg = _mg()
     c = mg.CASES[case]

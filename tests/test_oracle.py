@@ -141,6 +141,33 @@ def test_sancho_rubio_iteration_cap_and_quirks():
     assert list(cse["sr_iters"]) == [1, 1]
 
 
+def test_saved_sancho_rubio_counter_caps_the_whole_process():
+    """The reference's SAVEd counter (Contact_Self_Energy.F90:119,154-155): calls sharing it
+    add up their iterations; once the sum passes 20000 a call does no decimation at all and
+    its Sigma comes from the first term alone, while a fresh per-call counter converges."""
+    htotd, hopx = _wire(npx=3)
+    per_call = O.SolveOptions(eta=1e-5, sr_tol=1e-10)
+    ref = O.contact_self_energy(htotd, hopx, 0.1, per_call)
+    n = int(ref["sr_iters"][0])
+    assert n > 3
+    # a fresh process: the shared counter gives the same result as the per-call one and
+    # advances by both leads' iterations
+    st = O.SrCounter()
+    shared = O.SolveOptions(eta=1e-5, sr_tol=1e-10, sr_counter=st)
+    a = O.contact_self_energy(htotd, hopx, 0.1, shared)
+    assert np.array_equal(a["SigmaL"], ref["SigmaL"]) and np.array_equal(a["SigmaR"], ref["SigmaR"])
+    assert st.value == 1 + int(ref["sr_iters"].sum())
+    # late in a long single-process run: the left lead gets 2 iterations, the right none
+    st.value = 20000 - 1
+    b = O.contact_self_energy(htotd, hopx, 0.1, shared)
+    assert list(b["sr_iters"]) == [2, 0] and st.value == 20001
+    err = np.abs(b["SigmaR"] - ref["SigmaR"]).max() / np.abs(ref["SigmaR"]).max()
+    assert err > 1e-3          # Sigma from CapT = t alone, far from the converged one
+    c = O.contact_self_energy(htotd, hopx, 0.1, shared)
+    assert list(c["sr_iters"]) == [0, 0]
+    assert np.array_equal(c["SigmaR"], b["SigmaR"])
+
+
 def test_energy_weights_follow_energy_sweep():
     eaxis, de0 = O.energy_axis_reference((-0.1, 0.0), 0.0, 600)
     w = O.energy_weights(eaxis, de0)

@@ -53,6 +53,44 @@ def test_noalloc_matches_allocating_gemm_on_two_calls(need_gpu):
         assert (np.abs(got - (alpha * (A @ B) + beta * C)) <= tol).all()
 
 
+def test_noalloc_first_beta_zero_call_of_a_shape_and_device_memory(need_gpu):
+    """beta = 0 on a shape no call has used yet: the first such call of a shape times the
+    kernel variants on the shared scratch before it keeps one, so two calls in a row (the
+    tuning call and a tuned one) must both match negf_zgemm and alpha A B.  Free device
+    memory must not move across a call: the entry point allocates nothing."""
+    torch = pytest.importorskip("torch")
+    lib = capi.load()
+    rng = np.random.default_rng(33)
+    m, n, k, S = 96, 200, 64, 7
+    alpha, beta = 1.0 - 0.25j, 0.0 + 0.0j
+    for rep in range(2):
+        A = rng.standard_normal((m, k)) + 1j * rng.standard_normal((m, k))
+        B = rng.standard_normal((k, n)) + 1j * rng.standard_normal((k, n))
+        C = np.full((m, n), np.nan + 0j)          # beta = 0: C is never read
+        rc, got = _noalloc(lib, torch, S, A, B, C, alpha, beta)   # first: the tuning call
+        assert rc == capi.NEGF_OK, capi.strerror(rc)
+        want = capi.zgemm(A, B, alpha=alpha, slices=S)
+        tol = abs(alpha) * _bound(A, B, S)
+        assert np.isfinite(got).all()
+        assert (np.abs(got - want) <= tol).all(), rep
+        assert (np.abs(got - alpha * (A @ B)) <= tol).all(), rep
+    # device buffers first, then free memory around two more calls of the same shape
+    dA = torch.from_numpy(np.ascontiguousarray(A.T)).cuda()
+    dB = torch.from_numpy(np.ascontiguousarray(B.T)).cuda()
+    dC = torch.zeros((n, m), dtype=torch.complex128, device="cuda")
+    al = np.array([alpha.real, alpha.imag])
+    be = np.array([0.0, 0.0])
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for _ in range(2):
+        rc = lib.negf_zgemm_noalloc(S, m, n, k, al.ctypes.data_as(capi._dp), ctypes.c_void_p(dA.data_ptr()), m,
+                                    ctypes.c_void_p(dB.data_ptr()), k, be.ctypes.data_as(capi._dp),
+                                    ctypes.c_void_p(dC.data_ptr()), m, None)
+        assert rc == capi.NEGF_OK
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
+
+
 def test_noalloc_rejects_sizes_beyond_its_scratch(need_gpu):
     torch = pytest.importorskip("torch")
     lib = capi.load()
