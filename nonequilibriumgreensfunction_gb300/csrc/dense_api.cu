@@ -47,15 +47,15 @@ int negf_zgemm(int32_t slices, int32_t m, int32_t n, int32_t k, const double* al
   } else {
     const int kp = padded_k(k);
     DevBuf sa, sb, ea, fb;
-    NEGF_TRY(sa.alloc(sliced_bytes(m, kp, slices, batch)));
-    NEGF_TRY(sb.alloc(sliced_bytes(2 * n, kp, slices, batch)));
+    NEGF_TRY(sa.alloc(sliced_bytes_a(m, kp, slices, batch)));
+    NEGF_TRY(sb.alloc(sliced_bytes_b(n, kp, slices, batch)));
     NEGF_TRY(ea.alloc(sizeof(int) * (size_t)m * batch));
     NEGF_TRY(fb.alloc(sizeof(int) * (size_t)n * batch));
     SlicedOperand oa, ob;
     oa.data = (__nv_bfloat16*)sa.p; oa.exps = (int*)ea.p;
     ob.data = (__nv_bfloat16*)sb.p; ob.exps = (int*)fb.p;
-    oa.data_bytes = sliced_bytes(m, kp, slices, batch); oa.exps_count = (size_t)m * batch;
-    ob.data_bytes = sliced_bytes(2 * n, kp, slices, batch); ob.exps_count = (size_t)n * batch;
+    oa.data_bytes = sliced_bytes_a(m, kp, slices, batch); oa.exps_count = (size_t)m * batch;
+    ob.data_bytes = sliced_bytes_b(n, kp, slices, batch); ob.exps_count = (size_t)n * batch;
     NEGF_TRY(slice_a((const double2*)dA.p, lda, (long long)sA, m, k, batch, slices, oa, st));
     NEGF_TRY(slice_b((const double2*)dB.p, ldb, (long long)sB, k, n, batch, slices, ob, st));
     NEGF_TRY(zgemm_tc(oa, ob, al, be, (double2*)dC.p, ldc, (long long)sC, (int*)dErr.p, st));

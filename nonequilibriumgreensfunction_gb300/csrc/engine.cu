@@ -209,20 +209,20 @@ int Engine::alloc() {
     NEGF_TRY(dalloc(&dW32_, (size_t)(cap * MM_), bytes_));
     NEGF_TRY(dalloc(&dT_, (size_t)(cap * MM_), bytes_));
     const int kp = padded_k(M_);
-    NEGF_TRY(dalloc(reinterpret_cast<char**>(&sa_.data), sliced_bytes(M_, kp, smax, cap), bytes_));
-    NEGF_TRY(dalloc(reinterpret_cast<char**>(&sb_.data), sliced_bytes(2 * M_, kp, smax, cap), bytes_));
-    NEGF_TRY(dalloc(reinterpret_cast<char**>(&sw_.data), sliced_bytes(M_, kp, smax, cap), bytes_));
+    NEGF_TRY(dalloc(reinterpret_cast<char**>(&sa_.data), sliced_bytes_a(M_, kp, smax, cap), bytes_));
+    NEGF_TRY(dalloc(reinterpret_cast<char**>(&sb_.data), sliced_bytes_b(M_, kp, smax, cap), bytes_));
+    NEGF_TRY(dalloc(reinterpret_cast<char**>(&sw_.data), sliced_bytes_a(M_, kp, smax, cap), bytes_));
     NEGF_TRY(dalloc(&sw_.exps, (size_t)cap * M_, bytes_));
     NEGF_TRY(dalloc(&sa_.exps, (size_t)cap * M_, bytes_));
     NEGF_TRY(dalloc(&sb_.exps, (size_t)cap * M_, bytes_));
-    NEGF_TRY(dalloc(reinterpret_cast<char**>(&sgl_.data), sliced_bytes(2 * M_, kp, s_rgf_, B_), bytes_));
-    NEGF_TRY(dalloc(reinterpret_cast<char**>(&sgr_.data), sliced_bytes(2 * M_, kp, s_rgf_, B_), bytes_));
+    NEGF_TRY(dalloc(reinterpret_cast<char**>(&sgl_.data), sliced_bytes_b(M_, kp, s_rgf_, B_), bytes_));
+    NEGF_TRY(dalloc(reinterpret_cast<char**>(&sgr_.data), sliced_bytes_b(M_, kp, s_rgf_, B_), bytes_));
     NEGF_TRY(dalloc(&sgl_.exps, (size_t)B_ * M_, bytes_));
     NEGF_TRY(dalloc(&sgr_.exps, (size_t)B_ * M_, bytes_));
-    sgl_.data_bytes = sgr_.data_bytes = sliced_bytes(2 * M_, kp, s_rgf_, B_);
+    sgl_.data_bytes = sgr_.data_bytes = sliced_bytes_b(M_, kp, s_rgf_, B_);
     sgl_.exps_count = sgr_.exps_count = (size_t)B_ * M_;
-    sa_.data_bytes = sw_.data_bytes = sliced_bytes(M_, kp, smax, cap);
-    sb_.data_bytes = sliced_bytes(2 * M_, kp, smax, cap);
+    sa_.data_bytes = sw_.data_bytes = sliced_bytes_a(M_, kp, smax, cap);
+    sb_.data_bytes = sliced_bytes_b(M_, kp, smax, cap);
     sa_.exps_count = sb_.exps_count = sw_.exps_count = (size_t)cap * M_;
     NEGF_TRY(dalloc(&dRnorm_, (size_t)cap, bytes_));
     NEGF_TRY(dalloc(&dNsIdx_, (size_t)cap, bytes_));
@@ -420,7 +420,7 @@ int Engine::invert_impl(double2* A, long long sA, int batch, int* status_dev) {
   }
   const double2 one = make_double2(1, 0), zero = make_double2(0, 0);
   NEGF_TRY(split_copy(M_, batch, A, sA, dWinv_, MM_, dW32_, MM_, st_));
-  NEGF_TRY(cinv_f32(dW32_, MM_, M_, batch, inv_, st_));
+  NEGF_TRY(invert_f32(batch));
   NEGF_TRY(to_f64(M_, batch, dW32_, MM_, A, sA, st_));
   std::vector<int> info32(batch);
   NEGF_CUDA_TRY(cudaMemcpyAsync(info32.data(), inv_.info, sizeof(int) * batch, cudaMemcpyDeviceToHost, st_));
@@ -517,6 +517,39 @@ int Engine::invert_impl(double2* A, long long sA, int batch, int* status_dev) {
   last_rnorm_max_ = std::max(last_rnorm_max_, worst);
   last_rk_max_ = std::max(last_rk_max_, worst_last);
   return NEGF_OK;
+}
+
+// The FP32 inverse of the dW32_ batch in the faster of the two Gauss-Jordan forms.  Both
+// give bitwise the same inverse, so the choice never changes a result: the first call of a
+// batch size that admits the fused form runs the three-launch form, restores dW32_ from
+// the saved FP64 matrices, runs the fused form and keeps the faster (timed with events on
+// the engine's stream).
+int Engine::invert_f32(int batch) {
+  if (!cinv_f32_fused_ok(M_, batch)) return cinv_f32(dW32_, MM_, M_, batch, inv_, st_, 0);
+  int bb = 1;
+  while (bb < batch) bb <<= 1;
+  auto it = gj_form_.find(bb);
+  if (it != gj_form_.end()) return cinv_f32(dW32_, MM_, M_, batch, inv_, st_, it->second);
+  cudaEvent_t ev[4];
+  for (int i = 0; i < 4; ++i)
+    if (cudaEventCreate(&ev[i]) != cudaSuccess) {
+      for (int j = 0; j < i; ++j) cudaEventDestroy(ev[j]);
+      return NEGF_ECUDA;
+    }
+  int rc = NEGF_OK;
+  float t0 = 0.f, t1 = 0.f;
+  cudaEventRecord(ev[0], st_);
+  rc = cinv_f32(dW32_, MM_, M_, batch, inv_, st_, 0);
+  cudaEventRecord(ev[1], st_);
+  if (rc == NEGF_OK) rc = to_f32(M_, batch, dWinv_, MM_, dW32_, MM_, st_);   // the same FP32 copy again
+  cudaEventRecord(ev[2], st_);
+  if (rc == NEGF_OK) rc = cinv_f32(dW32_, MM_, M_, batch, inv_, st_, 1);
+  cudaEventRecord(ev[3], st_);
+  if (rc == NEGF_OK && cudaEventSynchronize(ev[3]) == cudaSuccess && cudaEventElapsedTime(&t0, ev[0], ev[1]) ==
+      cudaSuccess && cudaEventElapsedTime(&t1, ev[2], ev[3]) == cudaSuccess)
+    gj_form_[bb] = t1 < t0 ? 1 : 0;
+  for (int i = 0; i < 4; ++i) cudaEventDestroy(ev[i]);
+  return rc;
 }
 
 int Engine::set_refinement(int max_steps, double tol, double accept) {

@@ -3,6 +3,7 @@
 #pragma once
 
 #include <array>
+#include <map>
 #include <vector>
 
 #include "negf_internal.cuh"
@@ -168,6 +169,10 @@ class Engine {
   // Newton-Schulz policy of the mixed form (negf_set_refinement); <= 0 restores a default
   int set_refinement(int max_steps, double tol, double accept);
   int invert(double2* A, long long sA, int batch, int* status_dev);
+  // FP32 Gauss-Jordan form per batch (rounded up to a power of two): 0 three launches per
+  // panel, 1 fused; chosen by timing both on the first inverse of that batch size
+  std::map<int, int> gj_form_;
+  int invert_f32(int batch);
   int invert_impl(double2* A, long long sA, int batch, int* status_dev);
   int solve_sr_impl(const std::vector<SrJob>& jobs, std::vector<int>& status, std::vector<int>& iters);
   int solve_rgf_impl(const std::vector<Item>& items, bool keep_columns);

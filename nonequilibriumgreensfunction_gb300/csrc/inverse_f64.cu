@@ -31,34 +31,25 @@ __device__ __forceinline__ void argmax_combine(V& v, int& i, V v2, int i2) {
   if (v2 > v || (v2 == v && i2 < i)) { v = v2; i = i2; }
 }
 
-// Panel stored column-major in shared memory: Ps[c * n + i], c in [0, kb), i in [0, n).
+// Factorisation of one n x kb panel held column-major in shared memory, Ps[c * n + i],
+// c in [0, kb), i in [0, n), by the whole CTA (blockDim.x a multiple of 32 and >= kb).
+// The pivot of each column is the first maximum of |re|+|im| (exact comparisons with the
+// lowest index winning ties), and every row is eliminated by one thread with the same
+// operations whatever the thread count, so the result does not depend on blockDim.
+// red_v / red_i hold one entry per warp.  Ends after a barrier.
 template <typename T>
-__global__ void __launch_bounds__(PANEL_THREADS) gj_panel_kernel(T* A, long long sA, int n, int k0, int kb,
-                                                                 int* ipiv, int* info) {
-  extern __shared__ __align__(16) unsigned char panel_raw[];
-  T* Ps = reinterpret_cast<T*>(panel_raw);
+__device__ __forceinline__ void panel_factor(T* Ps, int n, int k0, int kb, int* ip, int* info_b,
+                                             typename CplxTraits<T>::R* red_v, int* red_i, int* s_piv, T* s_d) {
   using R = typename CplxTraits<T>::R;
-  __shared__ R red_v[PANEL_THREADS / 32];
-  __shared__ int red_i[PANEL_THREADS / 32];
-  __shared__ int s_piv;
-  __shared__ T s_d;
-  const int b = blockIdx.x;
-  T* Ab = A + (long long)b * sA;
-  int* ip = ipiv + (long long)b * n;
-  const int t = threadIdx.x;
-  const int lane = t & 31, warp = t >> 5;
-
-  const T* src = Ab + (long long)k0 * n;
-  for (int e = t; e < n * kb; e += PANEL_THREADS) Ps[e] = src[e];
-  __syncthreads();
-
+  const int t = threadIdx.x, nth = blockDim.x;
+  const int lane = t & 31, warp = t >> 5, nwarps = nth >> 5;
   for (int c = 0; c < kb; ++c) {
     const int r = k0 + c;
     T* col = Ps + (long long)c * n;
     // ---- pivot search over rows r..n-1
     R bv = -1;
     int bi = n;
-    for (int i = r + t; i < n; i += PANEL_THREADS) argmax_combine(bv, bi, (R)cabs1(col[i]), i);
+    for (int i = r + t; i < n; i += nth) argmax_combine(bv, bi, (R)cabs1(col[i]), i);
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
       R ov = __shfl_down_sync(0xffffffffu, bv, off);
@@ -70,21 +61,21 @@ __global__ void __launch_bounds__(PANEL_THREADS) gj_panel_kernel(T* A, long long
     if (t == 0) {
       R v = red_v[0];
       int i = red_i[0];
-      for (int w = 1; w < PANEL_THREADS / 32; ++w) argmax_combine(v, i, red_v[w], red_i[w]);
+      for (int w = 1; w < nwarps; ++w) argmax_combine(v, i, red_v[w], red_i[w]);
       if (i >= n) i = r;
-      s_piv = i;
+      *s_piv = i;
       ip[r] = i;
       T pv = col[i];
       if (pv.x == 0 && pv.y == 0) {
-        if (info[b] == 0) info[b] = r + 1;
-        s_d = CplxTraits<T>::make(0, 0);
+        if (*info_b == 0) *info_b = r + 1;
+        *s_d = CplxTraits<T>::make(0, 0);
       } else {
-        s_d = crcp(pv);
+        *s_d = crcp(pv);
       }
     }
     __syncthreads();
-    const int p = s_piv;
-    const T d = s_d;
+    const int p = *s_piv;
+    const T d = *s_d;
     const bool singular = (d.x == 0 && d.y == 0);
     // ---- interchange rows r and p inside the panel, scale the pivot row
     if (t < kb) {
@@ -97,7 +88,7 @@ __global__ void __launch_bounds__(PANEL_THREADS) gj_panel_kernel(T* A, long long
     __syncthreads();
     if (singular) continue;
     // ---- eliminate column c from every other row; row i is owned by one thread
-    for (int i = t; i < n; i += PANEL_THREADS) {
+    for (int i = t; i < n; i += nth) {
       if (i == r) continue;
       const T f = col[i];
       for (int j = 0; j < kb; ++j) {
@@ -115,6 +106,26 @@ __global__ void __launch_bounds__(PANEL_THREADS) gj_panel_kernel(T* A, long long
     }
     __syncthreads();
   }
+}
+
+// One CTA per matrix: the panel [k0, k0 + kb) factorised in shared memory.
+template <typename T>
+__global__ void __launch_bounds__(PANEL_THREADS) gj_panel_kernel(T* A, long long sA, int n, int k0, int kb,
+                                                                 int* ipiv, int* info) {
+  extern __shared__ __align__(16) unsigned char panel_raw[];
+  T* Ps = reinterpret_cast<T*>(panel_raw);
+  using R = typename CplxTraits<T>::R;
+  __shared__ R red_v[PANEL_THREADS / 32];
+  __shared__ int red_i[PANEL_THREADS / 32];
+  __shared__ int s_piv;
+  __shared__ T s_d;
+  const int b = blockIdx.x;
+  T* Ab = A + (long long)b * sA;
+  const int t = threadIdx.x;
+  const T* src = Ab + (long long)k0 * n;
+  for (int e = t; e < n * kb; e += PANEL_THREADS) Ps[e] = src[e];
+  __syncthreads();
+  panel_factor<T>(Ps, n, k0, kb, ipiv + (long long)b * n, info + b, red_v, red_i, &s_piv, &s_d);
   T* dst = Ab + (long long)k0 * n;
   for (int e = t; e < n * kb; e += PANEL_THREADS) dst[e] = Ps[e];
 }
@@ -280,7 +291,137 @@ __global__ void gj_colswap_kernel(T* A, long long sA, int n, const int* ipiv) {
   }
 }
 
+// The whole FP32 Gauss-Jordan of one matrix in one CTA: for every panel, the panel
+// factorisation, its row interchanges and its rank-kb update, in the same order and with
+// the same operations per element as gj_panel + gj_swap + gj_update, so the inverse is
+// bitwise the same as the three-launch form's (the update's k order, its fused multiply-
+// adds and the final A + sum are those of gj_update_kernel).  It replaces 3 launches per
+// panel by one per inverse and keeps the panel in shared memory across its update.
+//   - the panel (n x 32 float2, up to 100 KB at n = 400) stays in shared memory;
+//   - the other columns are processed in chunks of 32: one warp per column applies the
+//     panel's interchanges (the same gather list as gj_swap) and moves rows K into the
+//     chunk's R slab (32 x 32 in shared memory), then all 256 threads update the chunk,
+//     each thread 4 rows x 8 columns of accumulators;
+//   - two CTAs share an SM, so one's serial panel steps overlap the other's updates.
+// Offered when the batch has at least one matrix per SM (below that the three-launch form
+// spreads a matrix over many SMs and always finishes first); the engine times both forms
+// on its first inverse of a shape and keeps the faster.  The column interchanges that end
+// the inverse stay a separate launch (gj_colswap_kernel).
+constexpr int FUSED_THREADS = 256, FUSED_JC = 32, FUSED_RS = FUSED_JC + 1, FUSED_MAX_N = 400;
+__global__ void __launch_bounds__(FUSED_THREADS, 2) gj_fused_f32_kernel(float2* A, long long sA, int n, int* ipiv,
+                                                                        int* info) {
+  extern __shared__ __align__(16) unsigned char fused_raw[];
+  float2* Ps = reinterpret_cast<float2*>(fused_raw);   // [32][n]: the panel, column-major
+  float2* Rs = Ps + 32 * n;                             // [32][FUSED_RS]: rows K of a chunk
+  __shared__ float red_v[FUSED_THREADS / 32];
+  __shared__ int red_i[FUSED_THREADS / 32];
+  __shared__ int s_piv, s_nt;
+  __shared__ float2 s_d;
+  __shared__ int trow[64], torig[64];
+  const int b = blockIdx.x;
+  float2* Ab = A + (long long)b * sA;
+  int* ip = ipiv + (long long)b * n;
+  const int t = threadIdx.x;
+  const int warp = t >> 5, lane = t & 31;
+  const int rg = t & 63, cg = t >> 6;                   // update: row group, column group
+  const float2 zero = make_float2(0.f, 0.f);
+  for (int k0 = 0; k0 < n; k0 += FUSED_JC) {
+    const int kb = n - k0 < FUSED_JC ? n - k0 : FUSED_JC;
+    const float2* src = Ab + (long long)k0 * n;
+    for (int e = t; e < n * kb; e += FUSED_THREADS) Ps[e] = src[e];
+    __syncthreads();
+    panel_factor<float2>(Ps, n, k0, kb, ip, info + b, red_v, red_i, &s_piv, &s_d);
+    float2* dst = Ab + (long long)k0 * n;
+    for (int e = t; e < n * kb; e += FUSED_THREADS) dst[e] = Ps[e];
+    if (t == 0) {   // the panel's interchanges as one gather over the touched rows (gj_swap)
+      int nt = kb;
+      for (int c = 0; c < kb; ++c) { trow[c] = k0 + c; torig[c] = k0 + c; }
+      for (int c = 0; c < kb; ++c) {
+        const int r = k0 + c, p = ip[r];
+        if (p == r) continue;
+        int ip_ = -1;
+        for (int q = 0; q < nt; ++q)
+          if (trow[q] == p) { ip_ = q; break; }
+        if (ip_ < 0) { ip_ = nt; trow[nt] = p; torig[nt] = p; ++nt; }
+        const int tmp = torig[c];
+        torig[c] = torig[ip_];
+        torig[ip_] = tmp;
+      }
+      s_nt = nt;
+    }
+    __syncthreads();
+    const int nt = s_nt;
+    for (int j0 = 0; j0 < n; j0 += FUSED_JC) {
+      if (j0 == k0) continue;                           // the panel's own columns
+      // interchanges of the chunk's columns; rows K go to R and become zero in A
+      for (int jj = warp; jj < FUSED_JC; jj += FUSED_THREADS / 32) {
+        const int j = j0 + jj;
+        if (j >= n) break;
+        float2* colj = Ab + (long long)j * n;
+        float2 v0 = zero, v1 = zero;
+        if (lane < nt) v0 = colj[torig[lane]];
+        if (lane + 32 < nt) v1 = colj[torig[lane + 32]];
+        __syncwarp();
+        if (lane < nt) {
+          const int r = trow[lane];
+          if (r >= k0 && r < k0 + kb) { Rs[(r - k0) * FUSED_RS + jj] = v0; colj[r] = zero; }
+          else colj[r] = v0;
+        }
+        if (lane + 32 < nt) {
+          const int r = trow[lane + 32];
+          if (r >= k0 && r < k0 + kb) { Rs[(r - k0) * FUSED_RS + jj] = v1; colj[r] = zero; }
+          else colj[r] = v1;
+        }
+      }
+      __syncthreads();
+      // A(:, j) += P R(:, j) for the chunk's columns: rows rg + 64 q (+ 256 per pass),
+      // columns j0 + 8 cg + c
+      for (int i0 = 0; i0 < n; i0 += 256) {
+        float2 acc[4][8];
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+#pragma unroll
+          for (int c = 0; c < 8; ++c) acc[q][c] = zero;
+        for (int k = 0; k < kb; ++k) {
+          float2 pv[4], rv[8];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const int i = i0 + rg + 64 * q;
+            pv[q] = i < n ? Ps[k * n + i] : zero;
+          }
+#pragma unroll
+          for (int c = 0; c < 8; ++c) rv[c] = Rs[k * FUSED_RS + 8 * cg + c];
+#pragma unroll
+          for (int q = 0; q < 4; ++q)
+#pragma unroll
+            for (int c = 0; c < 8; ++c) cfma(acc[q][c], pv[q], rv[c]);
+        }
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+          const int j = j0 + 8 * cg + c;
+          if (j >= n) break;
+          float2* colj = Ab + (long long)j * n;
+          float2 cin[4];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const int i = i0 + rg + 64 * q;
+            cin[q] = i < n ? colj[i] : zero;
+          }
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const int i = i0 + rg + 64 * q;
+            if (i < n) colj[i] = cadd(acc[q][c], cin[q]);
+          }
+        }
+      }
+      __syncthreads();   // the chunk's A and R are done before the next chunk's interchanges
+    }
+  }
+}
+
 }  // namespace
+
+size_t gj_fused_smem(int n) { return sizeof(float2) * ((size_t)32 * n + 32 * FUSED_RS); }
 
 int panel_width(int n, int elem_bytes) {
   // the panel (n x nb complex) must fit the 227 KB opt-in shared memory of a CTA.  The
@@ -315,6 +456,33 @@ void inv_work_free(InvWork& w) {
 
 namespace {
 
+
+int sm_count_cached() {
+  static int n = 0;
+  if (n == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 148;
+  }
+  return n;
+}
+
+// FP32 inverse as one fused launch per batch (plus the column interchanges)
+int gj_invert_fused_f32(float2* A, long long sA, int n, int batch, InvWork& w, cudaStream_t st) {
+  const size_t smem = gj_fused_smem(n);
+  NEGF_CUDA_TRY(cudaFuncSetAttribute(gj_fused_f32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  NEGF_CUDA_TRY(cudaMemsetAsync(w.info, 0, sizeof(int) * batch, st));
+  cudaEvent_t ev;
+  timed_begin(st, TK_F32, 8.0 * (double)n * n * n * batch, &ev);
+  gj_fused_f32_kernel<<<batch, FUSED_THREADS, smem, st>>>(A, sA, n, w.ipiv, w.info);
+  NEGF_CUDA_TRY(cudaGetLastError());
+  timed_end(st, TK_F32, ev);
+  dim3 g3((n + 127) / 128, batch);
+  gj_colswap_kernel<float2><<<g3, 128, 0, st>>>(A, sA, n, w.ipiv);
+  NEGF_CUDA_TRY(cudaGetLastError());
+  count_launch(2);
+  return NEGF_OK;
+}
 
 template <typename T>
 int gj_invert(T* A, long long sA, int n, int batch, InvWork& w, cudaStream_t st) {
@@ -365,7 +533,15 @@ int zinv_f64(double2* A, long long sA, int n, int batch, InvWork& w, cudaStream_
   return gj_invert<double2>(A, sA, n, batch, w, st);
 }
 
-int cinv_f32(float2* A, long long sA, int n, int batch, InvWork& w, cudaStream_t st) {
+bool cinv_f32_fused_ok(int n, int batch) { return n <= FUSED_MAX_N && batch >= sm_count_cached(); }
+
+int cinv_f32(float2* A, long long sA, int n, int batch, InvWork& w, cudaStream_t st, int form) {
+  if (form == 1) {
+    if (!cinv_f32_fused_ok(n, batch)) return NEGF_EINVAL;
+    if (batch <= 0) return NEGF_OK;
+    if (n > w.n_cap || batch > w.batch_cap) return NEGF_EINVAL;
+    return gj_invert_fused_f32(A, sA, n, batch, w, st);
+  }
   return gj_invert<float2>(A, sA, n, batch, w, st);
 }
 

@@ -159,8 +159,11 @@ int panel_width(int n, int elem_bytes = 16);
 // A: batch matrices of n x n, column-major, consecutive at stride sA.  On return A holds
 // the inverses; w.info[b] (device) holds the LAPACK-style INFO of each matrix.
 int zinv_f64(double2* A, long long sA, int n, int batch, InvWork& w, cudaStream_t st);
-// FP32 twin (the first guess of the mixed-form inverse)
-int cinv_f32(float2* A, long long sA, int n, int batch, InvWork& w, cudaStream_t st);
+// FP32 twin (the first guess of the mixed-form inverse).  form 0: panel / interchange /
+// update launches per 32-column panel; form 1: one fused launch with a CTA per matrix (needs
+// cinv_f32_fused_ok).  Both give bitwise the same result.
+int cinv_f32(float2* A, long long sA, int n, int batch, InvWork& w, cudaStream_t st, int form = 0);
+bool cinv_f32_fused_ok(int n, int batch);
 
 // ----------------------------------------------------------------------------------
 // per-item description of a batch (uploaded once per batch)

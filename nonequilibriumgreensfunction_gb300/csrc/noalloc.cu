@@ -35,9 +35,10 @@ namespace {
 constexpr int kMaxDim = NEGF_NOALLOC_MAX_DIM;
 constexpr int kMaxSlices = NEGF_NOALLOC_MAX_SLICES;
 constexpr size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
-// layout: A slices | B slices | row exponents | column exponents | error flag
-constexpr size_t kABytes = align256(sizeof(__nv_bfloat16) * (size_t)kMaxSlices * kMaxDim * 2 * kMaxDim);
-constexpr size_t kBBytes = align256(sizeof(__nv_bfloat16) * (size_t)kMaxSlices * 2 * kMaxDim * 2 * kMaxDim);
+// layout: A slices (2m rows of 2k) | B slices (n rows of 2k) | row exponents | column
+// exponents | error flag
+constexpr size_t kABytes = align256(sizeof(__nv_bfloat16) * (size_t)kMaxSlices * 2 * kMaxDim * 2 * kMaxDim);
+constexpr size_t kBBytes = align256(sizeof(__nv_bfloat16) * (size_t)kMaxSlices * kMaxDim * 2 * kMaxDim);
 constexpr size_t kEBytes = align256(sizeof(int) * (size_t)kMaxDim);
 constexpr size_t kScratchBytes = kABytes + kBBytes + 2 * kEBytes + 256;
 static_assert(kScratchBytes <= NEGF_NOALLOC_SCRATCH_BYTES, "scratch layout exceeds the declared size");

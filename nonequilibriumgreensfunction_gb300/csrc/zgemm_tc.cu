@@ -6,9 +6,13 @@
 // largest |re|,|im|) and every column j of B by 2^-f_j, so all scaled entries lie in
 // (-1, 1).  An entry a is then cut into S integer slices of 7 bits,
 //     a = 2^-6 (s_0 + 2^-7 (s_1 + 2^-7 (s_2 + ...))),   s_p in [-64, 64],
-// each of which is exact in BF16.  With the complex product written as one real product
-//     [Cr | Ci] = [Ar  Ai] [[Br, Bi], [-Bi, Br]]      (K' = 2K, N' = 2N),
-// the slice products S_p T_q are integer matrices with |entries| <= K' * 2^12.  The MMAs
+// each of which is exact in BF16.  The complex product is one real product of K' = 2K with
+// the complex rows of A expanded into pairs of real rows,
+//     row 2i:   [Ar(i,:)  -Ai(i,:)] . [Br(:,j); Bi(:,j)] = Cr(i,j)
+//     row 2i+1: [Ai(i,:)   Ar(i,:)] . [Br(:,j); Bi(:,j)] = Ci(i,j),
+// so the MMA's M side covers the 2M real rows (M = 400: 800 rows in 7 tiles of 128, against
+// 4 tiles of 128 for 400 rows, 22% of them padding) and its N side the N complex columns.
+// The slice products S_p T_q are integer matrices with |entries| <= K' * 2^12.  The MMAs
 // of one anti-diagonal d = p + q (at most S pairs) accumulate into one FP32 TMEM
 // accumulator; for d < 5 and K' <= 800 every partial sum stays below (d+1) 800 2^12 < 2^24,
 // so those accumulators are EXACT (products of 7-bit integers and their sums are
@@ -27,13 +31,17 @@
 //               (NT x 32) into a ring of shared-memory stages (SWIZZLE_64B, K-major).
 //   warp 1      TMEM allocation and the single-thread tcgen05.mma issue loop; commits
 //               release the stage and, at the end, signal the epilogue.
-//   warps 2-5   epilogue: tcgen05.ld of the S accumulators, FP64 recombination, store.
+//   warps 2-5   epilogue: tcgen05.ld of the S accumulators, FP64 recombination; lanes
+//               2i and 2i+1 hold the real and imaginary parts of C row i and exchange
+//               them with one shuffle, the even lane storing the even columns and the
+//               odd lane the odd ones.
 // Every mbarrier wait is bounded; on expiry the kernel records an error code and returns
 // after draining its own TMA copies and freeing its TMEM.
 //
 // Replaces, in the mixed form, the ZGEMM calls of Source/Recursive_Greens.F90 and the
 // G Gamma products of Source/Calculate_Gnp.F90.
 #include <algorithm>
+#include <cstdlib>
 #include <mutex>
 #include <map>
 #include <cuda.h>
@@ -305,7 +313,9 @@ __global__ void row_exp_kernel(const double2* A, int lda, long long sA, int m, i
   }
 }
 
-// A slices, K-major: out[((b*S + p)*m + i)*kp + k] with kp = 2*half: [Ar(i, :), Ai(i, :)],
+// A slices, K-major, two real rows per complex row i (kp = 2*half):
+//     out[((b*S + p)*2m + 2i)*kp + k]   = [Ar(i, :), -Ai(i, :)]
+//     out[((b*S + p)*2m + 2i+1)*kp + k] = [Ai(i, :),  Ar(i, :)],
 // zero in the padding k in [K, half).  A tile of 32 rows x 64 k is staged through shared
 // memory (coalesced column-major reads); each thread then slices one row x 8 consecutive
 // k and writes 16-byte vectors.
@@ -328,7 +338,7 @@ __global__ void __launch_bounds__(256) slice_a_kernel(const double2* A, int lda,
   const int i = i0 + row, kb = k0 + 8 * kg;
   if (i >= m || kb >= half) return;
   const int e = ea[(long long)b * m + i];
-  __align__(16) __nv_bfloat16 sr[S][8], si[S][8];
+  __align__(16) __nv_bfloat16 sr[S][8], si[S][8], ni[S][8];
 #pragma unroll
   for (int q = 0; q < 8; ++q) {
     const double2 v = tile[8 * kg + q][row];
@@ -336,20 +346,23 @@ __global__ void __launch_bounds__(256) slice_a_kernel(const double2* A, int lda,
     slice_value<S>(v.x, e, a);
     slice_value<S>(v.y, e, c);
 #pragma unroll
-    for (int p = 0; p < S; ++p) { sr[p][q] = a[p]; si[p][q] = c[p]; }
+    for (int p = 0; p < S; ++p) { sr[p][q] = a[p]; si[p][q] = c[p]; ni[p][q] = __hneg(c[p]); }
   }
 #pragma unroll
   for (int p = 0; p < S; ++p) {
-    __nv_bfloat16* rowp = out + ((long long)(b * S + p) * m + i) * kp;
-    *reinterpret_cast<uint4*>(rowp + kb) = *reinterpret_cast<const uint4*>(sr[p]);
-    *reinterpret_cast<uint4*>(rowp + half + kb) = *reinterpret_cast<const uint4*>(si[p]);
+    __nv_bfloat16* re_row = out + ((long long)(b * S + p) * 2 * m + 2 * i) * kp;
+    __nv_bfloat16* im_row = re_row + kp;
+    *reinterpret_cast<uint4*>(re_row + kb) = *reinterpret_cast<const uint4*>(sr[p]);
+    *reinterpret_cast<uint4*>(re_row + half + kb) = *reinterpret_cast<const uint4*>(ni[p]);
+    *reinterpret_cast<uint4*>(im_row + kb) = *reinterpret_cast<const uint4*>(si[p]);
+    *reinterpret_cast<uint4*>(im_row + half + kb) = *reinterpret_cast<const uint4*>(sr[p]);
   }
 }
 
-// B slices: one warp per column j of B (K x N complex, column-major).  Rows of the
-// K-major operand (output columns): 2j -> [Br(:,j); -Bi(:,j)], 2j+1 -> [Bi(:,j); Br(:,j)],
-// zero in the padding.  Chunks of 256 k are read coalesced into shared memory; each lane
-// then slices 8 consecutive k and writes 16-byte vectors.
+// B slices: one warp per column j of B (K x N complex, column-major).  Row j of the
+// K-major operand is [Br(:,j); Bi(:,j)], zero in the padding: out[((b*S + p)*n + j)*kp + k].
+// Chunks of 256 k are read coalesced into shared memory; each lane then slices 8
+// consecutive k and writes 16-byte vectors.
 template <int S>
 __global__ void __launch_bounds__(256) slice_b_kernel(const double2* B, int ldb, long long sB, int k, int n, int* fb,
                                                       __nv_bfloat16* out, int half) {
@@ -366,7 +379,6 @@ __global__ void __launch_bounds__(256) slice_b_kernel(const double2* B, int ldb,
   for (int off = 16; off > 0; off >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, off));
   const int e = scale_exponent(mx);
   if (lane == 0) fb[(long long)b * n + j] = e;
-  const long long n2 = 2LL * n;
   double2* ch = chunk[warp];
   for (int c0 = 0; c0 < half; c0 += 256) {
 #pragma unroll
@@ -377,7 +389,7 @@ __global__ void __launch_bounds__(256) slice_b_kernel(const double2* B, int ldb,
     __syncwarp();
     const int kb = c0 + 8 * lane;
     if (kb < half) {
-      __align__(16) __nv_bfloat16 rr[S][8], ri[S][8], nr[S][8];
+      __align__(16) __nv_bfloat16 rr[S][8], ri[S][8];
 #pragma unroll
       for (int q = 0; q < 8; ++q) {
         const double2 v = ch[8 * lane + q];
@@ -385,16 +397,13 @@ __global__ void __launch_bounds__(256) slice_b_kernel(const double2* B, int ldb,
         slice_value<S>(v.x, e, a);
         slice_value<S>(v.y, e, c);
 #pragma unroll
-        for (int p = 0; p < S; ++p) { rr[p][q] = a[p]; ri[p][q] = c[p]; nr[p][q] = __hneg(c[p]); }
+        for (int p = 0; p < S; ++p) { rr[p][q] = a[p]; ri[p][q] = c[p]; }
       }
 #pragma unroll
       for (int p = 0; p < S; ++p) {
-        __nv_bfloat16* re_row = out + ((long long)(b * S + p) * n2 + 2LL * j) * kp;
-        __nv_bfloat16* im_row = re_row + kp;
-        *reinterpret_cast<uint4*>(re_row + kb) = *reinterpret_cast<const uint4*>(rr[p]);
-        *reinterpret_cast<uint4*>(re_row + half + kb) = *reinterpret_cast<const uint4*>(nr[p]);
-        *reinterpret_cast<uint4*>(im_row + kb) = *reinterpret_cast<const uint4*>(ri[p]);
-        *reinterpret_cast<uint4*>(im_row + half + kb) = *reinterpret_cast<const uint4*>(rr[p]);
+        __nv_bfloat16* rowp = out + ((long long)(b * S + p) * n + j) * kp;
+        *reinterpret_cast<uint4*>(rowp + kb) = *reinterpret_cast<const uint4*>(rr[p]);
+        *reinterpret_cast<uint4*>(rowp + half + kb) = *reinterpret_cast<const uint4*>(ri[p]);
       }
     }
     __syncwarp();
@@ -418,7 +427,7 @@ struct TcCfg {
 #define TC_MAX_STAGES 4
 #endif
   static constexpr int STAGES = BUDGET / STAGE > TC_MAX_STAGES ? TC_MAX_STAGES : BUDGET / STAGE;
-  static constexpr int SMEM = STAGES * STAGE + 1024 + 256 + 4 * (NT / 2);   // + alignment, barriers, exponents
+  static constexpr int SMEM = STAGES * STAGE + 1024 + 256 + 4 * NT;   // + alignment, barriers, exponents
   static constexpr int TMEM_COLS_USED = KS * S * NT;
   static constexpr int TMEM_COLS = TMEM_COLS_USED <= 32 ? 32 : TMEM_COLS_USED <= 64 ? 64
                                  : TMEM_COLS_USED <= 128 ? 128 : TMEM_COLS_USED <= 256 ? 256 : 512;
@@ -431,8 +440,8 @@ struct TcCfg {
 struct TcArgs {
   int m, n, kp;            // rows of C, complex columns of C, K' = 2K
   int batch;
-  long long rowsA;         // rows of one (item, slice) plane in the A map (= m)
-  long long rowsB;         // rows of one (item, slice) plane in the B map (= 2n)
+  long long rowsA;         // rows of one (item, slice) plane in the A map (= 2m)
+  long long rowsB;         // rows of one (item, slice) plane in the B map (= n)
   int planesA, planesB;    // slice planes stored per item (>= S: the leading S are used)
   const int* ea;           // [batch][m]
   const int* fb;           // [batch][n]
@@ -442,6 +451,44 @@ struct TcArgs {
   int beta_kind;           // 0: beta == 0, 1: beta == 1, 2: general
   int* err;
 };
+
+// Stores one chunk of CW tile columns.  Each lane holds, for its real output row, the exact
+// integer sums of the real part (even row, part 0) or the imaginary part (odd row, part 1)
+// of C(row / 2, col0 + c); it converts them to doubles, and lanes 2i and 2i+1 swap what
+// the other one stores -- the even lane stores the even columns, the odd lane the odd
+// ones -- with one shuffle per pair of columns.  Every lane of the warp must call it (the
+// shuffles); `valid` masks the stores.
+template <int S, int DH, int CW>
+__device__ __forceinline__ void store_chunk(const long long (&hi)[CW], const long long (&lo)[CW], const int* cexp,
+                                            int e_row, int part, int row, int col0, bool valid, const TcArgs& a,
+                                            double2* Cb) {
+  double v[CW];
+#pragma unroll
+  for (int c = 0; c < CW; ++c) v[c] = recombine<S, DH>(hi[c], lo[c], e_row + cexp[c] - 12 - 7 * (S - 1));
+  double recv[CW / 2];   // the partner's half of the columns this lane stores
+#pragma unroll
+  for (int h = 0; h < CW / 2; ++h) recv[h] = __shfl_xor_sync(0xffffffffu, part ? v[2 * h] : v[2 * h + 1], 1);
+  if (!valid) return;
+  double2 cin[CW / 2];
+  if (a.beta_kind != 0) {                // issue all loads of the chunk before any store
+#pragma unroll
+    for (int h = 0; h < CW / 2; ++h) {
+      const int col = col0 + 2 * h + part;
+      cin[h] = col < a.n ? Cb[(long long)col * a.ldc + row] : make_double2(0.0, 0.0);
+    }
+  }
+#pragma unroll
+  for (int h = 0; h < CW / 2; ++h) {
+    const int col = col0 + 2 * h + part;
+    if (col >= a.n) continue;
+    const double mine = part ? v[2 * h + 1] : v[2 * h];
+    double2 out = part ? make_double2(recv[h], mine) : make_double2(mine, recv[h]);
+    if (!a.alpha_one) out = cmul(a.alpha, out);
+    if (a.beta_kind == 1) out = cadd(out, cin[h]);
+    else if (a.beta_kind == 2) out = cadd(out, cmul(a.beta, cin[h]));
+    Cb[(long long)col * a.ldc + row] = out;
+  }
+}
 
 template <int S, int NT, int MINB, int KS>
 __global__ void __launch_bounds__(TC_THREADS, MINB)
@@ -454,7 +501,7 @@ __global__ void __launch_bounds__(TC_THREADS, MINB)
   uint64_t* done = empty + Cfg::STAGES;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
   int* abort_flag = reinterpret_cast<int*>(tmem_slot + 1);
-  int* col_exp = abort_flag + 1;   // NT/2 column exponents of this tile
+  int* col_exp = abort_flag + 1;   // NT column exponents of this tile
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int tm = blockIdx.x, tn = blockIdx.y, b = blockIdx.z;
@@ -551,18 +598,20 @@ __global__ void __launch_bounds__(TC_THREADS, MINB)
       tc_commit(done);
     }
   } else {
-    // ---- epilogue: warps 2..5 -> TMEM lane quarter (warp % 4).  While the MMAs run,
-    // stage this tile's column exponents in shared memory.
+    // ---- epilogue: warps 2..5 -> TMEM lane quarter (warp % 4); lane l of the tile is real
+    // output row tm*128 + l.  While the MMAs run, stage the tile's column exponents in
+    // shared memory.
     const int quarter = warp & 3;
-    for (int c = threadIdx.x - 64; c < NT / 2; c += 128) {
-      const int col = tn * (NT / 2) + c;
+    for (int c = threadIdx.x - 64; c < NT; c += 128) {
+      const int col = tn * NT + c;
       col_exp[c] = col < a.n ? a.fb[(long long)b * a.n + col] : 0;
     }
     asm volatile("bar.sync 1, 128;" ::: "memory");   // the four epilogue warps only
     const bool ok = mbar_wait(done, 0);
     if (!ok && a.err) atomicCAS(a.err, 0, 3);
     tc_fence_after();
-    const int row = tm * TILE_M + quarter * 32 + lane;
+    const int rr = tm * TILE_M + quarter * 32 + lane;
+    const int row = rr >> 1, part = rr & 1;          // C row, real (0) or imaginary (1) part
     const bool aborted = !ok || *((volatile int*)abort_flag);
     const int e_row = (row < a.m) ? a.ea[(long long)b * a.m + row] : 0;
     double2* Cb = a.C + (long long)b * a.sC;
@@ -602,27 +651,7 @@ __global__ void __launch_bounds__(TC_THREADS, MINB)
           }
         }
       }
-      if (row >= a.m || aborted) continue;
-      const int col0 = (tn * NT + c0) / 2;   // first complex output column of this chunk
-      double2 cin[CW / 2];
-      if (a.beta_kind != 0) {                // issue all loads of the chunk before any store
-#pragma unroll
-        for (int jj = 0; jj < CW / 2; ++jj)
-          cin[jj] = (col0 + jj < a.n) ? Cb[(long long)(col0 + jj) * a.ldc + row] : make_double2(0.0, 0.0);
-      }
-#pragma unroll
-      for (int jj = 0; jj < CW / 2; ++jj) {
-        const int col = col0 + jj;
-        if (col >= a.n) continue;
-        const int sc = e_row + col_exp[c0 / 2 + jj] - 12 - 7 * (S - 1);
-        const double re = recombine<S, DH>(hi[2 * jj], lo[2 * jj], sc);
-        const double im = recombine<S, DH>(hi[2 * jj + 1], lo[2 * jj + 1], sc);
-        double2 out = make_double2(re, im);
-        if (!a.alpha_one) out = cmul(a.alpha, out);
-        if (a.beta_kind == 1) out = cadd(out, cin[jj]);
-        else if (a.beta_kind == 2) out = cadd(out, cmul(a.beta, cin[jj]));
-        Cb[(long long)col * a.ldc + row] = out;
-      }
+      store_chunk<S, DH, CW>(hi, lo, col_exp + c0, e_row, part, row, tn * NT + c0, row < a.m && !aborted, a, Cb);
     }
   }
   tc_fence_before();
@@ -657,7 +686,7 @@ struct TcPCfg {
   static constexpr int BUDGET = 220 * 1024;
   static constexpr int STAGES = BUDGET / STAGE > 6 ? 6 : BUDGET / STAGE;
   static constexpr int ACC = S * NT;   // TMEM columns of one accumulator set
-  static constexpr int SMEM = STAGES * STAGE + 1024 + 256 + 4 * NT;   // + alignment, barriers, exponents
+  static constexpr int SMEM = STAGES * STAGE + 1024 + 256 + 8 * NT;   // + alignment, barriers, 2 x NT exponents
   static_assert(STAGES >= 2, "at least two stages");
   static_assert(2 * ACC <= 512, "two accumulator sets in TMEM");
   static_assert(SMEM <= 227 * 1024, "shared memory of one CTA");
@@ -697,7 +726,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   uint64_t* fin = tempty + 2;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(fin + 1);
   int* abort_flag = reinterpret_cast<int*>(tmem_slot + 1);
-  int* col_exp = abort_flag + 1;   // [2][NT/2] column exponents of the tiles in flight
+  int* col_exp = abort_flag + 1;   // [2][NT] column exponents of the tiles in flight
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nk = (a.kp + BK - 1) / BK;
@@ -814,9 +843,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       const int b = (int)(t / tiles_item);
       const int r = (int)(t % tiles_item);
       const int tm = r / tiles_n, tn = r % tiles_n;
-      int* cexp = col_exp + buf * (NT / 2);
-      for (int c = threadIdx.x - 64; c < NT / 2; c += 128) {
-        const int col = tn * (NT / 2) + c;
+      int* cexp = col_exp + buf * NT;
+      for (int c = threadIdx.x - 64; c < NT; c += 128) {
+        const int col = tn * NT + c;
         cexp[c] = col < a.n ? a.fb[(long long)b * a.n + col] : 0;
       }
       // the exponents are visible to all four warps, and all agree on stopping
@@ -828,7 +857,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         break;
       }
       tc_fence_after();
-      const int row = tm * TILE_M + quarter * 32 + lane;
+      const int rr = tm * TILE_M + quarter * 32 + lane;
+      const int row = rr >> 1, part = rr & 1;        // C row, real (0) or imaginary (1) part
       const int e_row = (row < a.m) ? a.ea[(long long)b * a.m + row] : 0;
       double2* Cb = a.C + (long long)b * a.sC;
       const uint32_t acc0 = tmem + (uint32_t)(buf * Cfg::ACC);
@@ -855,27 +885,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             else lo[i] += q * (1LL << (7 * (S - 1 - d)));
           }
         }
-        if (row >= a.m) continue;
-        const int col0 = (tn * NT + c0) / 2;
-        double2 cin[CW / 2];
-        if (a.beta_kind != 0) {
-#pragma unroll
-          for (int jj = 0; jj < CW / 2; ++jj)
-            cin[jj] = (col0 + jj < a.n) ? Cb[(long long)(col0 + jj) * a.ldc + row] : make_double2(0.0, 0.0);
-        }
-#pragma unroll
-        for (int jj = 0; jj < CW / 2; ++jj) {
-          const int col = col0 + jj;
-          if (col >= a.n) continue;
-          const int sc = e_row + cexp[c0 / 2 + jj] - 12 - 7 * (S - 1);
-          const double re = recombine<S, DH>(hi[2 * jj], lo[2 * jj], sc);
-          const double im = recombine<S, DH>(hi[2 * jj + 1], lo[2 * jj + 1], sc);
-          double2 out = make_double2(re, im);
-          if (!a.alpha_one) out = cmul(a.alpha, out);
-          if (a.beta_kind == 1) out = cadd(out, cin[jj]);
-          else if (a.beta_kind == 2) out = cadd(out, cmul(a.beta, cin[jj]));
-          Cb[(long long)col * a.ldc + row] = out;
-        }
+        store_chunk<S, DH, CW>(hi, lo, cexp + c0, e_row, part, row, tn * NT + c0, row < a.m, a, Cb);
       }
       tc_fence_before();
       mbar_arrive(&tempty[buf]);
@@ -917,28 +927,11 @@ int make_map(CUtensorMap* map, const void* base, int kp, long long rows, int box
   return r == CUDA_SUCCESS ? NEGF_OK : NEGF_ECUDA;
 }
 
-// Tile configuration <slices, N tile, CTAs per SM> of the slice counts below 6 (the others
-// use N = 64 and one CTA per SM: S x N TMEM columns must fit 512 / CTAs).  Compile-time
-// defaults; a build may override them to compare variants.
-#ifndef TC_PERSIST
-#define TC_PERSIST 0    // 1: every slice count through the persistent kernel
-#endif
-#ifndef TC_NT3
-#define TC_NT3 80
-#define TC_MINB3 2
-#endif
-#ifndef TC_NT4
-#define TC_NT4 64
-#define TC_MINB4 2
-#endif
-#ifndef TC_NT5
-#define TC_NT5 48
-#define TC_MINB5 2
-#endif
-#ifndef TC_NT7
-#define TC_NT7 64
-#define TC_MINB7 1
-#endif
+// Kernel variants, timed per shape by the autotuner below (results are bitwise the same
+// in every variant): 0 and 1 are per-tile kernels <N tile, CTAs per SM> with different N
+// tiles (the N tile sets how evenly the N columns divide, and with the slice count how
+// much TMEM a CTA needs: S x N columns <= 512 / CTAs per SM), 2 is the persistent kernel.
+constexpr int kVariants = 3;
 
 template <int S, int NT, int MINB, int KS = 1>
 int launch_mma(const SlicedOperand& A, const SlicedOperand& B, const TcArgs& args, cudaStream_t st) {
@@ -950,7 +943,7 @@ int launch_mma(const SlicedOperand& A, const SlicedOperand& B, const TcArgs& arg
   NEGF_TRY(make_map(&mb, B.data, args.kp, (long long)args.batch * args.planesB * args.rowsB, NT));
   NEGF_CUDA_TRY(
       cudaFuncSetAttribute(zgemm_tc_kernel<S, NT, MINB, KS>, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM));
-  dim3 grid((args.m + TILE_M - 1) / TILE_M, (unsigned)((2LL * args.n + NT - 1) / NT), args.batch);
+  dim3 grid((unsigned)((2LL * args.m + TILE_M - 1) / TILE_M), (unsigned)((args.n + NT - 1) / NT), args.batch);
   cudaEvent_t ev;
   const double cflops = 8.0 * args.m * (double)args.n * (args.kp / 2) * args.batch;
   add_tc_complex_flops(cflops);
@@ -979,8 +972,8 @@ int launch_persistent(const SlicedOperand& A, const SlicedOperand& B, const TcAr
   NEGF_TRY(make_map(&ma, A.data, args.kp, (long long)args.batch * args.planesA * args.rowsA, TILE_M));
   NEGF_TRY(make_map(&mb, B.data, args.kp, (long long)args.batch * args.planesB * args.rowsB, NT));
   NEGF_CUDA_TRY(cudaFuncSetAttribute(zgemm_tc_persistent<S, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM));
-  const int tiles_m = (args.m + TILE_M - 1) / TILE_M;
-  const int tiles_n = (int)((2LL * args.n + NT - 1) / NT);
+  const int tiles_m = (int)((2LL * args.m + TILE_M - 1) / TILE_M);
+  const int tiles_n = (int)((args.n + NT - 1) / NT);
   const long long ntiles = (long long)tiles_m * tiles_n * args.batch;
   const int grid = (int)std::min<long long>(ntiles, sm_count());
   cudaEvent_t ev;
@@ -1028,14 +1021,16 @@ bool tc_supported_slices(int s) { return s >= 3 && s <= 8; }
 size_t sliced_bytes(int rows, int k, int slices, int batch) {
   return sizeof(__nv_bfloat16) * (size_t)batch * slices * rows * 2 * (size_t)k;
 }
+size_t sliced_bytes_a(int m, int k, int slices, int batch) { return sliced_bytes(2 * m, k, slices, batch); }
+size_t sliced_bytes_b(int n, int k, int slices, int batch) { return sliced_bytes(n, k, slices, batch); }
 
 int padded_k(int k) { return (k + 7) & ~7; }   // 16-byte slice vectors and TMA rows
 
 int slice_a(const double2* A, int lda, long long sA, int m, int k, int batch, int slices, SlicedOperand& out,
             cudaStream_t st) {
-  if (sliced_bytes(m, padded_k(k), slices, batch) > out.data_bytes || (size_t)m * batch > out.exps_count)
+  if (sliced_bytes_a(m, padded_k(k), slices, batch) > out.data_bytes || (size_t)m * batch > out.exps_count)
     return NEGF_EINVAL;
-  out.rows = m; out.k = padded_k(k); out.slices = slices; out.batch = batch;
+  out.rows = 2 * m; out.k = padded_k(k); out.slices = slices; out.batch = batch;
   switch (slices) {
     case 2: return slice_a_t<2>(A, lda, sA, m, k, batch, out, st);
     case 3: return slice_a_t<3>(A, lda, sA, m, k, batch, out, st);
@@ -1050,9 +1045,9 @@ int slice_a(const double2* A, int lda, long long sA, int m, int k, int batch, in
 
 int slice_b(const double2* B, int ldb, long long sB, int k, int n, int batch, int slices, SlicedOperand& out,
             cudaStream_t st) {
-  if (sliced_bytes(2 * n, padded_k(k), slices, batch) > out.data_bytes || (size_t)n * batch > out.exps_count)
+  if (sliced_bytes_b(n, padded_k(k), slices, batch) > out.data_bytes || (size_t)n * batch > out.exps_count)
     return NEGF_EINVAL;
-  out.rows = 2 * n; out.k = padded_k(k); out.slices = slices; out.batch = batch;
+  out.rows = n; out.k = padded_k(k); out.slices = slices; out.batch = batch;
   switch (slices) {
     case 2: return slice_b_t<2>(B, ldb, sB, k, n, batch, out, st);
     case 3: return slice_b_t<3>(B, ldb, sB, k, n, batch, out, st);
@@ -1065,18 +1060,20 @@ int slice_b(const double2* B, int ldb, long long sB, int k, int n, int batch, in
   return NEGF_EINVAL;
 }
 
-int launch_persistent_s(int S, const SlicedOperand& A, const SlicedOperand& B, const TcArgs& args, cudaStream_t st);
-int launch_per_tile_s(int S, const SlicedOperand& A, const SlicedOperand& B, const TcArgs& args, cudaStream_t st);
+int launch_variant(int v, int S, const SlicedOperand& A, const SlicedOperand& B, const TcArgs& args,
+                   cudaStream_t st);
 
 namespace {
 
 // Autotuner of the kernel variant per shape (slices, m, n, K', batch rounded up to a power
-// of two): the per-tile kernel (several CTAs per SM for S <= 5) or the persistent kernel.
-// Both issue each tile's MMAs in the same order into the same accumulators and run the same
+// of two): the two per-tile kernels (N tiles of different widths; two CTAs per SM where
+// TMEM and shared memory allow) and the persistent kernel.  All issue each output
+// element's MMAs in the same K order into the same exact accumulators and run the same
 // epilogue, so their results are bitwise identical and the choice never changes a number.
-// The first call of a shape with beta = 0 runs both variants (each overwrites C with the
-// same values), times them with events on the caller's stream and keeps the faster; calls
-// with beta != 0 before that use the per-tile kernel.
+// The first call of a shape with beta = 0 runs every variant three times (each run
+// overwrites C with the same values), times the last two runs with events on the caller's
+// stream and keeps the fastest; calls with beta != 0 before that use variant 0.  Beyond
+// K' = 800 only the per-tile kernel with two accumulator sets along K exists.
 struct TuneKey {
   int S, m, n, kp, batch;
   bool operator<(const TuneKey& o) const {
@@ -1088,14 +1085,14 @@ struct TuneKey {
   }
 };
 std::mutex g_tune_mu;
-std::map<TuneKey, int> g_tune;   // 0 per-tile, 1 persistent
+std::map<TuneKey, int> g_tune;   // the chosen variant
 
 float time_variant(int v, int S, const SlicedOperand& A, const SlicedOperand& B, const TcArgs& args, cudaStream_t st) {
   cudaEvent_t e0, e1;
   if (cudaEventCreate(&e0) != cudaSuccess) return -1.0f;
   if (cudaEventCreate(&e1) != cudaSuccess) { cudaEventDestroy(e0); return -1.0f; }
   cudaEventRecord(e0, st);
-  const int rc = v ? launch_persistent_s(S, A, B, args, st) : launch_per_tile_s(S, A, B, args, st);
+  const int rc = launch_variant(v, S, A, B, args, st);
   cudaEventRecord(e1, st);
   float ms = -1.0f;
   if (rc == NEGF_OK && cudaEventSynchronize(e1) == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
@@ -1116,17 +1113,19 @@ int choose_variant(int S, const SlicedOperand& A, const SlicedOperand& B, const 
     auto it = g_tune.find(key);
     if (it != g_tune.end()) return it->second;
   }
-  // beyond K' = 800 only the per-tile kernel splits its accumulators along K
   if (args.beta_kind != 0 || args.kp > 800) return 0;
   // two timings each, after a first run of each that pays one-time costs
-  float best[2] = {1e30f, 1e30f};
+  float best[kVariants];
+  for (int v = 0; v < kVariants; ++v) best[v] = 1e30f;
   for (int rep = 0; rep < 3; ++rep)
-    for (int v = 0; v < 2; ++v) {
+    for (int v = 0; v < kVariants; ++v) {
       const float ms = time_variant(v, S, A, B, args, st);
       if (ms < 0.0f) return -3;
       if (rep > 0 && ms < best[v]) best[v] = ms;
     }
-  const int choice = best[1] < best[0] ? 1 : 0;
+  int choice = 0;
+  for (int v = 1; v < kVariants; ++v)
+    if (best[v] < best[choice]) choice = v;
   std::lock_guard<std::mutex> g(g_tune_mu);
   g_tune[key] = choice;
   return -2;
@@ -1143,7 +1142,8 @@ int zgemm_tc(const SlicedOperand& A, const SlicedOperand& B, double2 alpha, doub
   // has at most two sets along K
   if (2 * A.k > 1600) return NEGF_EINVAL;
   TcArgs args{};
-  args.m = A.rows; args.n = B.rows / 2; args.kp = 2 * A.k; args.batch = A.batch;
+  if (A.rows % 2 != 0) return NEGF_EINVAL;
+  args.m = A.rows / 2; args.n = B.rows; args.kp = 2 * A.k; args.batch = A.batch;
   args.rowsA = A.rows; args.rowsB = B.rows;
   args.planesA = A.slices; args.planesB = B.slices;
   args.ea = A.exps; args.fb = B.exps;
@@ -1151,39 +1151,20 @@ int zgemm_tc(const SlicedOperand& A, const SlicedOperand& B, double2 alpha, doub
   args.alpha = alpha; args.beta = beta; args.err = err;
   args.alpha_one = (alpha.x == 1.0 && alpha.y == 0.0) ? 1 : 0;
   args.beta_kind = (beta.x == 0.0 && beta.y == 0.0) ? 0 : (beta.x == 1.0 && beta.y == 0.0) ? 1 : 2;
-#if TC_PERSIST
-  if (args.kp <= 800) switch (S) {
-    case 2: return launch_persistent<2, 128>(A, B, args, st);
-    case 3: return launch_persistent<3, 80>(A, B, args, st);
-    case 4: return launch_persistent<4, 64>(A, B, args, st);
-    case 5: return launch_persistent<5, 48>(A, B, args, st);
-    case 6: return launch_persistent<6, 32>(A, B, args, st);
-    case 7: return launch_persistent<7, 32>(A, B, args, st);
-    case 8: return launch_persistent<8, 32>(A, B, args, st);
+  // NEGF_TC_VARIANT = 0, 1 or 2 runs that kernel variant instead of the autotuner's choice
+  // (to compare or profile variants; all give bitwise the same result)
+  if (const char* ev = std::getenv("NEGF_TC_VARIANT")) {
+    const int v = std::atoi(ev);
+    if (ev[0] >= '0' && ev[0] <= '9' && v < kVariants) return launch_variant(v, S, A, B, args, st);
   }
-  if (args.kp <= 800) return NEGF_EINVAL;
-#endif
   const int variant = choose_variant(S, A, B, args, st);
   if (variant == -2) return NEGF_OK;        // the tuning runs computed C
   if (variant == -3) return NEGF_ECUDA;
-  if (variant == 1) return launch_persistent_s(S, A, B, args, st);
-  return launch_per_tile_s(S, A, B, args, st);
+  return launch_variant(variant, S, A, B, args, st);
 }
 
-int launch_persistent_s(int S, const SlicedOperand& A, const SlicedOperand& B, const TcArgs& args, cudaStream_t st) {
-  switch (S) {
-    case 2: return launch_persistent<2, 128>(A, B, args, st);
-    case 3: return launch_persistent<3, 80>(A, B, args, st);
-    case 4: return launch_persistent<4, 64>(A, B, args, st);
-    case 5: return launch_persistent<5, 48>(A, B, args, st);
-    case 6: return launch_persistent<6, 32>(A, B, args, st);
-    case 7: return launch_persistent<7, 32>(A, B, args, st);
-    case 8: return launch_persistent<8, 32>(A, B, args, st);
-  }
-  return NEGF_EINVAL;
-}
-
-int launch_per_tile_s(int S, const SlicedOperand& A, const SlicedOperand& B, const TcArgs& args, cudaStream_t st) {
+int launch_variant(int v, int S, const SlicedOperand& A, const SlicedOperand& B, const TcArgs& args,
+                   cudaStream_t st) {
   if (args.kp > 800) {
     // two accumulator sets along K, one CTA per SM: 2 S NT <= 512 TMEM columns
     switch (S) {
@@ -1196,14 +1177,26 @@ int launch_per_tile_s(int S, const SlicedOperand& A, const SlicedOperand& B, con
     }
     return NEGF_EINVAL;
   }
+  if (v == 2) {
+    switch (S) {
+      case 2: return launch_persistent<2, 128>(A, B, args, st);
+      case 3: return launch_persistent<3, 80>(A, B, args, st);
+      case 4: return launch_persistent<4, 64>(A, B, args, st);
+      case 5: return launch_persistent<5, 48>(A, B, args, st);
+      case 6: return launch_persistent<6, 32>(A, B, args, st);
+      case 7: return launch_persistent<7, 32>(A, B, args, st);
+      case 8: return launch_persistent<8, 32>(A, B, args, st);
+    }
+    return NEGF_EINVAL;
+  }
   switch (S) {
-    case 2: return launch_mma<2, 128, 2>(A, B, args, st);   // internal: small corrections
-    case 3: return launch_mma<3, TC_NT3, TC_MINB3>(A, B, args, st);
-    case 4: return launch_mma<4, TC_NT4, TC_MINB4>(A, B, args, st);
-    case 5: return launch_mma<5, TC_NT5, TC_MINB5>(A, B, args, st);
-    case 6: return launch_mma<6, 64, 1>(A, B, args, st);
-    case 7: return launch_mma<7, TC_NT7, TC_MINB7>(A, B, args, st);
-    case 8: return launch_mma<8, 64, 1>(A, B, args, st);
+    case 2: return v ? launch_mma<2, 64, 2>(A, B, args, st) : launch_mma<2, 128, 2>(A, B, args, st);
+    case 3: return v ? launch_mma<3, 48, 2>(A, B, args, st) : launch_mma<3, 80, 2>(A, B, args, st);
+    case 4: return v ? launch_mma<4, 80, 1>(A, B, args, st) : launch_mma<4, 64, 2>(A, B, args, st);
+    case 5: return v ? launch_mma<5, 80, 1>(A, B, args, st) : launch_mma<5, 48, 2>(A, B, args, st);
+    case 6: return v ? launch_mma<6, 80, 1>(A, B, args, st) : launch_mma<6, 64, 1>(A, B, args, st);
+    case 7: return v ? launch_mma<7, 48, 1>(A, B, args, st) : launch_mma<7, 64, 1>(A, B, args, st);
+    case 8: return v ? launch_mma<8, 48, 1>(A, B, args, st) : launch_mma<8, 64, 1>(A, B, args, st);
   }
   return NEGF_EINVAL;
 }

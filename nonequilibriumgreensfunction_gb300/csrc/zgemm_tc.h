@@ -8,8 +8,10 @@
 namespace negf {
 
 // An operand cut into integer BF16 slices, K-major: for slice p of item b, `rows` rows of
-// 2K BF16 values at data + ((b*slices + p)*rows + r)*2K, with one power-of-two exponent
-// per row in exps[b*rows_logical + r] (rows_logical = rows for A, rows/2 for B).
+// 2K BF16 values at data + ((b*slices + p)*rows + r)*2K.  A (M x K complex) has rows = 2M:
+// row 2i = [Ar(i,:), -Ai(i,:)], row 2i+1 = [Ai(i,:), Ar(i,:)]; B (K x N complex) has
+// rows = N: row j = [Br(:,j), Bi(:,j)].  One power-of-two exponent per complex row of A
+// (exps[b*M + i]) or column of B (exps[b*N + j]).
 struct SlicedOperand {
   __nv_bfloat16* data = nullptr;
   int* exps = nullptr;
@@ -21,9 +23,11 @@ struct SlicedOperand {
 bool tc_supported_slices(int s);
 // K padded to a multiple of 4 (TMA rows must be a multiple of 16 bytes)
 int padded_k(int k);
-// bytes of the slice planes for `rows` x K complex operands (A: rows = M; B: rows = 2N);
-// pass padded_k(K)
+// bytes of the slice planes of `rows` K-major rows of 2K values; pass padded_k(K)
 size_t sliced_bytes(int rows, int k, int slices, int batch);
+// the same for an M x K complex A operand (2M rows) and a K x N complex B operand (N rows)
+size_t sliced_bytes_a(int m, int k, int slices, int batch);
+size_t sliced_bytes_b(int n, int k, int slices, int batch);
 // A operand: M x K complex, column-major (lda, batch stride sA)
 int slice_a(const double2* A, int lda, long long sA, int m, int k, int batch, int slices, SlicedOperand& out,
             cudaStream_t st);

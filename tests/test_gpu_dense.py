@@ -79,14 +79,47 @@ def test_inverse_matches_lapack(need_gpu):
     assert info == 4          # LAPACK INFO: 1-based index of the first zero pivot
 
 
-def test_tensor_core_variant_choice_does_not_change_results(need_gpu):
-    """The first product of a shape times the per-tile and the persistent tcgen05 kernels
-    and keeps the faster; both issue the same MMAs in the same order, so the tuning call
-    and the later (cached-choice) calls give bitwise equal results."""
+def test_tensor_core_variant_choice_does_not_change_results(need_gpu, monkeypatch):
+    """The first product of a shape times the two per-tile tcgen05 kernels (different N
+    tiles) and the persistent one and keeps the fastest; all issue each output's MMAs in
+    the same K order into exact accumulators, so every variant, the tuning call and the
+    later (cached-choice) calls give bitwise equal results.  NEGF_TC_VARIANT forces one."""
     rng = np.random.default_rng(11)
-    for s in (3, 5, 7):
-        a = rng.standard_normal((6, 96, 96)) + 1j * rng.standard_normal((6, 96, 96))
-        b = rng.standard_normal((6, 96, 96)) + 1j * rng.standard_normal((6, 96, 96))
-        first = capi.zgemm(a, b, slices=s)
-        again = capi.zgemm(a, b, slices=s)
-        assert np.array_equal(first, again)
+    for s in (3, 4, 5, 6, 7, 8):
+        for shape in ((6, 96, 96, 96), (3, 144, 144, 144), (2, 400, 400, 400)):
+            nb, m, n, k = shape
+            a = rng.standard_normal((nb, m, k)) + 1j * rng.standard_normal((nb, m, k))
+            b = rng.standard_normal((nb, k, n)) + 1j * rng.standard_normal((nb, k, n))
+            monkeypatch.delenv("NEGF_TC_VARIANT", raising=False)
+            first = capi.zgemm(a, b, slices=s)
+            again = capi.zgemm(a, b, slices=s)
+            assert np.array_equal(first, again), (s, shape)
+            for v in ("0", "1", "2"):
+                monkeypatch.setenv("NEGF_TC_VARIANT", v)
+                assert np.array_equal(capi.zgemm(a, b, slices=s), first), (s, shape, v)
+            assert (np.abs(first - a @ b) <= _bound(a, b, s)).all(), (s, shape)
+    monkeypatch.delenv("NEGF_TC_VARIANT", raising=False)
+
+
+@pytest.mark.parametrize("S", [3, 5, 7, 8])
+def test_sliced_gemm_split_k_accumulators(need_gpu, S):
+    """K' = 2k > 800: the K blocks are split in two halves with their own exact
+    accumulators (k = 576 and 784, the config-5 and largest config-4 cross-sections, and
+    an odd k = 613); the error bound is the same, alpha and beta are applied once."""
+    rng = np.random.default_rng(100 + S)
+    for (m, n, k) in ((576, 576, 576), (784, 160, 784), (200, 136, 613)):
+        A = _rand(rng, 1, m, k, spread=1.0)
+        B = _rand(rng, 1, k, n)
+        C = _rand(rng, 1, m, n)
+        al, be = 0.5 + 0.25j, 1.0
+        got = capi.zgemm(A, B, C, alpha=al, beta=be, slices=S)
+        ref = al * (A @ B) + be * C
+        assert (np.abs(got - ref) <= abs(al) * _bound(A, B, S) + 1e-12 * np.abs(C)).all(), (S, m, n, k)
+
+
+def test_sliced_gemm_refuses_k_beyond_its_exact_accumulators(need_gpu):
+    A = np.zeros((1, 16, 801), dtype=complex)
+    B = np.zeros((1, 801, 16), dtype=complex)
+    with pytest.raises(capi.NegfError) as ei:
+        capi.zgemm(A, B, slices=5)
+    assert ei.value.code == capi.NEGF_EINVAL

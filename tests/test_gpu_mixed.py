@@ -195,3 +195,26 @@ def test_set_refinement_validates_its_arguments(need_gpu):
         with pytest.raises(capi.NegfError) as ei:
             s.set_refinement(ns_max_steps=3)
         assert ei.value.code == capi.NEGF_ESTATE
+
+
+def test_fused_gauss_jordan_gives_the_same_bits_as_the_three_launch_form(need_gpu):
+    """A batch with at least one matrix per SM inverts its FP32 blocks with the fused
+    one-CTA-per-matrix Gauss-Jordan kernel; smaller batches use the panel / interchange /
+    update launches.  Both run the same operations in the same order, so a request's
+    results are bitwise the same in a batch of 160 and in batches of 8."""
+    npx, npy, npz = 6, 3, 3
+    htotd, hopx = HB.ti_wire(npx, npy, npz, W=0.1, seed=6, flux=0.5, zeeman=0.01)
+    es = np.linspace(-0.29, 0.29, 160)
+    f1 = np.full(es.size, 0.7)
+    f2 = np.full(es.size, 0.2)
+    out = []
+    for mb in (160, 8):
+        with Solver(npx, npy, npz, eta=1e-5, sr_tol=1e-10, calc_spin=True, max_batch=mb, precision="mixed") as s:
+            s.set_hamiltonian(htotd, hopx)
+            rn = s.new_site_array(1)
+            r = s.solve_batch(es, f1, f2, 1e-3, rho_n=rn)
+            out.append((r, rn))
+    (ra, rna), (rb, rnb) = out
+    assert (ra["status"] == 0).all() and (rb["status"] == 0).all()
+    for k in ("T12", "Modec1", "Modec2", "EDensity", "HDensity", "DOSc1"):
+        assert np.array_equal(ra[k], rb[k]), k
