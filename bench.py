@@ -208,15 +208,29 @@ def cpu_sample(n_energies=1):
 SERVING_XS = (6, 8, 10)            # Npy = Npz of the served wires (M = 144, 256, 400)
 SERVING_NPX = (50, 75, 100)
 SERVING_E = (8, 64)                # energies per request, log-uniform
+# the serving configuration as stated: Npy = Npz in {6, 8, 10, 12, 14} (M up to 784), Npx
+# uniform in [50, 200], energies per request log-uniform in [64, 1024] (scaled by
+# --serving-energy-scale to bound the run)
+C4_XS = (6, 8, 10, 12, 14)
+C4_NPX = (50, 200)
+C4_E = (64, 1024)
 
 
-def serving_request(rng):
+def serving_request(rng, mix="reduced", e_scale=1.0):
     """One request of the serving mix: a wire given as a model (its Hamiltonian is built on
-    the device), per-request disorder seed, W ~ U[0, 0.2] eV and flux ~ U[0, 1] Phi_0."""
+    the device), per-request disorder seed, W ~ U[0, 0.2] eV and flux ~ U[0, 1] Phi_0.
+    mix "reduced": the bench's default mix; "c4": the serving configuration's cross-sections,
+    Npx in [50, 200] and [64, 1024] energies times e_scale."""
     from nonequilibriumgreensfunction_gb300 import hamiltonian as HB
-    n = int(rng.choice(SERVING_XS))
-    npx = int(rng.choice(SERVING_NPX))
-    ne = int(round(math.exp(rng.uniform(math.log(SERVING_E[0]), math.log(SERVING_E[1])))))
+    if mix == "c4":
+        n = int(rng.choice(C4_XS))
+        npx = int(rng.integers(C4_NPX[0], C4_NPX[1] + 1))
+        lo, hi = C4_E[0] * e_scale, C4_E[1] * e_scale
+    else:
+        n = int(rng.choice(SERVING_XS))
+        npx = int(rng.choice(SERVING_NPX))
+        lo, hi = SERVING_E
+    ne = max(1, int(round(math.exp(rng.uniform(math.log(lo), math.log(hi))))))
     e = np.sort(rng.choice(energy_grid(), size=ne, replace=False))
     model = HB.wire_model(W=float(rng.uniform(0.0, 0.2)), seed=int(rng.integers(1 << 62)),
                           flux=float(rng.uniform(0.0, 1.0)), zeeman=ZEEMAN)
@@ -225,16 +239,19 @@ def serving_request(rng):
     return dict(shape=(npx, n, n), model=model, energies=e, f1=f1, f2=f2, dE=0.6 / (N_E - 1))
 
 
-def serving_bench(seconds, device):
-    """p50/p99 latency under Poisson arrivals at 80% of the measured capacity (the serving
-    configuration, scaled to a bench run: cross-sections {6, 8, 10}, Npx in {50, 75, 100},
-    8-64 energies per request instead of {6..14}, [50, 200] and 64-1024)."""
+def serving_bench(seconds, device, form="mixed", mix="reduced", e_scale=1.0, burst_n=24):
+    """p50/p99 latency under Poisson arrivals at 80% of the measured capacity.  mix
+    "reduced" (the default bench run): cross-sections {6, 8, 10}, Npx in {50, 75, 100},
+    8-64 energies per request instead of {6..14}, [50, 200] and 64-1024; mix "c4": the
+    serving configuration's wires with the energies per request scaled by e_scale."""
     from nonequilibriumgreensfunction_gb300.serving import Server, run_poisson_load
     rng = np.random.default_rng(4)
-    with Server(precision="mixed", max_batch=32, slots_per_geometry=8, eta=ETA, sr_tol=SR_TOL,
+    mk = lambda g: serving_request(g, mix, e_scale)  # noqa: E731
+    slots = 8 if mix == "reduced" else 2
+    with Server(precision=form, max_batch=32, slots_per_geometry=slots, eta=ETA, sr_tol=SR_TOL,
                 device=device) as srv:
         # capacity: a closed burst (also creates the engines of the geometries)
-        burst = [serving_request(rng) for _ in range(24)]
+        burst = [mk(rng) for _ in range(burst_n)]
         t0 = time.perf_counter()
         ids = [srv.submit_model(*r["shape"], r["model"], r["energies"], r["f1"], r["f2"], r["dE"]) for r in burst]
         for rid in ids:
@@ -245,29 +262,52 @@ def serving_bench(seconds, device):
         capacity = cap_solves / cap_wall
         mean_e = float(np.mean([r["energies"].size for r in burst]))
         rate = 0.8 * capacity / mean_e
-        lat, solves, wall = run_poisson_load(srv, serving_request, rate, seconds, rng)
+        lat, solves, wall = run_poisson_load(srv, mk, rate, seconds, rng)
+    if mix == "c4":
+        load = ("Poisson arrivals at 0.8 x measured capacity; Npy=Npz in {6,8,10,12,14} (M up to 784), "
+                "Npx ~ U[50,200], %g-%g energies/request (log-uniform; the configuration's 64-1024 x %g), "
+                "W~U[0,0.2] eV, flux~U[0,1] Phi0, per-request seed; wires sent as models and built on the "
+                "device" % (C4_E[0] * e_scale, C4_E[1] * e_scale, e_scale))
+    else:
+        load = ("Poisson arrivals at 0.8 x measured capacity; Npy=Npz in {6,8,10}, Npx in {50,75,100}, "
+                "8-64 energies/request (log-uniform), W~U[0,0.2] eV, flux~U[0,1] Phi0, per-request seed; "
+                "wires sent as models and built on the device")
     return {"p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+            "p90_s": float(np.percentile(lat, 90)), "mean_s": float(np.mean(lat)),
             "solves_per_s": solves / wall, "capacity_solves_per_s": capacity, "arrival_rate_req_per_s": rate,
-            "requests": int(lat.size), "seconds": seconds, "form": "mixed",
-            "load": "Poisson arrivals at 0.8 x measured capacity; Npy=Npz in {6,8,10}, Npx in {50,75,100}, "
-                    "8-64 energies/request (log-uniform), W~U[0,0.2] eV, flux~U[0,1] Phi0, per-request seed; "
-                    "wires sent as models and built on the device"}
+            "requests": int(lat.size), "seconds": seconds, "wall_s": wall, "form": form, "mix": mix,
+            "load": load}
+
+
+def run_serving_bench(args):
+    """The serving leg on its own (--workload serving): one JSON line with a result per form."""
+    forms = ["mixed", "fp64"] if args.serving_form == "both" else [args.serving_form]
+    out = {"metric": "serving p50/p99 latency (s) and solves/s under Poisson arrivals at 80% of capacity",
+           "workload": "serving_%s" % args.serving_config, "data": "synthetic", "results": []}
+    for f in forms:
+        secs = args.serving_seconds if f == "mixed" or args.serving_fp64_seconds <= 0 else args.serving_fp64_seconds
+        scale = args.serving_energy_scale if f == "mixed" else args.serving_fp64_energy_scale
+        out["results"].append(serving_bench(secs, 0, form=f, mix=args.serving_config, e_scale=scale,
+                                            burst_n=args.serving_burst))
+    print(json.dumps(out), flush=True)
 
 
 def run_scf_bench(args):
     """Self-consistent bias point at the config-5 geometry: Npx = 60, Npy = Npz = 12 (M = 576),
     W = 0.1 eV, mu_L - mu_R = 0.05 eV, eps_r = 100, a 0.1 eV gate on the wire surface, linear
-    mixing 0.3 for 10 iterations, mixed form.  The sample is 64 energies x 2 disorder seeds
-    per iteration (the configuration names 1024 x 8), stated in the output.  The mixed solve
-    is then compared with the FP64 solve on the converged potential: T(E) at 16 energies."""
+    mixing 0.3 for 10 iterations, mixed form.  The sample is --scf-energies energies x
+    --scf-seeds disorder seeds per iteration (the configuration names 1024 x 8), stated in
+    the output.  The mixed solve is then compared with the FP64 solve on the converged
+    potential: T(E) at 16 energies."""
     from nonequilibriumgreensfunction_gb300 import Solver, scf
     from nonequilibriumgreensfunction_gb300 import hamiltonian as HB
-    npx, npy, npz, n_seeds, n_e, n_iter = 60, 12, 12, 2, 64, 10
+    npx, npy, npz, n_iter = 60, 12, 12, 10
+    n_seeds, n_e = args.scf_seeds, args.scf_energies
     mu_l, mu_r = 0.025, -0.025
     models = [HB.wire_model(W=0.1, seed=s, zeeman=ZEEMAN) for s in range(n_seeds)]
     energies = np.linspace(-0.3, 0.3, n_e)
     de = energies[1] - energies[0]
-    with Solver(npx, npy, npz, n_hamiltonians=n_seeds, max_batch=n_e * n_seeds, eta=ETA, sr_tol=SR_TOL,
+    with Solver(npx, npy, npz, n_hamiltonians=n_seeds, max_batch=min(n_e * n_seeds, 256), eta=ETA, sr_tol=SR_TOL,
                 precision="mixed") as s:
         t0 = time.perf_counter()
         out = scf.run_scf(s, models, energies, de, mu_l, mu_r, KT, eps_r=100.0, u_gate=0.1, beta=0.3,
@@ -296,7 +336,7 @@ def run_scf_bench(args):
             "config": {"npx": npx, "npy": npy, "npz": npz, "M": 4 * npy * npz, "seeds": n_seeds,
                        "energies_per_iteration": n_e, "eps_r": 100.0, "gate_eV": 0.1, "mixing": 0.3,
                        "mu_l": mu_l, "mu_r": mu_r, "kT": KT,
-                       "sample": "64 energies x 2 seeds per iteration (config: 1024 x 8)"},
+                       "sample": "%d energies x %d seeds per iteration (config: 1024 x 8)" % (n_e, n_seeds)},
             "data": "synthetic"}
     print(json.dumps(line), flush=True)
 
@@ -363,8 +403,21 @@ def main():
                     help="steps of the end-to-end leg (each re-uploads the Hamiltonians); at most --steps")
     ap.add_argument("--npx", type=int, default=NPX,
                     help="slices of the wire; the benchmark workload is 100, shorter wires only for profiling")
-    ap.add_argument("--workload", default="wire", choices=["wire", "scf"],
-                    help="wire: the solves/s benchmark; scf: the self-consistent bias point (config 5 geometry)")
+    ap.add_argument("--workload", default="wire", choices=["wire", "scf", "serving"],
+                    help="wire: the solves/s benchmark; scf: the self-consistent bias point (config 5 geometry); "
+                         "serving: the serving leg alone")
+    ap.add_argument("--serving-config", default="reduced", choices=["reduced", "c4"],
+                    help="--workload serving: the bench's reduced mix or the serving configuration's wires")
+    ap.add_argument("--serving-form", default="mixed", choices=["mixed", "fp64", "both"])
+    ap.add_argument("--serving-energy-scale", type=float, default=1.0 / 16,
+                    help="c4 mix: energies per request are log-uniform in [64, 1024] x this")
+    ap.add_argument("--serving-fp64-energy-scale", type=float, default=1.0 / 64,
+                    help="c4 mix, FP64 form: the same scale for the FP64 server")
+    ap.add_argument("--serving-fp64-seconds", type=float, default=0.0,
+                    help="--workload serving: Poisson seconds of the FP64 form (0 = --serving-seconds)")
+    ap.add_argument("--serving-burst", type=int, default=24, help="requests of the closed capacity burst")
+    ap.add_argument("--scf-energies", type=int, default=64, help="--workload scf: energies per iteration")
+    ap.add_argument("--scf-seeds", type=int, default=2, help="--workload scf: disorder seeds per iteration")
     ap.add_argument("--kernel-case", default="none", choices=["none", "gemm_tc"],
                     help="profiling aid: run only one kernel case (gemm_tc: 16 complex 400^3 products at "
                          "--slices slices, twice) and exit")
@@ -388,6 +441,9 @@ def main():
         return
     if args.workload == "scf":
         run_scf_bench(args)
+        return
+    if args.workload == "serving":
+        run_serving_bench(args)
         return
     if args.kernel_case == "gemm_tc":
         from nonequilibriumgreensfunction_gb300 import capi

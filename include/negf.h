@@ -122,6 +122,12 @@ NEGF_API int  negf_destroy(negf_handle* h);
 NEGF_API const char* negf_strerror(int code);
 /* bytes of device memory the handle holds (for admission / reporting) */
 NEGF_API int  negf_device_bytes(const negf_handle* h, int64_t* bytes);
+/* bytes of device memory negf_create would allocate for these parameters, computed on the
+ * host without a device (the admission unit of the serving layer: the Npx*M^2*16-byte
+ * block store per batch entry plus the Hamiltonian slots and work buffers).  No reference
+ * counterpart: the reference allocates its arrays per rank at start-up
+ * (Source/Read_In_Allocate.F90:104-238).  NEGF_EINVAL for parameters negf_create refuses. */
+NEGF_API int  negf_estimate_device_bytes(const negf_params* p, int64_t* bytes);
 
 /* Run the handle's work on a caller-owned CUDA stream (cudaStream_t passed as void*);
  * NULL restores the handle's own stream.  Calls still return only after their results

@@ -32,7 +32,7 @@ NEGF_CONTACT_LEADS, NEGF_CONTACT_PBIG, NEGF_CONTACT_PSMALL, NEGF_CONTACT_SC = 0,
 
 # every symbol include/negf.h declares
 EXPORTED_SYMBOLS = (
-    "negf_create", "negf_destroy", "negf_strerror", "negf_device_bytes",
+    "negf_create", "negf_destroy", "negf_strerror", "negf_device_bytes", "negf_estimate_device_bytes",
     "negf_set_stream", "negf_profile", "negf_get_stats", "negf_set_refinement",
     "negf_set_hamiltonian", "negf_build_hamiltonian", "negf_contact_self_energy", "negf_get_retarded_greens",
     "negf_copy_g_columns", "negf_calculate_gnp", "negf_calculate_observables",
@@ -153,6 +153,7 @@ def _declare(lib):
         "negf_destroy": (c_int, [h]),
         "negf_strerror": (c_char_p, [c_int]),
         "negf_device_bytes": (c_int, [h, POINTER(c_int64)]),
+        "negf_estimate_device_bytes": (c_int, [POINTER(NegfParams), POINTER(c_int64)]),
         "negf_set_stream": (c_int, [h, c_void_p]),
         "negf_profile": (c_int, [h, c_int]),
         "negf_get_stats": (c_int, [h, POINTER(NegfStats)]),

@@ -141,6 +141,16 @@ int negf_device_bytes(const negf_handle* h, int64_t* bytes) {
   return NEGF_OK;
 }
 
+int negf_estimate_device_bytes(const negf_params* p, int64_t* bytes) {
+  if (!p || !bytes) return NEGF_EINVAL;
+  for (int i = 0; i < 3; ++i)
+    if (p->reserved[i] != 0) return NEGF_EINVAL;
+  const long long b = Engine::estimate_bytes(*p);
+  if (b < 0) return NEGF_EINVAL;
+  *bytes = b;
+  return NEGF_OK;
+}
+
 int negf_set_stream(negf_handle* h, void* stream) {
   if (!h) return NEGF_EINVAL;
   Engine& e = h->eng;

@@ -47,8 +47,10 @@ __global__ void merge_info_k(int batch, const int* info, int* status) {
   if (b < batch && status[b] == 0 && info[b] != 0) status[b] = info[b];
 }
 
+// device allocation of `count` T, added to `bytes`; with `dry` only the bytes are counted
 template <typename T>
-int dalloc(T** p, size_t count, long long& bytes) {
+int dalloc(T** p, size_t count, long long& bytes, bool dry = false) {
+  if (dry) { *p = nullptr; bytes += (long long)(sizeof(T) * count); return NEGF_OK; }
   if (count == 0) { *p = nullptr; return NEGF_OK; }
   if (cudaMalloc((void**)p, sizeof(T) * count) != cudaSuccess) { *p = nullptr; return NEGF_ENOMEM; }
   bytes += (long long)(sizeof(T) * count);
@@ -97,7 +99,7 @@ Engine::~Engine() {
   if (own_st_) cudaStreamDestroy(own_st_);
 }
 
-int Engine::init(const negf_params& p) {
+int Engine::configure(const negf_params& p) {
   if (p.npx < 2 || p.npy < 1 || p.npz < 1 || p.norb < 1 || p.norb > 8) return NEGF_EINVAL;
   if (p.contact_type < NEGF_CONTACT_LEADS || p.contact_type > NEGF_CONTACT_SC || p.reserved1 != 0) return NEGF_EINVAL;
   for (int i = 0; i < 8; ++i)
@@ -116,9 +118,6 @@ int Engine::init(const negf_params& p) {
     return NEGF_EINVAL;
   // the tensor-core products keep exact accumulators up to K' = 2 M = 1600
   if (p.precision == NEGF_PREC_MIXED && 2 * padded_k(p.norb * p.npy * p.npz) > 1600) return NEGF_EINVAL;
-  int ndev = 0;
-  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return NEGF_ENODEV;
-  if (p.device < 0 || p.device >= ndev) return NEGF_EINVAL;
   p_ = p;
   M_ = p.norb * p.npy * p.npz;
   MM_ = (long long)M_ * M_;
@@ -139,6 +138,22 @@ int Engine::init(const negf_params& p) {
     if (p.residual_slices < 5 || p.residual_slices > 8) return NEGF_EINVAL;
     s_res_ = p.residual_slices;
   }
+  return NEGF_OK;
+}
+
+long long Engine::estimate_bytes(const negf_params& p) {
+  Engine e;
+  if (e.configure(p) != NEGF_OK) return -1;
+  e.dry_ = true;
+  if (e.alloc() != NEGF_OK) return -1;
+  return e.bytes_;
+}
+
+int Engine::init(const negf_params& p) {
+  NEGF_TRY(configure(p));
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return NEGF_ENODEV;
+  if (p.device < 0 || p.device >= ndev) return NEGF_EINVAL;
   NEGF_CUDA_TRY(cudaSetDevice(p.device));
   NEGF_CUDA_TRY(cudaStreamCreateWithFlags(&own_st_, cudaStreamNonBlocking));
   st_ = own_st_;
@@ -153,84 +168,90 @@ int Engine::init(const negf_params& p) {
 int Engine::alloc() {
   const long long N = p_.npx;
   const long long total = nsite_total();
-  NEGF_TRY(dalloc(&dH_, (size_t)(p_.n_hamiltonians * N * MM_), bytes_));
-  NEGF_TRY(dalloc(&dHop_, (size_t)MM_, bytes_));
-  NEGF_TRY(dalloc(&dHopBD_, (size_t)nsite_ * p_.norb * p_.norb, bytes_));
-  NEGF_TRY(dalloc(&dSpin_, (size_t)3 * p_.norb * p_.norb, bytes_));
-  NEGF_TRY(dalloc(&dHtab_, (size_t)16 * (2 + p_.npz), bytes_));
-  NEGF_TRY(dalloc(&dVext_, (size_t)total, bytes_));
-  NEGF_TRY(dalloc(&dG_, (size_t)(B_ * N * MM_), bytes_));
+  NEGF_TRY(dalloc(&dH_, (size_t)(p_.n_hamiltonians * N * MM_), bytes_, dry_));
+  NEGF_TRY(dalloc(&dHop_, (size_t)MM_, bytes_, dry_));
+  NEGF_TRY(dalloc(&dHopBD_, (size_t)nsite_ * p_.norb * p_.norb, bytes_, dry_));
+  NEGF_TRY(dalloc(&dSpin_, (size_t)3 * p_.norb * p_.norb, bytes_, dry_));
+  NEGF_TRY(dalloc(&dHtab_, (size_t)16 * (2 + p_.npz), bytes_, dry_));
+  NEGF_TRY(dalloc(&dVext_, (size_t)total, bytes_, dry_));
+  NEGF_TRY(dalloc(&dG_, (size_t)(B_ * N * MM_), bytes_, dry_));
   double2** bufs[] = {&dC1_, &dCN_, &dZ_, &dY_, &dQ_, &dSigL_, &dSigR_, &dGamL_, &dGamR_};
-  for (double2** b : bufs) NEGF_TRY(dalloc(b, (size_t)(B_ * MM_), bytes_));
-  NEGF_TRY(dalloc(&dP1_, (size_t)(B_ * N * M_ * p_.norb), bytes_));
-  NEGF_TRY(dalloc(&dP2_, (size_t)(B_ * N * M_ * p_.norb), bytes_));
+  for (double2** b : bufs) NEGF_TRY(dalloc(b, (size_t)(B_ * MM_), bytes_, dry_));
+  NEGF_TRY(dalloc(&dP1_, (size_t)(B_ * N * M_ * p_.norb), bytes_, dry_));
+  NEGF_TRY(dalloc(&dP2_, (size_t)(B_ * N * M_ * p_.norb), bytes_, dry_));
   if (keep_columns_) {
-    NEGF_TRY(dalloc(&dCol1_, (size_t)(N * MM_), bytes_));
-    NEGF_TRY(dalloc(&dColN_, (size_t)(N * MM_), bytes_));
+    NEGF_TRY(dalloc(&dCol1_, (size_t)(N * MM_), bytes_, dry_));
+    NEGF_TRY(dalloc(&dColN_, (size_t)(N * MM_), bytes_, dry_));
   }
   if (currents_) {
     double2** pb[] = {&dPx1_, &dPy1_, &dPz1_, &dPx2_, &dPy2_, &dPz2_};
-    for (double2** b : pb) NEGF_TRY(dalloc(b, (size_t)(B_ * N * M_ * p_.norb), bytes_));
-    NEGF_TRY(dalloc(&dYalt_, (size_t)(B_ * MM_), bytes_));
-    NEGF_TRY(dalloc(&dCNalt_, (size_t)(B_ * MM_), bytes_));
+    for (double2** b : pb) NEGF_TRY(dalloc(b, (size_t)(B_ * N * M_ * p_.norb), bytes_, dry_));
+    NEGF_TRY(dalloc(&dYalt_, (size_t)(B_ * MM_), bytes_, dry_));
+    NEGF_TRY(dalloc(&dCNalt_, (size_t)(B_ * MM_), bytes_, dry_));
     // the x bond of the last slice does not exist: its blocks stay zero
-    for (double2* b : {dPx1_, dPx2_})
-      NEGF_CUDA_TRY(cudaMemset(b, 0, sizeof(double2) * (size_t)(B_ * N * M_ * p_.norb)));
+    if (!dry_)
+      for (double2* b : {dPx1_, dPx2_})
+        NEGF_CUDA_TRY(cudaMemset(b, 0, sizeof(double2) * (size_t)(B_ * N * M_ * p_.norb)));
   } else {
     dYalt_ = dY_;
     dCNalt_ = dCN_;
   }
   sums_blocks_ = (int)((total + 255) / 256);
-  if (p_.contact_type != NEGF_CONTACT_LEADS) NEGF_TRY(dalloc(&dContactCoef_, (size_t)S_ * 6, bytes_));
+  if (p_.contact_type != NEGF_CONTACT_LEADS) NEGF_TRY(dalloc(&dContactCoef_, (size_t)S_ * 6, bytes_, dry_));
   if (sc_()) {
-    NEGF_TRY(dalloc(&dG11_, (size_t)B_ * M_ * p_.norb, bytes_));
-    NEGF_TRY(dalloc(&dTrJ_, (size_t)B_, bytes_));
+    NEGF_TRY(dalloc(&dG11_, (size_t)B_ * M_ * p_.norb, bytes_, dry_));
+    NEGF_TRY(dalloc(&dTrJ_, (size_t)B_, bytes_, dry_));
   }
-  NEGF_TRY(dalloc(&dSite_, (size_t)(B_ * nf_ * total), bytes_));
-  NEGF_TRY(dalloc(&dSums_, (size_t)B_ * sums_blocks_ * 2, bytes_));
-  NEGF_TRY(dalloc(&dTr_, (size_t)B_ * 4, bytes_));
-  NEGF_TRY(dalloc(&dAcc_, (size_t)(p_.n_hamiltonians * nf_ * total), bytes_));
-  NEGF_TRY(dalloc(&dStatus_, (size_t)B_, bytes_));
-  NEGF_TRY(dalloc(&dItems_, (size_t)B_, bytes_));
-  NEGF_TRY(dalloc(&dSr_, (size_t)(kSrBlocks * S_ * MM_), bytes_));
+  NEGF_TRY(dalloc(&dSite_, (size_t)(B_ * nf_ * total), bytes_, dry_));
+  NEGF_TRY(dalloc(&dSums_, (size_t)B_ * sums_blocks_ * 2, bytes_, dry_));
+  NEGF_TRY(dalloc(&dTr_, (size_t)B_ * 4, bytes_, dry_));
+  NEGF_TRY(dalloc(&dAcc_, (size_t)(p_.n_hamiltonians * nf_ * total), bytes_, dry_));
+  NEGF_TRY(dalloc(&dStatus_, (size_t)B_, bytes_, dry_));
+  NEGF_TRY(dalloc(&dItems_, (size_t)B_, bytes_, dry_));
+  NEGF_TRY(dalloc(&dSr_, (size_t)(kSrBlocks * S_ * MM_), bytes_, dry_));
   double2** srb[] = {&dSrSigL_, &dSrSigR_, &dSrGamL_, &dSrGamR_};
-  for (double2** b : srb) NEGF_TRY(dalloc(b, (size_t)(S_ * MM_), bytes_));
-  NEGF_TRY(dalloc(&dSrCmax_, (size_t)2 * S_, bytes_));
-  NEGF_TRY(dalloc(&dSrDos_, (size_t)2 * S_, bytes_));
-  NEGF_TRY(dalloc(&dSrActive_, (size_t)2 * S_, bytes_));
-  NEGF_TRY(dalloc(&dSrE_, (size_t)S_, bytes_));
-  NEGF_TRY(dalloc(&dSrHend_, (size_t)S_, bytes_));
-  NEGF_TRY(dalloc(&dSrStatus_, (size_t)S_, bytes_));
-  NEGF_TRY(inv_work_alloc(inv_, M_, std::max(B_, S_)));
+  for (double2** b : srb) NEGF_TRY(dalloc(b, (size_t)(S_ * MM_), bytes_, dry_));
+  NEGF_TRY(dalloc(&dSrCmax_, (size_t)2 * S_, bytes_, dry_));
+  NEGF_TRY(dalloc(&dSrDos_, (size_t)2 * S_, bytes_, dry_));
+  NEGF_TRY(dalloc(&dSrActive_, (size_t)2 * S_, bytes_, dry_));
+  NEGF_TRY(dalloc(&dSrE_, (size_t)S_, bytes_, dry_));
+  NEGF_TRY(dalloc(&dSrHend_, (size_t)S_, bytes_, dry_));
+  NEGF_TRY(dalloc(&dSrStatus_, (size_t)S_, bytes_, dry_));
+  {   // inv_work_alloc: R buffer, pivots, INFO
+    const long long cap = std::max(B_, S_);
+    if (!dry_) NEGF_TRY(inv_work_alloc(inv_, M_, (int)cap));
+    bytes_ += 16LL * cap * panel_width(M_) * M_ + 4LL * cap * M_ + 4LL * cap;
+  }
   if (mixed_) {
     const int cap = std::max(B_, S_);
     const int smax = 8;   // every slice count a phase may use (RGF, Sancho-Rubio, residual: <= 8)
-    NEGF_TRY(dalloc(&dWinv_, (size_t)(cap * MM_), bytes_));
-    NEGF_TRY(dalloc(&dW32_, (size_t)(cap * MM_), bytes_));
-    NEGF_TRY(dalloc(&dT_, (size_t)(cap * MM_), bytes_));
+    NEGF_TRY(dalloc(&dWinv_, (size_t)(cap * MM_), bytes_, dry_));
+    NEGF_TRY(dalloc(&dW32_, (size_t)(cap * MM_), bytes_, dry_));
+    NEGF_TRY(dalloc(&dT_, (size_t)(cap * MM_), bytes_, dry_));
     const int kp = padded_k(M_);
-    NEGF_TRY(dalloc(reinterpret_cast<char**>(&sa_.data), sliced_bytes_a(M_, kp, smax, cap), bytes_));
-    NEGF_TRY(dalloc(reinterpret_cast<char**>(&sb_.data), sliced_bytes_b(M_, kp, smax, cap), bytes_));
-    NEGF_TRY(dalloc(reinterpret_cast<char**>(&sw_.data), sliced_bytes_a(M_, kp, smax, cap), bytes_));
-    NEGF_TRY(dalloc(&sw_.exps, (size_t)cap * M_, bytes_));
-    NEGF_TRY(dalloc(&sa_.exps, (size_t)cap * M_, bytes_));
-    NEGF_TRY(dalloc(&sb_.exps, (size_t)cap * M_, bytes_));
-    NEGF_TRY(dalloc(reinterpret_cast<char**>(&sgl_.data), sliced_bytes_b(M_, kp, s_rgf_, B_), bytes_));
-    NEGF_TRY(dalloc(reinterpret_cast<char**>(&sgr_.data), sliced_bytes_b(M_, kp, s_rgf_, B_), bytes_));
-    NEGF_TRY(dalloc(&sgl_.exps, (size_t)B_ * M_, bytes_));
-    NEGF_TRY(dalloc(&sgr_.exps, (size_t)B_ * M_, bytes_));
+    NEGF_TRY(dalloc(reinterpret_cast<char**>(&sa_.data), sliced_bytes_a(M_, kp, smax, cap), bytes_, dry_));
+    NEGF_TRY(dalloc(reinterpret_cast<char**>(&sb_.data), sliced_bytes_b(M_, kp, smax, cap), bytes_, dry_));
+    NEGF_TRY(dalloc(reinterpret_cast<char**>(&sw_.data), sliced_bytes_a(M_, kp, smax, cap), bytes_, dry_));
+    NEGF_TRY(dalloc(&sw_.exps, (size_t)cap * M_, bytes_, dry_));
+    NEGF_TRY(dalloc(&sa_.exps, (size_t)cap * M_, bytes_, dry_));
+    NEGF_TRY(dalloc(&sb_.exps, (size_t)cap * M_, bytes_, dry_));
+    NEGF_TRY(dalloc(reinterpret_cast<char**>(&sgl_.data), sliced_bytes_b(M_, kp, s_rgf_, B_), bytes_, dry_));
+    NEGF_TRY(dalloc(reinterpret_cast<char**>(&sgr_.data), sliced_bytes_b(M_, kp, s_rgf_, B_), bytes_, dry_));
+    NEGF_TRY(dalloc(&sgl_.exps, (size_t)B_ * M_, bytes_, dry_));
+    NEGF_TRY(dalloc(&sgr_.exps, (size_t)B_ * M_, bytes_, dry_));
     sgl_.data_bytes = sgr_.data_bytes = sliced_bytes_b(M_, kp, s_rgf_, B_);
     sgl_.exps_count = sgr_.exps_count = (size_t)B_ * M_;
     sa_.data_bytes = sw_.data_bytes = sliced_bytes_a(M_, kp, smax, cap);
     sb_.data_bytes = sliced_bytes_b(M_, kp, smax, cap);
     sa_.exps_count = sb_.exps_count = sw_.exps_count = (size_t)cap * M_;
-    NEGF_TRY(dalloc(&dRnorm_, (size_t)cap, bytes_));
-    NEGF_TRY(dalloc(&dNsIdx_, (size_t)cap, bytes_));
-    NEGF_TRY(dalloc(&dNsX_, (size_t)cap * MM_, bytes_));
-    NEGF_TRY(dalloc(&dNsW_, (size_t)cap * MM_, bytes_));
-    NEGF_TRY(dalloc(&dTcErr_, (size_t)1, bytes_));
-    NEGF_CUDA_TRY(cudaMemset(dTcErr_, 0, sizeof(int)));
+    NEGF_TRY(dalloc(&dRnorm_, (size_t)cap, bytes_, dry_));
+    NEGF_TRY(dalloc(&dNsIdx_, (size_t)cap, bytes_, dry_));
+    NEGF_TRY(dalloc(&dNsX_, (size_t)cap * MM_, bytes_, dry_));
+    NEGF_TRY(dalloc(&dNsW_, (size_t)cap * MM_, bytes_, dry_));
+    NEGF_TRY(dalloc(&dTcErr_, (size_t)1, bytes_, dry_));
+    if (!dry_) NEGF_CUDA_TRY(cudaMemset(dTcErr_, 0, sizeof(int)));
   }
+  if (dry_) return NEGF_OK;   // estimate_bytes: device bytes only
   hPinBytes_ = sizeof(double) * (size_t)std::max<long long>(
                    {(long long)B_ * sums_blocks_ * 2, (long long)B_ * 4, 4LL * S_,
                     (long long)p_.n_hamiltonians * nf_ * total, (long long)nf_ * total, 64});

@@ -32,6 +32,9 @@ class Engine {
  public:
   ~Engine();
   int init(const negf_params& p);
+  // device bytes an engine with these parameters allocates at init (< 0: invalid
+  // parameters); the serving layer admits engines by it
+  static long long estimate_bytes(const negf_params& p);
   int set_hamiltonian(int slot, const double* Htotd, const double* HopX);
   // Htotd of `slot` generated on the device from a wire model (Build_Hamiltonian)
   int build_hamiltonian(int slot, const negf_wire_model& m);
@@ -197,6 +200,8 @@ class Engine {
   bool keep_columns_ = false;
 
  private:
+  int configure(const negf_params& p);   // validation and derived sizes, no CUDA calls
+  bool dry_ = false;                      // alloc() counts bytes without allocating
   int alloc();
   // Y = op(H) X (left) or X op(H) (right) for every block of a strided batch
   int hop_mul(int left, Op op, const double2* X, long long sX, double2* Y, long long sY, int batch);

@@ -102,13 +102,11 @@ struct negf_server {
     return ep;
   }
 
-  // upper estimate of an engine's device bytes (mirrors Engine::alloc)
+  // an engine's device bytes: Engine::alloc counted without allocating, plus 64 MB for the
+  // allocator's rounding and the library's per-context state
   long long estimate(const GeomKey& k) const {
-    const long long m = (long long)k.norb * k.npy * k.npz, mm = m * m, n = k.npx, b = p.max_batch, s = 2 * b;
-    long long blocks = p.slots_per_geometry * n * mm + b * n * mm + 9 * b * mm + 17 * s * mm + 2 * b * n * m * k.norb;
-    long long bytes = blocks * 16;
-    if (p.precision == NEGF_PREC_MIXED) bytes += s * mm * (16 + 16 + 8) + s * 7 * (2 * m * m + 4 * m * m) * 2;
-    return bytes + (64LL << 20);
+    const long long b = negf::Engine::estimate_bytes(engine_params(k));
+    return b < 0 ? b : b + (64LL << 20);
   }
 
   // Destroy idle workers (no admitted requests, not running a batch) until `need` bytes
@@ -154,6 +152,14 @@ struct negf_server {
         w = wi->second.get();
       } else {
         const long long need = estimate(r->key);
+        if (need < 0) {   // a geometry no engine accepts (e.g. M > 800 in the mixed form)
+          r->status = NEGF_EINVAL;
+          r->done = true;
+          r->t_done = now();
+          it = pending.erase(it);
+          done_cv.notify_all();
+          continue;
+        }
         if (budget - used < need) {
           const bool ok = evict_idle_locked(need, self);
           it = std::find(pending.begin(), pending.end(), r);   // the lock may have been released

@@ -149,3 +149,32 @@ def test_fortran_shim_params_type_matches_header():
         vals = [int(v) for v in subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()]
     assert vals[:-1] == [o for _, o in fields], list(zip([f for f, _ in fields], vals, [o for _, o in fields]))
     assert vals[-1] == total
+
+
+def test_device_bytes_estimate_needs_no_device():
+    """negf_estimate_device_bytes counts the allocation of negf_create on the host: it grows
+    with the batch by the Npx*M^2*16-byte block store per entry, the mixed form adds its
+    slice planes, and parameters negf_create refuses are refused."""
+    lib = capi.load()
+
+    def est(**kw):
+        p = capi.NegfParams()
+        p.npx, p.npy, p.npz, p.norb = kw.get("npx", 100), kw.get("npy", 10), kw.get("npz", 10), 4
+        p.n_hamiltonians, p.max_batch = kw.get("slots", 4), kw.get("batch", 256)
+        p.eta, p.sr_tol, p.sr_max_iter = 1e-5, 1e-10, 20000
+        p.precision = kw.get("precision", capi.NEGF_PREC_MIXED)
+        v = ctypes.c_int64()
+        rc = lib.negf_estimate_device_bytes(ctypes.byref(p), ctypes.byref(v))
+        return rc, v.value
+
+    rc, b256 = est()
+    assert rc == capi.NEGF_OK
+    m2 = 400 * 400
+    assert b256 > (256 + 4) * 100 * m2 * 16                 # block store + slots
+    rc, b255 = est(batch=255)
+    assert rc == capi.NEGF_OK and b256 - b255 >= 100 * m2 * 16
+    rc, f64 = est(precision=capi.NEGF_PREC_FP64)
+    assert rc == capi.NEGF_OK and f64 < b256
+    assert est(npy=15, npz=14)[0] == capi.NEGF_EINVAL         # M = 840 > 800 in the mixed form
+    assert est(npy=15, npz=14, precision=capi.NEGF_PREC_FP64)[0] == capi.NEGF_OK
+    assert est(batch=0)[0] == capi.NEGF_EINVAL

@@ -90,3 +90,17 @@ def test_server_model_requests_match_uploaded_wires(need_gpu):
             want, rn = _alone(h, x, 6, 3, es, 0.8, 0.1, 1e-3, "mixed")
             assert np.array_equal(got["T12"], want["T12"])
             assert np.array_equal(got["RhoN"], rn)
+
+
+@pytest.mark.parametrize("precision,currents", [("fp64", False), ("mixed", False), ("mixed", True)])
+def test_admission_estimate_equals_the_engine_allocation(need_gpu, precision, currents):
+    """The serving layer admits engines by negf_estimate_device_bytes; it must be the bytes
+    negf_create actually allocates (mixed form: slice planes, Newton-Schulz buffers)."""
+    import ctypes
+    from nonequilibriumgreensfunction_gb300 import capi
+    for (npx, n, batch) in ((12, 6, 8), (5, 14, 3)):
+        with Solver(npx, n, n, max_batch=batch, n_hamiltonians=2, precision=precision,
+                    calc_currents=currents) as s:
+            v = ctypes.c_int64()
+            assert s.lib.negf_estimate_device_bytes(ctypes.byref(s.params), ctypes.byref(v)) == capi.NEGF_OK
+            assert v.value == s.device_bytes(), (npx, n, batch)
