@@ -431,7 +431,7 @@ NEGF_API int negf_zinv(int32_t n, const double* G, double* invG, int32_t batch);
  * Runs on `stream` (cudaStream_t, NULL = default stream), then reads the device error
  * flag and synchronises `stream`: it returns after the product is complete and cannot be
  * captured into a CUDA graph.  The first beta = 0 call of each shape with 2k <= 800 also
- * times the tensor-core kernel variants: it launches the product six times and waits for
+ * times the tensor-core kernel variants: it launches the product nine times and waits for
  * them before returning.                                                               */
 #define NEGF_NOALLOC_MAX_DIM      512
 #define NEGF_NOALLOC_MAX_SLICES   8

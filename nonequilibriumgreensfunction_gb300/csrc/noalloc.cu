@@ -23,7 +23,7 @@
 // Every call ends by copying the device error flag to the host and synchronising
 // `stream`, so it blocks until the product is complete and cannot be recorded into a CUDA
 // graph.  The first beta = 0 call of each shape with K' = 2k <= 800 also runs the kernel
-// variant choice of the tensor-core GEMM: it launches the product six times on `stream`
+// variant choice of the tensor-core GEMM: it launches the product nine times on `stream`
 // and waits for their events before it returns.
 #include <mutex>
 
