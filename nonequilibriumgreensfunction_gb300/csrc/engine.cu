@@ -622,6 +622,16 @@ int Engine::solve_sr_impl(const std::vector<SrJob>& jobs, std::vector<int>& stat
   const long long sM = MM_;
   auto inv_merge = [&](double2* A) -> int { return invert(A, sM, S, dSrStatus_); };
   cur_slices_ = s_sr_;
+  // Each lead's own products run over the contiguous range of problems that want that
+  // lead (batch_solve orders problems left-only, joint, right-only); a problem inside a
+  // range that does not want the lead only computes values nobody reads.
+  int lo[2] = {S, S}, hi[2] = {0, 0};
+  for (int q = 0; q < S; ++q) {
+    if (jobs[q].want_l) { lo[0] = std::min(lo[0], q); hi[0] = q + 1; }
+    if (jobs[q].want_r) { lo[1] = std::min(lo[1], q); hi[1] = q + 1; }
+  }
+  auto at = [&](int r, int lead) { return buf(r) + (long long)lo[lead] * sM; };
+  auto nlead = [&](int lead) { return hi[lead] > lo[lead] ? hi[lead] - lo[lead] : 0; };
 
   // alpha = (E + i eta) I - H_end (:71-74 / :83-86)
   NEGF_TRY(form_alpha(M_, S, dSrE_, dSrHend_, p_.eta, 0.0, buf(SR_ALPHA), sM, st_));
@@ -646,10 +656,14 @@ int Engine::solve_sr_impl(const std::vector<SrJob>& jobs, std::vector<int>& stat
   auto any_active = [&]() { return std::any_of(act.begin(), act.end(), [](int a) { return a != 0; }); };
   while (any_active() && it < p_.sr_max_iter) {
     ++it;
-    // Told_L <- Told_L t~ ; Told_R <- Told_R t  (:157-158, with t <-> t~ for the right lead)
-    NEGF_TRY(gemm(S, OP_N, buf(SR_TOLDL), sM, OP_N, buf(SR_TT), sM, buf(SR_W1), sM, one, zero));
+    // Told_L <- Told_L t~ ; Told_R <- Told_R t  (:157-158, with t <-> t~ for the right lead),
+    // each over its lead's problems; W1 then takes the old Told's role, and the problems
+    // outside the range keep their (unread) values in the swapped buffers
+    if (nlead(0))
+      NEGF_TRY(gemm(nlead(0), OP_N, at(SR_TOLDL, 0), sM, OP_N, at(SR_TT, 0), sM, at(SR_W1, 0), sM, one, zero));
     std::swap(role[SR_TOLDL], role[SR_W1]);
-    NEGF_TRY(gemm(S, OP_N, buf(SR_TOLDR), sM, OP_N, buf(SR_T), sM, buf(SR_W1), sM, one, zero));
+    if (nlead(1))
+      NEGF_TRY(gemm(nlead(1), OP_N, at(SR_TOLDR, 1), sM, OP_N, at(SR_T, 1), sM, at(SR_W1, 1), sM, one, zero));
     std::swap(role[SR_TOLDR], role[SR_W1]);
     // tmp = inv(I - t t~ - t~ t) (:160-163)
     NEGF_TRY(set_identity(M_, S, buf(SR_TMP), sM, st_));
@@ -661,11 +675,17 @@ int Engine::solve_sr_impl(const std::vector<SrJob>& jobs, std::vector<int>& stat
     NEGF_TRY(gemm(S, OP_N, buf(SR_W1), sM, OP_N, buf(SR_T), sM, buf(SR_TN), sM, one, zero));
     NEGF_TRY(gemm(S, OP_N, buf(SR_TMP), sM, OP_N, buf(SR_TT), sM, buf(SR_W1), sM, one, zero));
     NEGF_TRY(gemm(S, OP_N, buf(SR_W1), sM, OP_N, buf(SR_TT), sM, buf(SR_TTN), sM, one, zero));
-    // change = Told t ; T += change (:178-180)
-    NEGF_TRY(gemm(S, OP_N, buf(SR_TOLDL), sM, OP_N, buf(SR_TN), sM, buf(SR_CHG), sM, one, zero));
-    NEGF_TRY(sr_accumulate(M_, S, dSrActive_, buf(SR_CHG), sM, buf(SR_TL), sM, dSrCmax_, st_));
-    NEGF_TRY(gemm(S, OP_N, buf(SR_TOLDR), sM, OP_N, buf(SR_TTN), sM, buf(SR_CHG), sM, one, zero));
-    NEGF_TRY(sr_accumulate(M_, S, dSrActive_ + S, buf(SR_CHG), sM, buf(SR_TR), sM, dSrCmax_ + S, st_));
+    // change = Told t ; T += change (:178-180), each over its lead's problems
+    if (nlead(0)) {
+      NEGF_TRY(gemm(nlead(0), OP_N, at(SR_TOLDL, 0), sM, OP_N, at(SR_TN, 0), sM, at(SR_CHG, 0), sM, one, zero));
+      NEGF_TRY(sr_accumulate(M_, nlead(0), dSrActive_ + lo[0], at(SR_CHG, 0), sM, at(SR_TL, 0), sM,
+                             dSrCmax_ + lo[0], st_));
+    }
+    if (nlead(1)) {
+      NEGF_TRY(gemm(nlead(1), OP_N, at(SR_TOLDR, 1), sM, OP_N, at(SR_TTN, 1), sM, at(SR_CHG, 1), sM, one, zero));
+      NEGF_TRY(sr_accumulate(M_, nlead(1), dSrActive_ + S + lo[1], at(SR_CHG, 1), sM, at(SR_TR, 1), sM,
+                             dSrCmax_ + S + lo[1], st_));
+    }
     std::swap(role[SR_T], role[SR_TN]);
     std::swap(role[SR_TT], role[SR_TTN]);
     NEGF_CUDA_TRY(cudaMemcpyAsync(hPin_, dSrCmax_, sizeof(double) * 2 * S, cudaMemcpyDeviceToHost, st_));
@@ -687,26 +707,30 @@ int Engine::solve_sr_impl(const std::vector<SrJob>& jobs, std::vector<int>& stat
   for (int q = 0; q < 2 * S; ++q)
     if (act[q]) { iters[q] = it; if (status[q % S] == 0) status[q % S] = NEGF_ESR_NOCONV; }
 
-  // g = inv(alpha + beta T), Sigma = beta g beta^H (:195-209) for each lead
+  // g = inv(alpha + beta T), Sigma = beta g beta^H (:195-209) for each lead, over the
+  // problems that want it
   for (int lead = 0; lead < 2; ++lead) {
-    double2* T = buf(lead == 0 ? SR_TL : SR_TR);
-    double2* W = buf(SR_TMP);
+    const int n = nlead(lead), a = lo[lead];
+    if (n == 0) continue;
+    const long long off = (long long)a * sM;
+    double2* T = buf(lead == 0 ? SR_TL : SR_TR) + off;
+    double2* W = buf(SR_TMP) + off;
     if (hop_bd_) {
-      NEGF_TRY(sr_form_final(hop(), M_, S, lead, buf(SR_ALPHA), sM, T, sM, W, sM, st_));
+      NEGF_TRY(sr_form_final(hop(), M_, n, lead, buf(SR_ALPHA) + off, sM, T, sM, W, sM, st_));
     } else {
-      NEGF_TRY(copy_blocks(M_, S, buf(SR_ALPHA), sM, W, sM, st_));
-      NEGF_TRY(gemm(S, lead == 0 ? OP_C : OP_N, dHop_, 0, OP_N, T, sM, W, sM, mone, one));
+      NEGF_TRY(copy_blocks(M_, n, buf(SR_ALPHA) + off, sM, W, sM, st_));
+      NEGF_TRY(gemm(n, lead == 0 ? OP_C : OP_N, dHop_, 0, OP_N, T, sM, W, sM, mone, one));
     }
-    NEGF_TRY(inv_merge(W));
-    double2* sig = lead == 0 ? dSrSigL_ : dSrSigR_;
-    double2* gam = lead == 0 ? dSrGamL_ : dSrGamR_;
+    NEGF_TRY(invert(W, sM, n, dSrStatus_ + a));
+    double2* sig = (lead == 0 ? dSrSigL_ : dSrSigR_) + off;
+    double2* gam = (lead == 0 ? dSrGamL_ : dSrGamR_) + off;
     if (hop_bd_) {
-      NEGF_TRY(sr_sigma(hop(), M_, S, lead, W, sM, sig, sM, gam, sM, dSrDos_ + lead * S, st_));
+      NEGF_TRY(sr_sigma(hop(), M_, n, lead, W, sM, sig, sM, gam, sM, dSrDos_ + lead * S + a, st_));
     } else {
       // lead 0: H^H g H ; lead 1: H g H^H
-      NEGF_TRY(gemm(S, lead == 0 ? OP_C : OP_N, dHop_, 0, OP_N, W, sM, buf(SR_W1), sM, one, zero));
-      NEGF_TRY(gemm(S, OP_N, buf(SR_W1), sM, lead == 0 ? OP_N : OP_C, dHop_, 0, sig, sM, one, zero));
-      NEGF_TRY(sr_sigma(HopBD{}, M_, S, -1, nullptr, 0, sig, sM, gam, sM, dSrDos_ + lead * S, st_));
+      NEGF_TRY(gemm(n, lead == 0 ? OP_C : OP_N, dHop_, 0, OP_N, W, sM, buf(SR_W1) + off, sM, one, zero));
+      NEGF_TRY(gemm(n, OP_N, buf(SR_W1) + off, sM, lead == 0 ? OP_N : OP_C, dHop_, 0, sig, sM, one, zero));
+      NEGF_TRY(sr_sigma(HopBD{}, M_, n, -1, nullptr, 0, sig, sM, gam, sM, dSrDos_ + lead * S + a, st_));
     }
   }
   std::vector<int> st(S);
@@ -1013,10 +1037,13 @@ int Engine::batch_solve(const negf_request* req, int n, negf_result* res, double
   NEGF_CUDA_TRY(cudaMemsetAsync(dAcc_, 0, sizeof(double) * nslots * nf_ * total, st_));
   for (int c0 = 0; c0 < n; c0 += B_) {
     const int nb = std::min(B_, n - c0);
-    // Sancho-Rubio problems: one per (energy, lead class), two if H_1 != H_N
-    std::vector<SrJob> jobs;
-    std::map<std::pair<double, int>, std::pair<int, int>> key2job;
+    // Sancho-Rubio problems: one per (energy, lead class) when H_1 == H_N, otherwise a
+    // left-only and a right-only one.  They are ordered left-only, joint, right-only, so
+    // the problems that need each lead's products form one contiguous range.
+    std::vector<SrJob> jl_only, joint, jr_only;
+    std::map<std::pair<double, int>, std::pair<int, int>> key2job;   // (list, index) codes
     std::vector<Item> items(nb);
+    std::vector<std::pair<int, int>> item_jobs(nb);
     for (int i = 0; i < nb; ++i) {
       const negf_request& r = req[c0 + i];
       // model contacts do not depend on the Hamiltonian: one problem per energy
@@ -1024,23 +1051,34 @@ int Engine::batch_solve(const negf_request* req, int n, negf_result* res, double
       const int rep = model ? 0 : slot_rep_[r.slot];
       auto key = std::make_pair(r.energy, rep);
       auto itk = key2job.find(key);
-      std::pair<int, int> jl;
+      std::pair<int, int> code;   // list * 2^20 + index, for the left and the right lead
       if (itk == key2job.end()) {
         if (model || slot_joint_[rep]) {
-          jobs.push_back(SrJob{r.energy, rep, 0, 1, 1});
-          jl = {(int)jobs.size() - 1, (int)jobs.size() - 1};
+          joint.push_back(SrJob{r.energy, rep, 0, 1, 1});
+          const int c = (1 << 20) + (int)joint.size() - 1;
+          code = {c, c};
         } else {
-          jobs.push_back(SrJob{r.energy, rep, 0, 1, 0});
-          jobs.push_back(SrJob{r.energy, rep, 1, 0, 1});
-          jl = {(int)jobs.size() - 2, (int)jobs.size() - 1};
+          jl_only.push_back(SrJob{r.energy, rep, 0, 1, 0});
+          jr_only.push_back(SrJob{r.energy, rep, 1, 0, 1});
+          code = {(int)jl_only.size() - 1, (2 << 20) + (int)jr_only.size() - 1};
         }
-        key2job[key] = jl;
+        key2job[key] = code;
       } else {
-        jl = itk->second;
+        code = itk->second;
       }
+      item_jobs[i] = code;
+    }
+    std::vector<SrJob> jobs(jl_only);
+    jobs.insert(jobs.end(), joint.begin(), joint.end());
+    jobs.insert(jobs.end(), jr_only.begin(), jr_only.end());
+    const int base[3] = {0, (int)jl_only.size(), (int)(jl_only.size() + joint.size())};
+    for (int i = 0; i < nb; ++i) {
+      const negf_request& r = req[c0 + i];
       Item& it = items[i];
       it.energy = r.energy; it.f1 = r.f1; it.f2 = r.f2; it.dE = r.dE; it.slot = r.slot;
-      it.sr_l = jl.first; it.sr_r = jl.second; it.pad = 0;
+      it.sr_l = base[item_jobs[i].first >> 20] + (item_jobs[i].first & ((1 << 20) - 1));
+      it.sr_r = base[item_jobs[i].second >> 20] + (item_jobs[i].second & ((1 << 20) - 1));
+      it.pad = 0;
     }
     std::vector<int> sr_status, sr_iters;
     NEGF_TRY(solve_sr(jobs, sr_status, sr_iters));

@@ -189,6 +189,39 @@ def test_dense_hopx_and_asymmetric_leads(need_gpu):
     assert_close(rn[..., 0], want, "RhoN")
 
 
+@pytest.mark.parametrize("precision,rtol", [("fp64", RTOL), ("mixed", 1e-6)])
+def test_joint_and_one_sided_decimations_in_one_batch(need_gpu, precision, rtol):
+    """Two slots in one batch: slot 0 has equal end slices (one decimation serves both
+    leads), slot 1 a right end slice shifted by a potential (a left-only and a right-only
+    decimation).  The problems are ordered left-only, joint, right-only, and each lead's
+    products run over its own range; every request must match the oracle."""
+    npx, npy, npz = 6, 3, 3
+    h0, hopx = HB.ti_wire(npx, npy, npz, W=0.1, seed=7, flux=0.4, zeeman=0.01)
+    h1, _ = HB.ti_wire(npx, npy, npz, W=0.1, seed=8, flux=0.4, zeeman=0.01)
+    h1 = h1.copy()
+    h1[-1] = h1[-1] + 0.02 * np.eye(h1.shape[1])
+    opt = O.SolveOptions(eta=1e-5, sr_tol=1e-10, kT=0.025)
+    mu = (0.005, -0.005)
+    es = np.array([-0.22, -0.05, 0.011, 0.17])
+    e_all = np.concatenate([es, es])
+    slots = np.repeat([1, 0], es.size)            # the one-sided slot first in the batch
+    f1 = [O.fermi(x, mu[0], opt.kT) for x in e_all]
+    f2 = [O.fermi(x, mu[1], opt.kT) for x in e_all]
+    with Solver(npx, npy, npz, n_hamiltonians=2, eta=opt.eta, sr_tol=opt.sr_tol, max_batch=e_all.size,
+                precision=precision) as s:
+        s.set_hamiltonian(h0, hopx, slot=0)
+        s.set_hamiltonian(h1, hopx, slot=1)
+        r = s.solve_batch(e_all, f1, f2, 1e-3, slots=slots)
+    assert (r["status"] == 0).all()
+    for i, (e, sl) in enumerate(zip(e_all, slots)):
+        ref = O.energy_sweep(h1 if sl else h0, hopx, float(e), mu, 1e-3, npy, npz, opt)
+        for k in ("T12", "Modec1", "Modec2"):
+            assert_close(r[k][i], ref[k], "%s[%d]" % (k, i), rtol=rtol, floor=1e-3)
+        assert_close([r["DOSc1"][i], r["DOSc2"][i]], ref["dosc"], "dosc[%d]" % i, rtol=rtol)
+        if precision == "fp64":
+            assert r["sr_iters"][i] == max(ref["sr_iters"])
+
+
 @pytest.mark.parametrize("precision,rtol,rho_rtol", [("fp64", RTOL, RTOL), ("mixed", 1e-6, 5e-6)])
 def test_uniform_hop_block_with_general_entries(need_gpu, precision, rtol, rho_rtol):
     """Every site shares one HopX block whose nonzeros are general complex numbers, with
