@@ -65,6 +65,11 @@ struct Worker {
   long long bytes = 0;
   bool busy = false;
   bool quit = false;
+  // true only while the worker's thread is blocked in its wait on work_cv: the one state in
+  // which another thread may evict it (its thread runs none of the worker's code then, and
+  // wakes on `quit`).  A worker that has just finished a batch may release the server lock
+  // inside admit_locked; it must not be evicted from under itself there.
+  bool waiting = false;
 };
 
 size_t hash_bytes(const void* p, size_t n) {
@@ -116,7 +121,7 @@ struct negf_server {
     long long freed = 0;
     for (auto it = workers.begin(); it != workers.end() && budget - used + freed < need;) {
       Worker* w = it->second.get();
-      const bool idle = w != self && !w->busy && w->active.empty() &&
+      const bool idle = w != self && w->waiting && !w->busy && w->active.empty() &&
                         std::all_of(w->slot_owner.begin(), w->slot_owner.end(), [](Request* r) { return r == nullptr; });
       if (idle) {
         w->quit = true;
@@ -152,8 +157,10 @@ struct negf_server {
         w = wi->second.get();
       } else {
         const long long need = estimate(r->key);
-        if (need < 0) {   // a geometry no engine accepts (e.g. M > 800 in the mixed form)
-          r->status = NEGF_EINVAL;
+        if (need < 0 || need > budget) {
+          // a geometry no engine accepts (e.g. M > 800 in the mixed form), or one whose
+          // engine alone exceeds the whole budget: it would never be admitted
+          r->status = need < 0 ? NEGF_EINVAL : NEGF_EADMIT;
           r->done = true;
           r->t_done = now();
           it = pending.erase(it);
@@ -208,12 +215,14 @@ struct negf_server {
     std::vector<double> items((size_t)nf * total * (size_t)p.max_batch);
     std::unique_lock<std::mutex> lk(mu);
     for (;;) {
+      w->waiting = true;
       work_cv.wait(lk, [&] {
         if (w->quit) return true;
         for (Request* r : w->active)
           if (!r->uploaded || r->next < (int)r->e.size()) return true;
         return false;
       });
+      w->waiting = false;
       if (w->quit) return;
       w->busy = true;
       // uploads of newly admitted requests
@@ -295,9 +304,9 @@ struct negf_server {
       done_cv.notify_all();
       const bool idle = w->active.empty() &&
                         std::all_of(w->slot_owner.begin(), w->slot_owner.end(), [](Request* r) { return r == nullptr; });
-      if (idle && !pending.empty()) {
+      auto it = workers.find(w->key);
+      if (idle && !pending.empty() && it != workers.end() && it->second.get() == w) {
         // requests of other geometries wait for memory: release this idle engine and exit
-        auto it = workers.find(w->key);
         std::unique_ptr<Worker> self = std::move(it->second);
         workers.erase(it);
         const long long freed = self->bytes;

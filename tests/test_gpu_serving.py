@@ -104,3 +104,49 @@ def test_admission_estimate_equals_the_engine_allocation(need_gpu, precision, cu
             v = ctypes.c_int64()
             assert s.lib.negf_estimate_device_bytes(ctypes.byref(s.params), ctypes.byref(v)) == capi.NEGF_OK
             assert v.value == s.device_bytes(), (npx, n, batch)
+
+
+def test_eviction_churn_with_many_geometries(need_gpu):
+    """The serving configuration's regime: many geometries and an HBM budget that holds
+    about two engines, so workers are evicted and re-created continually while others run
+    (a worker that has just finished a batch, and may release the server lock while it
+    admits, is never evicted from under itself).  Every request finishes with the results
+    it has alone."""
+    import ctypes
+    from nonequilibriumgreensfunction_gb300 import capi
+    geoms = [(2, 5), (3, 5), (2, 6), (3, 6), (2, 7), (3, 7)]      # (cross-section, npx)
+    with Solver(7, 3, 3, max_batch=3, n_hamiltonians=1, precision="mixed") as s:
+        v = ctypes.c_int64()
+        assert s.lib.negf_estimate_device_bytes(ctypes.byref(s.params), ctypes.byref(v)) == capi.NEGF_OK
+        big = v.value
+    rng = np.random.default_rng(9)
+    reqs = []
+    # admission asks for an engine's bytes plus 64 MB: this budget holds two engines
+    with Server(precision="mixed", max_batch=3, slots_per_geometry=1,
+                hbm_budget_bytes=int(2.3 * big) + (64 << 20)) as srv:
+        for i in range(30):
+            n, npx = geoms[int(rng.integers(len(geoms)))]
+            h, x = _wire(n, npx, 200 + i)
+            es = np.sort(rng.uniform(-0.25, 0.25, size=int(rng.integers(2, 7))))
+            reqs.append((srv.submit(h, x, es, 0.7, 0.2, 1e-3), h, x, n, npx, es))
+        for rid, h, x, n, npx, es in reqs:
+            srv.wait(rid, timeout=600)
+            got = srv.result(rid)
+            assert got["status"] == 0
+            want, _ = _alone(h, x, npx, n, es, 0.7, 0.2, 1e-3, "mixed")
+            assert np.array_equal(got["T12"], want["T12"])
+
+
+def test_request_larger_than_the_budget_fails_at_once(need_gpu):
+    """A request whose engine alone exceeds the server's HBM budget can never be admitted:
+    it finishes at once with NEGF_EADMIT instead of waiting, and the server keeps serving."""
+    from nonequilibriumgreensfunction_gb300 import capi
+    with Server(precision="fp64", max_batch=2, slots_per_geometry=1, hbm_budget_bytes=80 << 20) as srv:
+        hb, xb = _wire(8, 20, 1)                        # M = 256, Npx = 20: an engine of ~150 MB
+        big = srv.submit(hb, xb, [0.01], 1.0, 0.0, 1e-3)
+        h, x = _wire(2, 5, 2)
+        small = srv.submit(h, x, [0.02, 0.1], 1.0, 0.0, 1e-3)
+        srv.wait(big, timeout=60)
+        assert srv.result(big)["status"] == capi.NEGF_EADMIT
+        srv.wait(small, timeout=300)
+        assert srv.result(small)["status"] == 0
