@@ -320,7 +320,8 @@ typedef struct negf_batch_outputs {
 NEGF_API int negf_solve_batch_ex(negf_handle* h, const negf_request* req, int32_t n, negf_result* res,
                                  const negf_batch_outputs* out);
 /* ---- serving ----------------------------------------------------------------------
- * A device-resident request loop in place of the MPI energy sweep: wires of different
+ * A request server in place of the MPI energy sweep, with every request's state (its
+ * Hamiltonian, block store and results) kept on the device: wires of different
  * cross-sections arrive as requests (Hamiltonian + a list of energy points with their
  * occupations), are admitted while the HBM budget has room for their geometry's block
  * store (Npx*M^2*16 bytes per in-flight energy point) and a free Hamiltonian slot, and

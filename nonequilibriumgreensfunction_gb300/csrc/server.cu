@@ -1,4 +1,5 @@
-// Device-resident request server (negf_server_*): replaces the MPI master/worker energy
+// Request server (negf_server_*), with each request's state kept on the device (host
+// worker threads drive the batches): replaces the MPI master/worker energy
 // sweep of Source/NEGF_Main.F90:21-27 with continuous batching on one GPU.
 //
 // Requests (a wire's Htotd/HopX and a list of energy points) are queued by submit().

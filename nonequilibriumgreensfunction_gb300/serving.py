@@ -1,5 +1,6 @@
-"""Python side of the device-resident request server (negf_server_* in include/negf.h),
-and the Poisson-arrival load generator used to measure serving latency.
+"""Python side of the request server (negf_server_* in include/negf.h), whose requests keep
+their state on the device, and the Poisson-arrival load generator used to measure serving
+latency.
 
 The server replaces the MPI master/worker energy sweep (Source/NEGF_Main.F90:21-27):
 wires of different cross-sections arrive as requests, are admitted by their HBM
