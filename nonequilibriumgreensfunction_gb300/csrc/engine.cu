@@ -31,6 +31,7 @@
 #include <cmath>
 #include <complex>
 #include <cstddef>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <utility>
@@ -547,6 +548,10 @@ int Engine::invert_impl(double2* A, long long sA, int batch, int* status_dev) {
 // the engine's stream).
 int Engine::invert_f32(int batch) {
   if (!cinv_f32_fused_ok(M_, batch)) return cinv_f32(dW32_, MM_, M_, batch, inv_, st_, 0);
+  // NEGF_GJ_FORM = 0 or 1 runs that form instead of the timed choice (to compare or profile
+  // the forms; both give bitwise the same inverse)
+  if (const char* ev = std::getenv("NEGF_GJ_FORM"))
+    if (ev[0] == '0' || ev[0] == '1') return cinv_f32(dW32_, MM_, M_, batch, inv_, st_, ev[0] - '0');
   int bb = 1;
   while (bb < batch) bb <<= 1;
   auto it = gj_form_.find(bb);
