@@ -263,6 +263,7 @@ def serving_bench(seconds, device, form="mixed", mix="reduced", e_scale=1.0, bur
         mean_e = float(np.mean([r["energies"].size for r in burst]))
         rate = 0.8 * capacity / mean_e
         lat, solves, wall = run_poisson_load(srv, mk, rate, seconds, rng)
+        churn = srv.stats()
     if mix == "c4":
         load = ("Poisson arrivals at 0.8 x measured capacity; Npy=Npz in {6,8,10,12,14} (M up to 784), "
                 "Npx ~ U[50,200], %g-%g energies/request (log-uniform; the configuration's 64-1024 x %g), "
@@ -276,7 +277,7 @@ def serving_bench(seconds, device, form="mixed", mix="reduced", e_scale=1.0, bur
             "p90_s": float(np.percentile(lat, 90)), "mean_s": float(np.mean(lat)),
             "solves_per_s": solves / wall, "capacity_solves_per_s": capacity, "arrival_rate_req_per_s": rate,
             "requests": int(lat.size), "seconds": seconds, "wall_s": wall, "form": form, "mix": mix,
-            "load": load}
+            "engines": churn, "load": load}
 
 
 def run_serving_bench(args):

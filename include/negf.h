@@ -379,6 +379,16 @@ NEGF_API int negf_server_poll(negf_server* s, int64_t id, negf_wire_status* st, 
 /* block until request `id` is done or timeout_s elapses (NEGF_ETIMEDOUT)               */
 NEGF_API int negf_server_wait(negf_server* s, int64_t id, double timeout_s);
 NEGF_API double negf_server_clock(const negf_server* s);
+/* Engine churn of the server (no reference counterpart): each geometry's engine is
+ * created on its first admitted request and released when memory is needed elsewhere. */
+typedef struct negf_server_stats {
+    int64_t engines_created, engines_released, engines_live;
+    double  create_s;         /* host seconds spent creating engines (device allocation)   */
+    double  release_s;        /* host seconds spent releasing them (device frees)          */
+    int64_t bytes_used, bytes_budget;
+    int64_t reserved[4];
+} negf_server_stats;
+NEGF_API int negf_server_get_stats(negf_server* s, negf_server_stats* out);
 NEGF_API int negf_server_destroy(negf_server* s);
 
 /* ---- self-consistent bias point: Poisson ---------------------------------------------

@@ -39,7 +39,7 @@ EXPORTED_SYMBOLS = (
     "negf_calculate_currents", "negf_calculate_resolved", "negf_solve_batch", "negf_solve_batch_ex",
     "negf_zgemm", "negf_zinv", "negf_zgemm_noalloc", "negf_poisson_solve",
     "negf_server_create", "negf_server_submit", "negf_server_poll", "negf_server_wait",
-    "negf_server_clock", "negf_server_destroy",
+    "negf_server_clock", "negf_server_get_stats", "negf_server_destroy",
 )
 
 
@@ -136,6 +136,12 @@ class NegfWireStatus(ctypes.Structure):
                 ("t_submit", c_double), ("t_admit", c_double), ("t_done", c_double)]
 
 
+class NegfServerStats(ctypes.Structure):
+    _fields_ = [("engines_created", c_int64), ("engines_released", c_int64), ("engines_live", c_int64),
+                ("create_s", c_double), ("release_s", c_double), ("bytes_used", c_int64), ("bytes_budget", c_int64),
+                ("reserved", c_int64 * 4)]
+
+
 class NegfError(RuntimeError):
     def __init__(self, code: int, where: str):
         self.code = code
@@ -180,6 +186,7 @@ def _declare(lib):
         "negf_server_poll": (c_int, [h, c_int64, POINTER(NegfWireStatus), _dp, _dp, c_int32]),
         "negf_server_wait": (c_int, [h, c_int64, c_double]),
         "negf_server_clock": (c_double, [h]),
+        "negf_server_get_stats": (c_int, [h, POINTER(NegfServerStats)]),
         "negf_server_destroy": (c_int, [h]),
         "negf_solve_batch": (c_int, [h, POINTER(NegfRequest), c_int32, POINTER(NegfResult),
                                      _dp, _dp, _dp, _dp, _dp]),

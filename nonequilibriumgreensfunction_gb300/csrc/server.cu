@@ -92,6 +92,10 @@ struct negf_server {
   std::map<GeomKey, std::unique_ptr<Worker>> workers;
   int64_t next_id = 1;
   long long budget = 0, used = 0;
+  // engine churn: engines created and released, and the host seconds spent in their
+  // allocation (negf_create's work) and release (their device frees)
+  long long n_created = 0, n_released = 0;
+  double t_create = 0.0, t_release = 0.0;
   Clock::time_point t0 = Clock::now();
 
   double now() const { return std::chrono::duration<double>(Clock::now() - t0).count(); }
@@ -136,12 +140,17 @@ struct negf_server {
     if (!dead.empty()) {
       work_cv.notify_all();
       mu.unlock();
+      double t_rel = 0.0;
       for (auto& w : dead) {
         if (w->th.joinable()) w->th.join();
+        const double t0 = now();
         w.reset();   // frees the engine's device memory
+        t_rel += now() - t0;
       }
       mu.lock();
       used -= freed;
+      n_released += (long long)dead.size();
+      t_release += t_rel;
     }
     return budget - used >= need;
   }
@@ -181,7 +190,10 @@ struct negf_server {
           auto nw = std::make_unique<Worker>();
           nw->key = r->key;
           nw->eng = std::make_unique<negf::Engine>();
-          if (nw->eng->init(engine_params(r->key)) != NEGF_OK) {
+          const double t0 = now();
+          const int irc = nw->eng->init(engine_params(r->key));
+          t_create += now() - t0;
+          if (irc != NEGF_OK) {
             r->status = NEGF_ENOMEM;
             r->done = true;
             r->t_done = now();
@@ -191,6 +203,7 @@ struct negf_server {
           }
           nw->bytes = nw->eng->bytes();
           used += nw->bytes;
+          ++n_created;
           nw->slot_owner.assign(p.slots_per_geometry, nullptr);
           w = nw.get();
           workers[r->key] = std::move(nw);
@@ -312,9 +325,13 @@ struct negf_server {
         workers.erase(it);
         const long long freed = self->bytes;
         lk.unlock();
+        const double t0 = now();
         self->eng.reset();
+        const double t_rel = now() - t0;
         lk.lock();
         used -= freed;
+        ++n_released;
+        t_release += t_rel;
         admit_locked(nullptr);
         done_cv.notify_all();
         self->th.detach();
@@ -422,6 +439,20 @@ int negf_server_wait(negf_server* s, int64_t id, double timeout_s) {
 }
 
 double negf_server_clock(const negf_server* s) { return s ? s->now() : 0.0; }
+
+int negf_server_get_stats(negf_server* s, negf_server_stats* out) {
+  if (!s || !out) return NEGF_EINVAL;
+  std::lock_guard<std::mutex> g(s->mu);
+  std::memset(out, 0, sizeof(*out));
+  out->engines_created = s->n_created;
+  out->engines_released = s->n_released;
+  out->create_s = s->t_create;
+  out->release_s = s->t_release;
+  out->engines_live = (int64_t)s->workers.size();
+  out->bytes_used = s->used;
+  out->bytes_budget = s->budget;
+  return NEGF_OK;
+}
 
 int negf_server_destroy(negf_server* s) {
   if (!s) return NEGF_EINVAL;

@@ -97,6 +97,13 @@ class Server:
     def set_geometry_hint(self, npy):
         self._infer_npy = lambda nsite, npy=npy: npy
 
+    def stats(self):
+        """Engine churn: engines created / released / live, host seconds spent creating and
+        releasing them, and the bytes in use against the budget."""
+        st = capi.NegfServerStats()
+        check(self.lib.negf_server_get_stats(self._h, ctypes.byref(st)), "negf_server_get_stats")
+        return {k: getattr(st, k) for k, _ in capi.NegfServerStats._fields_ if k != "reserved"}
+
     def status(self, rid):
         st = NegfWireStatus()
         check(self.lib.negf_server_poll(self._h, rid, ctypes.byref(st), None, None, 0), "negf_server_poll")

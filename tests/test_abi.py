@@ -70,6 +70,7 @@ def test_field_offsets_match_header():
         "negf_stats": capi.NegfStats, "negf_result": capi.NegfResult, "negf_request": capi.NegfRequest,
         "negf_wire_model": capi.NegfWireModel, "negf_serve_params": capi.NegfServeParams,
         "negf_wire_request": capi.NegfWireRequest, "negf_wire_status": capi.NegfWireStatus,
+        "negf_server_stats": capi.NegfServerStats,
     }
     lines = []
     for cname, cls in structs.items():

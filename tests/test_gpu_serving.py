@@ -135,6 +135,11 @@ def test_eviction_churn_with_many_geometries(need_gpu):
             assert got["status"] == 0
             want, _ = _alone(h, x, npx, n, es, 0.7, 0.2, 1e-3, "mixed")
             assert np.array_equal(got["T12"], want["T12"])
+        st = srv.stats()
+    # the budget forced engines to be released and created again
+    assert st["engines_created"] > len(geoms) // 2 and st["engines_released"] >= 1
+    assert st["engines_created"] - st["engines_released"] == st["engines_live"]
+    assert st["bytes_used"] <= st["bytes_budget"]
 
 
 def test_request_larger_than_the_budget_fails_at_once(need_gpu):
