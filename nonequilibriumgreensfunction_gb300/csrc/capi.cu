@@ -111,7 +111,12 @@ int negf_create(const negf_params* p, negf_handle** out) {
 }
 
 int negf_destroy(negf_handle* h) {
+  if (!h) return NEGF_OK;
+  const bool inited = h->eng.own_st_ != nullptr;
+  const int dev = h->eng.p_.device;
   delete h;
+  // the engine's blocks went back to the library's pool: return them to the device
+  if (inited) negf::pool_trim(dev);
   return NEGF_OK;
 }
 

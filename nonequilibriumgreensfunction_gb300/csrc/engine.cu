@@ -34,6 +34,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <utility>
 
 namespace negf {
@@ -48,18 +49,72 @@ __global__ void merge_info_k(int batch, const int* info, int* status) {
   if (b < batch && status[b] == 0 && info[b] != 0) status[b] = info[b];
 }
 
-// device allocation of `count` T, added to `bytes`; with `dry` only the bytes are counted
+// Engines allocate from a library-private stream-ordered memory pool per device, with an
+// unlimited release threshold: a freed engine's blocks stay in the pool and the next
+// engine takes them without a new device allocation, and freeing (cudaFreeAsync) does not
+// synchronise the device the way cudaFree does -- the serving layer creates and releases
+// engines while other engines run.  negf_destroy trims the pool, so a plain handle returns
+// its memory to the device.
+std::mutex g_pool_mu;
+cudaMemPool_t g_pool[64] = {};
+
+int pool_for(int device, cudaMemPool_t* out) {
+  if (device < 0 || device >= 64) return NEGF_EINVAL;
+  std::lock_guard<std::mutex> g(g_pool_mu);
+  if (!g_pool[device]) {
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = device;
+    NEGF_CUDA_TRY(cudaMemPoolCreate(&g_pool[device], &props));
+    uint64_t keep = ~0ULL;
+    NEGF_CUDA_TRY(cudaMemPoolSetAttribute(g_pool[device], cudaMemPoolAttrReleaseThreshold, &keep));
+  }
+  *out = g_pool[device];
+  return NEGF_OK;
+}
+
+// Pinned host staging buffers are kept for reuse as well (cudaFreeHost synchronises the
+// device); a buffer of at least the requested size is taken from the free list.
+std::mutex g_pin_mu;
+std::multimap<size_t, void*> g_pin_free;
+int pinned_take(size_t bytes, double** out, size_t* got) {
+  {
+    std::lock_guard<std::mutex> g(g_pin_mu);
+    auto it = g_pin_free.lower_bound(bytes);
+    if (it != g_pin_free.end()) {
+      *out = static_cast<double*>(it->second);
+      *got = it->first;
+      g_pin_free.erase(it);
+      return NEGF_OK;
+    }
+  }
+  NEGF_CUDA_TRY(cudaMallocHost((void**)out, bytes));
+  *got = bytes;
+  return NEGF_OK;
+}
+void pinned_give(double* p, size_t bytes) {
+  if (!p) return;
+  std::lock_guard<std::mutex> g(g_pin_mu);
+  g_pin_free.insert({bytes, p});
+}
+
+// device allocation of `count` T on stream `st` from `pool`, added to `bytes`; with `dry`
+// only the bytes are counted
 template <typename T>
-int dalloc(T** p, size_t count, long long& bytes, bool dry = false) {
+int dalloc(T** p, size_t count, long long& bytes, bool dry, cudaMemPool_t pool, cudaStream_t st) {
   if (dry) { *p = nullptr; bytes += (long long)(sizeof(T) * count); return NEGF_OK; }
   if (count == 0) { *p = nullptr; return NEGF_OK; }
-  if (cudaMalloc((void**)p, sizeof(T) * count) != cudaSuccess) { *p = nullptr; return NEGF_ENOMEM; }
+  if (cudaMallocFromPoolAsync((void**)p, sizeof(T) * count, pool, st) != cudaSuccess) {
+    *p = nullptr;
+    return NEGF_ENOMEM;
+  }
   bytes += (long long)(sizeof(T) * count);
   return NEGF_OK;
 }
 template <typename T>
-void dfree(T*& p) {
-  if (p) cudaFree((void*)p);
+void dfree(T*& p, cudaStream_t st) {
+  if (p) cudaFreeAsync((void*)p, st);
   p = nullptr;
 }
 
@@ -81,23 +136,38 @@ int merge_info_kernel_launch(int batch, const int* info, int* status, cudaStream
 }
 
 Engine::~Engine() {
-  if (p_.npx > 0) cudaSetDevice(p_.device);
-  dfree(dH_); dfree(dHop_); dfree(dHopBD_); dfree(dSpin_); dfree(dHtab_); dfree(dVext_);
-  dfree(dG_); dfree(dC1_); dfree(dCN_); dfree(dZ_); dfree(dY_); dfree(dQ_);
-  dfree(dSigL_); dfree(dSigR_); dfree(dGamL_); dfree(dGamR_);
-  dfree(dP1_); dfree(dP2_); dfree(dCol1_); dfree(dColN_);
-  dfree(dPx1_); dfree(dPy1_); dfree(dPz1_); dfree(dPx2_); dfree(dPy2_); dfree(dPz2_);
-  if (currents_) { dfree(dYalt_); dfree(dCNalt_); }
-  dfree(dEr_); dfree(dOrAcc_); dfree(dContactCoef_); dfree(dG11_); dfree(dTrJ_);
-  dfree(dSite_); dfree(dSums_); dfree(dTr_); dfree(dAcc_); dfree(dStatus_); dfree(dItems_);
-  dfree(dSr_); dfree(dSrSigL_); dfree(dSrSigR_); dfree(dSrGamL_); dfree(dSrGamR_);
-  dfree(dSrCmax_); dfree(dSrDos_); dfree(dSrActive_); dfree(dSrE_); dfree(dSrHend_); dfree(dSrStatus_);
-  inv_work_free(inv_);
-  dfree(dWinv_); dfree(dW32_); dfree(dT_); dfree(sa_.data); dfree(sb_.data); dfree(sa_.exps); dfree(sb_.exps);
-  dfree(sw_.data); dfree(sw_.exps); dfree(sgl_.data); dfree(sgl_.exps); dfree(sgr_.data); dfree(sgr_.exps);
-  dfree(dRnorm_); dfree(dNsIdx_); dfree(dNsX_); dfree(dNsW_); dfree(dTcErr_);
-  if (hPin_) cudaFreeHost(hPin_);
-  if (own_st_) cudaStreamDestroy(own_st_);
+  if (!own_st_) return;   // never initialised (or only sized by estimate_bytes)
+  cudaSetDevice(p_.device);
+  // nothing of this engine may still run when its blocks go back to the pool
+  if (st_ && st_ != own_st_) cudaStreamSynchronize(st_);
+  cudaStreamSynchronize(own_st_);
+  cudaStream_t s = own_st_;
+  dfree(dH_, s); dfree(dHop_, s); dfree(dHopBD_, s); dfree(dSpin_, s); dfree(dHtab_, s); dfree(dVext_, s);
+  dfree(dG_, s); dfree(dC1_, s); dfree(dCN_, s); dfree(dZ_, s); dfree(dY_, s); dfree(dQ_, s);
+  dfree(dSigL_, s); dfree(dSigR_, s); dfree(dGamL_, s); dfree(dGamR_, s);
+  dfree(dP1_, s); dfree(dP2_, s); dfree(dCol1_, s); dfree(dColN_, s);
+  dfree(dPx1_, s); dfree(dPy1_, s); dfree(dPz1_, s); dfree(dPx2_, s); dfree(dPy2_, s); dfree(dPz2_, s);
+  if (currents_) { dfree(dYalt_, s); dfree(dCNalt_, s); }
+  dfree(dEr_, s); dfree(dOrAcc_, s); dfree(dContactCoef_, s); dfree(dG11_, s); dfree(dTrJ_, s);
+  dfree(dSite_, s); dfree(dSums_, s); dfree(dTr_, s); dfree(dAcc_, s); dfree(dStatus_, s); dfree(dItems_, s);
+  dfree(dSr_, s); dfree(dSrSigL_, s); dfree(dSrSigR_, s); dfree(dSrGamL_, s); dfree(dSrGamR_, s);
+  dfree(dSrCmax_, s); dfree(dSrDos_, s); dfree(dSrActive_, s); dfree(dSrE_, s); dfree(dSrHend_, s);
+  dfree(dSrStatus_, s);
+  inv_work_free(inv_, s);
+  dfree(dWinv_, s); dfree(dW32_, s); dfree(dT_, s); dfree(sa_.data, s); dfree(sb_.data, s); dfree(sa_.exps, s);
+  dfree(sb_.exps, s); dfree(sw_.data, s); dfree(sw_.exps, s); dfree(sgl_.data, s); dfree(sgl_.exps, s);
+  dfree(sgr_.data, s); dfree(sgr_.exps, s);
+  dfree(dRnorm_, s); dfree(dNsIdx_, s); dfree(dNsX_, s); dfree(dNsW_, s); dfree(dTcErr_, s);
+  cudaStreamSynchronize(own_st_);   // the frees have run: the blocks are back in the pool
+  pinned_give(hPin_, hPinBytes_);
+  cudaStreamDestroy(own_st_);
+}
+
+int pool_trim(int device) {
+  cudaMemPool_t pool;
+  NEGF_TRY(pool_for(device, &pool));
+  NEGF_CUDA_TRY(cudaMemPoolTrimTo(pool, 0));
+  return NEGF_OK;
 }
 
 int Engine::configure(const negf_params& p) {
@@ -167,96 +237,100 @@ int Engine::init(const negf_params& p) {
 }
 
 int Engine::alloc() {
+  if (!dry_) NEGF_TRY(pool_for(p_.device, &pool_));
   const long long N = p_.npx;
   const long long total = nsite_total();
-  NEGF_TRY(dalloc(&dH_, (size_t)(p_.n_hamiltonians * N * MM_), bytes_, dry_));
-  NEGF_TRY(dalloc(&dHop_, (size_t)MM_, bytes_, dry_));
-  NEGF_TRY(dalloc(&dHopBD_, (size_t)nsite_ * p_.norb * p_.norb, bytes_, dry_));
-  NEGF_TRY(dalloc(&dSpin_, (size_t)3 * p_.norb * p_.norb, bytes_, dry_));
-  NEGF_TRY(dalloc(&dHtab_, (size_t)16 * (2 + p_.npz), bytes_, dry_));
-  NEGF_TRY(dalloc(&dVext_, (size_t)total, bytes_, dry_));
-  NEGF_TRY(dalloc(&dG_, (size_t)(B_ * N * MM_), bytes_, dry_));
+  NEGF_TRY(dalloc(&dH_, (size_t)(p_.n_hamiltonians * N * MM_), bytes_, dry_, pool_, own_st_));
+  NEGF_TRY(dalloc(&dHop_, (size_t)MM_, bytes_, dry_, pool_, own_st_));
+  NEGF_TRY(dalloc(&dHopBD_, (size_t)nsite_ * p_.norb * p_.norb, bytes_, dry_, pool_, own_st_));
+  NEGF_TRY(dalloc(&dSpin_, (size_t)3 * p_.norb * p_.norb, bytes_, dry_, pool_, own_st_));
+  NEGF_TRY(dalloc(&dHtab_, (size_t)16 * (2 + p_.npz), bytes_, dry_, pool_, own_st_));
+  NEGF_TRY(dalloc(&dVext_, (size_t)total, bytes_, dry_, pool_, own_st_));
+  NEGF_TRY(dalloc(&dG_, (size_t)(B_ * N * MM_), bytes_, dry_, pool_, own_st_));
   double2** bufs[] = {&dC1_, &dCN_, &dZ_, &dY_, &dQ_, &dSigL_, &dSigR_, &dGamL_, &dGamR_};
-  for (double2** b : bufs) NEGF_TRY(dalloc(b, (size_t)(B_ * MM_), bytes_, dry_));
-  NEGF_TRY(dalloc(&dP1_, (size_t)(B_ * N * M_ * p_.norb), bytes_, dry_));
-  NEGF_TRY(dalloc(&dP2_, (size_t)(B_ * N * M_ * p_.norb), bytes_, dry_));
+  for (double2** b : bufs) NEGF_TRY(dalloc(b, (size_t)(B_ * MM_), bytes_, dry_, pool_, own_st_));
+  NEGF_TRY(dalloc(&dP1_, (size_t)(B_ * N * M_ * p_.norb), bytes_, dry_, pool_, own_st_));
+  NEGF_TRY(dalloc(&dP2_, (size_t)(B_ * N * M_ * p_.norb), bytes_, dry_, pool_, own_st_));
   if (keep_columns_) {
-    NEGF_TRY(dalloc(&dCol1_, (size_t)(N * MM_), bytes_, dry_));
-    NEGF_TRY(dalloc(&dColN_, (size_t)(N * MM_), bytes_, dry_));
+    NEGF_TRY(dalloc(&dCol1_, (size_t)(N * MM_), bytes_, dry_, pool_, own_st_));
+    NEGF_TRY(dalloc(&dColN_, (size_t)(N * MM_), bytes_, dry_, pool_, own_st_));
   }
   if (currents_) {
     double2** pb[] = {&dPx1_, &dPy1_, &dPz1_, &dPx2_, &dPy2_, &dPz2_};
-    for (double2** b : pb) NEGF_TRY(dalloc(b, (size_t)(B_ * N * M_ * p_.norb), bytes_, dry_));
-    NEGF_TRY(dalloc(&dYalt_, (size_t)(B_ * MM_), bytes_, dry_));
-    NEGF_TRY(dalloc(&dCNalt_, (size_t)(B_ * MM_), bytes_, dry_));
+    for (double2** b : pb) NEGF_TRY(dalloc(b, (size_t)(B_ * N * M_ * p_.norb), bytes_, dry_, pool_, own_st_));
+    NEGF_TRY(dalloc(&dYalt_, (size_t)(B_ * MM_), bytes_, dry_, pool_, own_st_));
+    NEGF_TRY(dalloc(&dCNalt_, (size_t)(B_ * MM_), bytes_, dry_, pool_, own_st_));
     // the x bond of the last slice does not exist: its blocks stay zero
     if (!dry_)
       for (double2* b : {dPx1_, dPx2_})
-        NEGF_CUDA_TRY(cudaMemset(b, 0, sizeof(double2) * (size_t)(B_ * N * M_ * p_.norb)));
+        NEGF_CUDA_TRY(cudaMemsetAsync(b, 0, sizeof(double2) * (size_t)(B_ * N * M_ * p_.norb), own_st_));
   } else {
     dYalt_ = dY_;
     dCNalt_ = dCN_;
   }
   sums_blocks_ = (int)((total + 255) / 256);
-  if (p_.contact_type != NEGF_CONTACT_LEADS) NEGF_TRY(dalloc(&dContactCoef_, (size_t)S_ * 6, bytes_, dry_));
+  if (p_.contact_type != NEGF_CONTACT_LEADS) NEGF_TRY(dalloc(&dContactCoef_, (size_t)S_ * 6, bytes_, dry_, pool_, own_st_));
   if (sc_()) {
-    NEGF_TRY(dalloc(&dG11_, (size_t)B_ * M_ * p_.norb, bytes_, dry_));
-    NEGF_TRY(dalloc(&dTrJ_, (size_t)B_, bytes_, dry_));
+    NEGF_TRY(dalloc(&dG11_, (size_t)B_ * M_ * p_.norb, bytes_, dry_, pool_, own_st_));
+    NEGF_TRY(dalloc(&dTrJ_, (size_t)B_, bytes_, dry_, pool_, own_st_));
   }
-  NEGF_TRY(dalloc(&dSite_, (size_t)(B_ * nf_ * total), bytes_, dry_));
-  NEGF_TRY(dalloc(&dSums_, (size_t)B_ * sums_blocks_ * 2, bytes_, dry_));
-  NEGF_TRY(dalloc(&dTr_, (size_t)B_ * 4, bytes_, dry_));
-  NEGF_TRY(dalloc(&dAcc_, (size_t)(p_.n_hamiltonians * nf_ * total), bytes_, dry_));
-  NEGF_TRY(dalloc(&dStatus_, (size_t)B_, bytes_, dry_));
-  NEGF_TRY(dalloc(&dItems_, (size_t)B_, bytes_, dry_));
-  NEGF_TRY(dalloc(&dSr_, (size_t)(kSrBlocks * S_ * MM_), bytes_, dry_));
+  NEGF_TRY(dalloc(&dSite_, (size_t)(B_ * nf_ * total), bytes_, dry_, pool_, own_st_));
+  NEGF_TRY(dalloc(&dSums_, (size_t)B_ * sums_blocks_ * 2, bytes_, dry_, pool_, own_st_));
+  NEGF_TRY(dalloc(&dTr_, (size_t)B_ * 4, bytes_, dry_, pool_, own_st_));
+  NEGF_TRY(dalloc(&dAcc_, (size_t)(p_.n_hamiltonians * nf_ * total), bytes_, dry_, pool_, own_st_));
+  NEGF_TRY(dalloc(&dStatus_, (size_t)B_, bytes_, dry_, pool_, own_st_));
+  NEGF_TRY(dalloc(&dItems_, (size_t)B_, bytes_, dry_, pool_, own_st_));
+  NEGF_TRY(dalloc(&dSr_, (size_t)(kSrBlocks * S_ * MM_), bytes_, dry_, pool_, own_st_));
   double2** srb[] = {&dSrSigL_, &dSrSigR_, &dSrGamL_, &dSrGamR_};
-  for (double2** b : srb) NEGF_TRY(dalloc(b, (size_t)(S_ * MM_), bytes_, dry_));
-  NEGF_TRY(dalloc(&dSrCmax_, (size_t)2 * S_, bytes_, dry_));
-  NEGF_TRY(dalloc(&dSrDos_, (size_t)2 * S_, bytes_, dry_));
-  NEGF_TRY(dalloc(&dSrActive_, (size_t)2 * S_, bytes_, dry_));
-  NEGF_TRY(dalloc(&dSrE_, (size_t)S_, bytes_, dry_));
-  NEGF_TRY(dalloc(&dSrHend_, (size_t)S_, bytes_, dry_));
-  NEGF_TRY(dalloc(&dSrStatus_, (size_t)S_, bytes_, dry_));
+  for (double2** b : srb) NEGF_TRY(dalloc(b, (size_t)(S_ * MM_), bytes_, dry_, pool_, own_st_));
+  NEGF_TRY(dalloc(&dSrCmax_, (size_t)2 * S_, bytes_, dry_, pool_, own_st_));
+  NEGF_TRY(dalloc(&dSrDos_, (size_t)2 * S_, bytes_, dry_, pool_, own_st_));
+  NEGF_TRY(dalloc(&dSrActive_, (size_t)2 * S_, bytes_, dry_, pool_, own_st_));
+  NEGF_TRY(dalloc(&dSrE_, (size_t)S_, bytes_, dry_, pool_, own_st_));
+  NEGF_TRY(dalloc(&dSrHend_, (size_t)S_, bytes_, dry_, pool_, own_st_));
+  NEGF_TRY(dalloc(&dSrStatus_, (size_t)S_, bytes_, dry_, pool_, own_st_));
   {   // inv_work_alloc: R buffer, pivots, INFO
     const long long cap = std::max(B_, S_);
-    if (!dry_) NEGF_TRY(inv_work_alloc(inv_, M_, (int)cap));
+    if (!dry_) NEGF_TRY(inv_work_alloc(inv_, M_, (int)cap, pool_, own_st_));
     bytes_ += 16LL * cap * panel_width(M_) * M_ + 4LL * cap * M_ + 4LL * cap;
   }
   if (mixed_) {
     const int cap = std::max(B_, S_);
     const int smax = 8;   // every slice count a phase may use (RGF, Sancho-Rubio, residual: <= 8)
-    NEGF_TRY(dalloc(&dWinv_, (size_t)(cap * MM_), bytes_, dry_));
-    NEGF_TRY(dalloc(&dW32_, (size_t)(cap * MM_), bytes_, dry_));
-    NEGF_TRY(dalloc(&dT_, (size_t)(cap * MM_), bytes_, dry_));
+    NEGF_TRY(dalloc(&dWinv_, (size_t)(cap * MM_), bytes_, dry_, pool_, own_st_));
+    NEGF_TRY(dalloc(&dW32_, (size_t)(cap * MM_), bytes_, dry_, pool_, own_st_));
+    NEGF_TRY(dalloc(&dT_, (size_t)(cap * MM_), bytes_, dry_, pool_, own_st_));
     const int kp = padded_k(M_);
-    NEGF_TRY(dalloc(reinterpret_cast<char**>(&sa_.data), sliced_bytes_a(M_, kp, smax, cap), bytes_, dry_));
-    NEGF_TRY(dalloc(reinterpret_cast<char**>(&sb_.data), sliced_bytes_b(M_, kp, smax, cap), bytes_, dry_));
-    NEGF_TRY(dalloc(reinterpret_cast<char**>(&sw_.data), sliced_bytes_a(M_, kp, smax, cap), bytes_, dry_));
-    NEGF_TRY(dalloc(&sw_.exps, (size_t)cap * M_, bytes_, dry_));
-    NEGF_TRY(dalloc(&sa_.exps, (size_t)cap * M_, bytes_, dry_));
-    NEGF_TRY(dalloc(&sb_.exps, (size_t)cap * M_, bytes_, dry_));
-    NEGF_TRY(dalloc(reinterpret_cast<char**>(&sgl_.data), sliced_bytes_b(M_, kp, s_rgf_, B_), bytes_, dry_));
-    NEGF_TRY(dalloc(reinterpret_cast<char**>(&sgr_.data), sliced_bytes_b(M_, kp, s_rgf_, B_), bytes_, dry_));
-    NEGF_TRY(dalloc(&sgl_.exps, (size_t)B_ * M_, bytes_, dry_));
-    NEGF_TRY(dalloc(&sgr_.exps, (size_t)B_ * M_, bytes_, dry_));
+    NEGF_TRY(dalloc(reinterpret_cast<char**>(&sa_.data), sliced_bytes_a(M_, kp, smax, cap), bytes_, dry_, pool_, own_st_));
+    NEGF_TRY(dalloc(reinterpret_cast<char**>(&sb_.data), sliced_bytes_b(M_, kp, smax, cap), bytes_, dry_, pool_, own_st_));
+    NEGF_TRY(dalloc(reinterpret_cast<char**>(&sw_.data), sliced_bytes_a(M_, kp, smax, cap), bytes_, dry_, pool_, own_st_));
+    NEGF_TRY(dalloc(&sw_.exps, (size_t)cap * M_, bytes_, dry_, pool_, own_st_));
+    NEGF_TRY(dalloc(&sa_.exps, (size_t)cap * M_, bytes_, dry_, pool_, own_st_));
+    NEGF_TRY(dalloc(&sb_.exps, (size_t)cap * M_, bytes_, dry_, pool_, own_st_));
+    NEGF_TRY(dalloc(reinterpret_cast<char**>(&sgl_.data), sliced_bytes_b(M_, kp, s_rgf_, B_), bytes_, dry_, pool_, own_st_));
+    NEGF_TRY(dalloc(reinterpret_cast<char**>(&sgr_.data), sliced_bytes_b(M_, kp, s_rgf_, B_), bytes_, dry_, pool_, own_st_));
+    NEGF_TRY(dalloc(&sgl_.exps, (size_t)B_ * M_, bytes_, dry_, pool_, own_st_));
+    NEGF_TRY(dalloc(&sgr_.exps, (size_t)B_ * M_, bytes_, dry_, pool_, own_st_));
     sgl_.data_bytes = sgr_.data_bytes = sliced_bytes_b(M_, kp, s_rgf_, B_);
     sgl_.exps_count = sgr_.exps_count = (size_t)B_ * M_;
     sa_.data_bytes = sw_.data_bytes = sliced_bytes_a(M_, kp, smax, cap);
     sb_.data_bytes = sliced_bytes_b(M_, kp, smax, cap);
     sa_.exps_count = sb_.exps_count = sw_.exps_count = (size_t)cap * M_;
-    NEGF_TRY(dalloc(&dRnorm_, (size_t)cap, bytes_, dry_));
-    NEGF_TRY(dalloc(&dNsIdx_, (size_t)cap, bytes_, dry_));
-    NEGF_TRY(dalloc(&dNsX_, (size_t)cap * MM_, bytes_, dry_));
-    NEGF_TRY(dalloc(&dNsW_, (size_t)cap * MM_, bytes_, dry_));
-    NEGF_TRY(dalloc(&dTcErr_, (size_t)1, bytes_, dry_));
-    if (!dry_) NEGF_CUDA_TRY(cudaMemset(dTcErr_, 0, sizeof(int)));
+    NEGF_TRY(dalloc(&dRnorm_, (size_t)cap, bytes_, dry_, pool_, own_st_));
+    NEGF_TRY(dalloc(&dNsIdx_, (size_t)cap, bytes_, dry_, pool_, own_st_));
+    NEGF_TRY(dalloc(&dNsX_, (size_t)cap * MM_, bytes_, dry_, pool_, own_st_));
+    NEGF_TRY(dalloc(&dNsW_, (size_t)cap * MM_, bytes_, dry_, pool_, own_st_));
+    NEGF_TRY(dalloc(&dTcErr_, (size_t)1, bytes_, dry_, pool_, own_st_));
+    if (!dry_) NEGF_CUDA_TRY(cudaMemsetAsync(dTcErr_, 0, sizeof(int), own_st_));
   }
   if (dry_) return NEGF_OK;   // estimate_bytes: device bytes only
   hPinBytes_ = sizeof(double) * (size_t)std::max<long long>(
                    {(long long)B_ * sums_blocks_ * 2, (long long)B_ * 4, 4LL * S_,
                     (long long)p_.n_hamiltonians * nf_ * total, (long long)nf_ * total, 64});
-  NEGF_CUDA_TRY(cudaMallocHost((void**)&hPin_, hPinBytes_));
+  NEGF_TRY(pinned_take(hPinBytes_, &hPin_, &hPinBytes_));
+  // the allocations are ordered on the engine's stream; after this they are usable from
+  // any stream (the caller's, through negf_set_stream) and by the synchronous copies below
+  NEGF_CUDA_TRY(cudaStreamSynchronize(own_st_));
   // spin operators (default: tau0 (x) sigma_j of Source/Read_In_Allocate.F90:183-196)
   std::vector<double2> spin(3 * p_.norb * p_.norb, make_double2(0.0, 0.0));
   bool any = false;
@@ -990,8 +1064,12 @@ int Engine::densities_impl(const std::vector<Item>& items, std::vector<double>& 
 int Engine::ensure_resolved() {
   if (!currents_) return NEGF_ESTATE;
   const long long total = nsite_total();
-  if (!dEr_) NEGF_TRY(dalloc(&dEr_, (size_t)B_ * 4 * total, bytes_));
-  if (!dOrAcc_) NEGF_TRY(dalloc(&dOrAcc_, (size_t)p_.n_hamiltonians * n_or_fields() * total, bytes_));
+  if (!dEr_ || !dOrAcc_) {
+    if (!dEr_) NEGF_TRY(dalloc(&dEr_, (size_t)B_ * 4 * total, bytes_, false, pool_, own_st_));
+    if (!dOrAcc_)
+      NEGF_TRY(dalloc(&dOrAcc_, (size_t)p_.n_hamiltonians * n_or_fields() * total, bytes_, false, pool_, own_st_));
+    NEGF_CUDA_TRY(cudaStreamSynchronize(own_st_));
+  }
   return NEGF_OK;
 }
 

@@ -202,6 +202,7 @@ class Engine {
  private:
   int configure(const negf_params& p);   // validation and derived sizes, no CUDA calls
   bool dry_ = false;                      // alloc() counts bytes without allocating
+  cudaMemPool_t pool_ = nullptr;          // the library's stream-ordered pool on p_.device
   int alloc();
   // Y = op(H) X (left) or X op(H) (right) for every block of a strided batch
   int hop_mul(int left, Op op, const double2* X, long long sX, double2* Y, long long sY, int batch);
@@ -217,5 +218,7 @@ class Engine {
 };
 
 int merge_info_kernel_launch(int batch, const int* info, int* status, cudaStream_t st);
+// release the unused blocks of the library's memory pool on `device` to the device
+int pool_trim(int device);
 
 }  // namespace negf

@@ -434,23 +434,29 @@ int panel_width(int n, int elem_bytes) {
   return nb;
 }
 
-int inv_work_alloc(InvWork& w, int n, int batch) {
+int inv_work_alloc(InvWork& w, int n, int batch, cudaMemPool_t pool, cudaStream_t st) {
   if (w.n_cap >= n && w.batch_cap >= batch && w.rbuf) return NEGF_OK;
-  inv_work_free(w);
+  inv_work_free(w, st);
   w.nb = panel_width(n);
+  w.pooled = pool != nullptr;
+  auto get = [&](void** p, size_t bytes) {
+    return (pool ? cudaMallocFromPoolAsync(p, bytes, pool, st) : cudaMalloc(p, bytes)) == cudaSuccess;
+  };
   // R buffer: nb x n complex per matrix, large enough for both forms (FP64 nb, FP32 2nb)
-  if (cudaMalloc(&w.rbuf, sizeof(double2) * (size_t)batch * w.nb * n) != cudaSuccess) return NEGF_ENOMEM;
-  if (cudaMalloc(&w.ipiv, sizeof(int) * (size_t)batch * n) != cudaSuccess) return NEGF_ENOMEM;
-  if (cudaMalloc(&w.info, sizeof(int) * (size_t)batch) != cudaSuccess) return NEGF_ENOMEM;
+  if (!get((void**)&w.rbuf, sizeof(double2) * (size_t)batch * w.nb * n)) return NEGF_ENOMEM;
+  if (!get((void**)&w.ipiv, sizeof(int) * (size_t)batch * n)) return NEGF_ENOMEM;
+  if (!get((void**)&w.info, sizeof(int) * (size_t)batch)) return NEGF_ENOMEM;
   w.n_cap = n;
   w.batch_cap = batch;
   return NEGF_OK;
 }
 
-void inv_work_free(InvWork& w) {
-  if (w.rbuf) cudaFree(w.rbuf);
-  if (w.ipiv) cudaFree(w.ipiv);
-  if (w.info) cudaFree(w.info);
+void inv_work_free(InvWork& w, cudaStream_t st) {
+  for (void* p : {(void*)w.rbuf, (void*)w.ipiv, (void*)w.info})
+    if (p) {
+      if (w.pooled) cudaFreeAsync(p, st);
+      else cudaFree(p);
+    }
   w = InvWork{};
 }
 

@@ -152,9 +152,11 @@ struct InvWork {
   int* ipiv = nullptr;       // batch * n
   int* info = nullptr;       // batch
   int n_cap = 0, batch_cap = 0, nb = 0;
+  bool pooled = false;       // allocated stream-ordered from a memory pool
 };
-int inv_work_alloc(InvWork& w, int n, int batch);
-void inv_work_free(InvWork& w);
+// pool = nullptr: plain cudaMalloc / cudaFree; otherwise stream-ordered on `st` from `pool`
+int inv_work_alloc(InvWork& w, int n, int batch, cudaMemPool_t pool = nullptr, cudaStream_t st = 0);
+void inv_work_free(InvWork& w, cudaStream_t st = 0);
 int panel_width(int n, int elem_bytes = 16);
 // A: batch matrices of n x n, column-major, consecutive at stride sA.  On return A holds
 // the inverses; w.info[b] (device) holds the LAPACK-style INFO of each matrix.

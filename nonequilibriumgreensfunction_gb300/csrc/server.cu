@@ -191,7 +191,14 @@ struct negf_server {
           nw->key = r->key;
           nw->eng = std::make_unique<negf::Engine>();
           const double t0 = now();
-          const int irc = nw->eng->init(engine_params(r->key));
+          int irc = nw->eng->init(engine_params(r->key));
+          if (irc == NEGF_ENOMEM) {
+            // the library's pool keeps released engines' blocks for reuse; when they do not
+            // fit this engine's buffers, give them back to the device and try once more
+            nw->eng = std::make_unique<negf::Engine>();
+            negf::pool_trim(p.device);
+            irc = nw->eng->init(engine_params(r->key));
+          }
           t_create += now() - t0;
           if (irc != NEGF_OK) {
             r->status = NEGF_ENOMEM;
@@ -467,7 +474,9 @@ int negf_server_destroy(negf_server* s) {
   for (auto& w : ws)
     if (w->th.joinable()) w->th.join();
   ws.clear();
+  const int dev = s->p.device;
   delete s;
+  negf::pool_trim(dev);   // the released engines' blocks go back to the device
   return NEGF_OK;
 }
 
