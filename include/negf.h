@@ -84,7 +84,9 @@ typedef struct negf_params {
     int32_t reserved[3];     /* must be zero                                             */
     double  spin_ops[3][4][4][2]; /* gMx, gMy, gMz (row-major [row][col][re,im]) used by
                                      the spin reduction, Source/Read_In_Allocate.F90:183-196;
-                                     all zero = the reference's tau0 (x) sigma_j          */
+                                     all zero = the reference's own for the nh electron
+                                     orbitals: tau0 (x) sigma_j (nh = 4), the Pauli
+                                     matrices (nh = 2, :205-216), zero (nh = 1)           */
     /* Contacts (contactType, Source/Read_In_Allocate.F90:19, Contact_Self_Energy.F90:19-92):
      *   NEGF_CONTACT_LEADS   semi-infinite leads, Sancho-Rubio decimation (default);
      *   NEGF_CONTACT_PBIG    phenomenological: Sigma = -i rate on every orbital of the end
@@ -188,8 +190,8 @@ NEGF_API int negf_set_refinement(negf_handle* h, int32_t ns_max_steps, double ns
 NEGF_API int negf_set_hamiltonian(negf_handle* h, int32_t slot, const double* Htotd, const double* HopX);
 
 /* ---- on-device Hamiltonian ----------------------------------------------------------
- * Build_Hamiltonian (Source/Build_Hamiltonian.F90:1-303, model 0 with open boundaries) on
- * the device: the slot's Htotd is generated in HBM from 4 x 4 site blocks instead of being
+ * Build_Hamiltonian (Source/Build_Hamiltonian.F90:1-303, open boundaries) on the device:
+ * the slot's Htotd is generated in HBM from norb x norb site blocks instead of being
  * copied from the host (npx*M^2*16 bytes, 256 MB at M = 400, npx = 100).  Every slice holds
  * the on-site block on each site, hop_y between (y, z) and (y+1, z) times the Landau-gauge
  * phase exp(i 2 pi z flux / ((npy-1)(npz-1))) (:186-207), hop_z between (y, z) and (y, z+1),
@@ -200,8 +202,11 @@ NEGF_API int negf_set_hamiltonian(negf_handle* h, int32_t slot, const double* Ht
  * u = (s >> 11) 2^-53 and s the i-th output of SplitMix64 seeded with `seed` (Steele, Lea,
  * Flood 2014), i = x + npx (y + npy z) + 1; the site's potential is V + that.  The
  * reference's RANDOM_NUMBER stream is compiler-specific (:230-241); this one is
- * reproducible bit for bit on any host.  Requires norb = 4.  HopX is shared by all slots,
- * as in negf_set_hamiltonian.                                                           */
+ * reproducible bit for bit on any host.  The blocks are norb x norb, norb <= 4 (the
+ * channel models of :13-47: the TI and Bi2Se3 wires 4, the one-band metal 1, the TI
+ * surface and the 1-D spin-orbit wire 2), in the leading rows and columns of the 4 x 4
+ * arrays, whose other entries must be zero; not with superconducting contacts (a BdG
+ * Hamiltonian).  HopX is shared by all slots, as in negf_set_hamiltonian.               */
 typedef struct negf_wire_model {
     double   onsite[4][4][2];  /* row-major [row][col][re, im]                           */
     double   hop[3][4][4][2];  /* hop_x, hop_y, hop_z = H(site, site + e_j)              */

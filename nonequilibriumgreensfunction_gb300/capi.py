@@ -82,7 +82,15 @@ def wire_model_struct(model, shape):
     import numpy as np
     m = NegfWireModel()
     blocks = [np.asarray(model["onsite"], dtype=complex)] + [np.asarray(h, dtype=complex) for h in model["hops"]]
-    flat = [np.stack([b.real, b.imag], axis=-1).ravel() for b in blocks]
+    n = blocks[0].shape[0]
+    if n > 4 or any(b.shape != (n, n) for b in blocks):
+        raise ValueError("site blocks must be norb x norb with norb <= 4")
+    padded = []
+    for b in blocks:                        # norb x norb in the leading corner of 4 x 4
+        q = np.zeros((4, 4), dtype=complex)
+        q[:n, :n] = b
+        padded.append(q)
+    flat = [np.stack([b.real, b.imag], axis=-1).ravel() for b in padded]
     for i, v in enumerate(flat[0]):
         m.onsite[i] = v
     for j in range(3):

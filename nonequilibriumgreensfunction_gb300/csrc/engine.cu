@@ -331,7 +331,9 @@ int Engine::alloc() {
   // the allocations are ordered on the engine's stream; after this they are usable from
   // any stream (the caller's, through negf_set_stream) and by the synchronous copies below
   NEGF_CUDA_TRY(cudaStreamSynchronize(own_st_));
-  // spin operators (default: tau0 (x) sigma_j of Source/Read_In_Allocate.F90:183-196)
+  // spin operators, by default those of Source/Read_In_Allocate.F90 for nh electron orbitals:
+  // tau0 (x) sigma_j for nh = 4 (:183-196), the Pauli matrices for nh = 2 (:205-216), zero
+  // otherwise (:151-159)
   std::vector<double2> spin(3 * p_.norb * p_.norb, make_double2(0.0, 0.0));
   bool any = false;
   for (int j = 0; j < 3; ++j)
@@ -356,6 +358,12 @@ int Engine::alloc() {
       at(1, o, o + 1) = mi;  at(1, o + 1, o) = pi_;
       at(2, o, o) = one;     at(2, o + 1, o + 1) = m1;
     }
+  } else if (ne == 2) {
+    const double2 one = make_double2(1, 0), mi = make_double2(0, -1), pi_ = make_double2(0, 1), m1 = make_double2(-1, 0);
+    auto at = [&](int j, int r, int c) -> double2& { return spin[(j * no + r) * no + c]; };
+    at(0, 0, 1) = one; at(0, 1, 0) = one;
+    at(1, 0, 1) = mi;  at(1, 1, 0) = pi_;
+    at(2, 0, 0) = one; at(2, 1, 1) = m1;
   }
   NEGF_CUDA_TRY(cudaMemcpy(dSpin_, spin.data(), sizeof(double2) * spin.size(), cudaMemcpyHostToDevice));
   return NEGF_OK;

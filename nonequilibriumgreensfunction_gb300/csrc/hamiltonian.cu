@@ -1,6 +1,7 @@
-// On-device Build_Hamiltonian (Source/Build_Hamiltonian.F90:1-303, model 0, open
-// boundaries): one slot's Htotd (npx slices of M x M, column-major) is written in HBM from a
-// table of 4 x 4 site blocks, so a request ships a few hundred bytes instead of npx*M^2*16.
+// On-device Build_Hamiltonian (Source/Build_Hamiltonian.F90:1-303, open boundaries): one
+// slot's Htotd (npx slices of M x M, column-major) is written in HBM from a table of
+// norb x norb site blocks (norb <= 4: the channel models 0-4 of :13-47 have 4, 4, 1, 2 and 2
+// orbitals), so a request ships a few hundred bytes instead of npx*M^2*16.
 //
 // The host computes the blocks that involve rounding (the y hop times its Landau-gauge
 // phase, one block per z, Source/Build_Hamiltonian.F90:186-207); the kernel only places
@@ -39,18 +40,19 @@ __host__ __device__ __forceinline__ double anderson(unsigned long long seed, dou
 }
 
 // tab: [0..15] on-site block, [16..31] hop_z, [32 + 16 z ..] hop_y times the phase of layer z;
-// each block row-major [a][b].  The on-site potential of a site is V (npx*npy*npz,
-// column-major, may be null) plus the counter-based Anderson potential.
-__global__ void build_h_kernel(int npx, int npy, int npz, const double2* __restrict__ tab,
+// each block row-major [a][b] with a row stride of 4 whatever norb.  The on-site potential
+// of a site is V (npx*npy*npz, column-major, may be null) plus the counter-based Anderson
+// potential, on each of its norb orbitals (Insert_Impurity, :154-165).
+__global__ void build_h_kernel(int npx, int npy, int npz, int norb, const double2* __restrict__ tab,
                                const double* __restrict__ V, unsigned long long seed, double W, double2* H) {
   const int x = blockIdx.y;
   const int nsite = npy * npz;
-  const int n = 4 * nsite;
+  const int n = norb * nsite;
   const long long nn = (long long)n * n;
   double2* Hx = H + (long long)x * nn;
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nn; e += (long long)gridDim.x * blockDim.x) {
     const int col = (int)(e / n), row = (int)(e % n);
-    const int rs = row >> 2, ra = row & 3, cs = col >> 2, ca = col & 3;
+    const int rs = row / norb, ra = row - rs * norb, cs = col / norb, ca = col - cs * norb;
     double2 v = make_double2(0.0, 0.0);
     if (rs == cs) {
       v = tab[ra * 4 + ca];
@@ -79,7 +81,9 @@ double2 block_entry(const double (*b)[4][2], int r, int c) { return make_double2
 }  // namespace
 
 int Engine::build_hamiltonian(int slot, const negf_wire_model& m) {
-  if (slot < 0 || slot >= p_.n_hamiltonians || p_.norb != 4) return NEGF_EINVAL;
+  // a plain (not BdG) Hamiltonian of at most 4 orbitals per site
+  const int no = p_.norb;
+  if (slot < 0 || slot >= p_.n_hamiltonians || no > 4 || sc_()) return NEGF_EINVAL;
   for (int i = 0; i < 8; ++i)
     if (m.reserved[i] != 0) return NEGF_EINVAL;
   NEGF_CUDA_TRY(cudaSetDevice(p_.device));
@@ -88,6 +92,11 @@ int Engine::build_hamiltonian(int slot, const negf_wire_model& m) {
   std::vector<double2> tab((size_t)16 * (2 + npz));
   for (int a = 0; a < 4; ++a)
     for (int b = 0; b < 4; ++b) {
+      // entries outside the leading norb x norb block must be zero
+      if (a >= no || b >= no) {
+        for (const double (*blk)[4][2] : {m.onsite, m.hop[0], m.hop[1], m.hop[2]})
+          if (blk[a][b][0] != 0.0 || blk[a][b][1] != 0.0) return NEGF_EINVAL;
+      }
       tab[a * 4 + b] = block_entry(m.onsite, a, b);
       tab[16 + a * 4 + b] = block_entry(m.hop[2], a, b);
     }
@@ -108,8 +117,8 @@ int Engine::build_hamiltonian(int slot, const negf_wire_model& m) {
   // HopX: hop_x on every site (Source/Build_Hamiltonian.F90:59-64)
   std::vector<double2> hx((size_t)MM_, make_double2(0.0, 0.0));
   for (int st = 0; st < nsite_; ++st)
-    for (int a = 0; a < 4; ++a)
-      for (int b = 0; b < 4; ++b) hx[(size_t)(st * 4 + b) * M_ + st * 4 + a] = block_entry(m.hop[0], a, b);
+    for (int a = 0; a < no; ++a)
+      for (int b = 0; b < no; ++b) hx[(size_t)(st * no + b) * M_ + st * no + a] = block_entry(m.hop[0], a, b);
   NEGF_TRY(set_hopx(hx.data()));
 
   const long long total = nsite_total();
@@ -118,7 +127,7 @@ int Engine::build_hamiltonian(int slot, const negf_wire_model& m) {
   if (m.V) NEGF_CUDA_TRY(cudaMemcpyAsync(dVext_, m.V, sizeof(double) * total, cudaMemcpyHostToDevice, st_));
   const long long per = (MM_ + 255) / 256;
   dim3 grid((unsigned)std::min<long long>(per, 1024), npx);
-  build_h_kernel<<<grid, 256, 0, st_>>>(npx, npy, npz, dHtab_, m.V ? dVext_ : nullptr, (unsigned long long)m.seed, m.W,
+  build_h_kernel<<<grid, 256, 0, st_>>>(npx, npy, npz, no, dHtab_, m.V ? dVext_ : nullptr, (unsigned long long)m.seed, m.W,
                                         Hs);
   NEGF_CUDA_TRY(cudaGetLastError());
   count_launch();

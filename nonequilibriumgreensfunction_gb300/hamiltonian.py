@@ -32,6 +32,13 @@ _sy = np.array([[0, -1j], [1j, 0]], dtype=complex)
 _sz = np.array([[1, 0], [0, -1]], dtype=complex)
 
 
+# the reference's Dirac matrices g0..g3 for four orbitals (Source/Read_In_Allocate.F90:161-181)
+_G0 = np.diag([1.0, 1.0, -1.0, -1.0]).astype(complex)
+_G1 = np.array([[0, 0, 0, -1j], [0, 0, 1j, 0], [0, -1j, 0, 0], [1j, 0, 0, 0]], dtype=complex)
+_G2 = np.array([[0, 0, 0, -1], [0, 0, -1, 0], [0, -1, 0, 0], [-1, 0, 0, 0]], dtype=complex)
+_G3 = np.array([[0, 0, -1j, 0], [0, 0, 0, -1j], [1j, 0, 0, 0], [0, 1j, 0, 0]], dtype=complex)
+
+
 def tau_sigma(t, s):
     return np.kron(t, s)
 
@@ -49,16 +56,68 @@ def site_blocks(M0=0.3, B=0.25, A=0.5, zeeman=0.0, basis="tau_sigma"):
         hops = [B * tz - 0.5j * A * tau_sigma(_sx, s) for s in (_sx, _sy, _sz)]
         return onsite, hops[0], hops[1], hops[2]
     if basis == "reference":
-        c0, c1, ci = 0j, 1 + 0j, 1j
-        g0 = np.diag([c1, c1, -c1, -c1])
-        g1 = np.array([[c0, c0, c0, -ci], [c0, c0, ci, c0], [c0, -ci, c0, c0], [ci, c0, c0, c0]])
-        g2 = np.array([[c0, c0, c0, -c1], [c0, c0, -c1, c0], [c0, -c1, c0, c0], [-c1, c0, c0, c0]])
-        g3 = np.array([[c0, c0, -ci, c0], [c0, c0, c0, -ci], [ci, c0, c0, c0], [c0, ci, c0, c0]])
         mm, a0 = 1.5, 1.0
-        onsite = (mm - 3.0 / (a0 * a0)) * g0 + zeeman * tau_sigma(_s0, _sz)
-        hops = [0.5 * (g0 / (a0 * a0) - 1j / a0 * g) for g in (g1, g2, g3)]
+        onsite = (mm - 3.0 / (a0 * a0)) * _G0 + zeeman * tau_sigma(_s0, _sz)
+        hops = [0.5 * (_G0 / (a0 * a0) - 1j / a0 * g) for g in (_G1, _G2, _G3)]
         return onsite, hops[0], hops[1], hops[2]
     raise ValueError("basis must be 'tau_sigma' or 'reference'")
+
+
+# Bi2Se3 parameters (Source/NEGF_Module.F90:10-17, in eV, Angstrom).  The reference declares
+# them REAL(8) but writes them as default-kind literals, so they hold the single-precision
+# values of these decimals; the same values are used here.
+BI2SE3 = {k: float(np.float32(v)) for k, v in
+          dict(A1="2.26", A2="3.33", C="-0.0083", D1="5.74", D2="30.4", M="0.28", B1="6.86", B2="44.5").items()}
+
+# orbitals per site of each channel model (Source/Read_In_Allocate.F90:51-65)
+CHANNEL_NORB = {0: 4, 1: 4, 2: 1, 3: 2, 4: 2}
+
+
+def channel_blocks(channel_type, a0=1.0, mu_t=0.0, t_met=1.0):
+    """(onsite, hop_x, hop_y, hop_z) site blocks of the reference's channel models
+    (Source/Build_Hamiltonian.F90:13-47), norb x norb with norb = CHANNEL_NORB[channel_type]:
+
+        0  toy 3-D TI (norb 4):  (1.5 - 3/a0^2) g0 - mu_t,  hop_j = (g0/a0^2 - i g_j/a0) / 2
+        1  Bi2Se3 (norb 4):      (C + (2 D1 + 4 D2)/a0^2) + (M - (2 B1 + 4 B2)/a0^2) g0,
+                                 hop_x,y = i A2/(2 a0) g_1,2 - D2/a0^2 + B2/a0^2 g0,
+                                 hop_z   = i A1/(2 a0) g3    - D1/a0^2 + B1/a0^2 g0
+        2  one-band metal (1):   6 t,  hop_j = -t
+        3  TI surface (2):       0,  hop_x = -i sigma_y / 2,  hop_y = i sigma_x / 2,  hop_z = 0
+        4  1-D SOC wire (2):     -mu_t,  hop_x = -i sigma_y / 2,  hop_y = hop_z = 0
+
+    g0..g3 are the reference's Dirac matrices for norb 4 (Source/Read_In_Allocate.F90:161-181);
+    for norb 2 its g1, g2, g3 are the Pauli matrices (:205-213).  Model 3 needs npz = 1 and
+    model 4 npy = npz = 1 (Source/Read_In_Allocate.F90:53-60)."""
+    if channel_type not in CHANNEL_NORB:
+        raise ValueError("channel_type must be 0..4")
+    n = CHANNEL_NORB[channel_type]
+    ident = np.eye(n, dtype=complex)
+    zero = np.zeros((n, n), dtype=complex)
+    g0, g1, g2, g3 = _G0, _G1, _G2, _G3
+    if channel_type == 0:
+        onsite = (1.5 - 3.0 / (a0 * a0)) * g0 - mu_t * ident
+        hx, hy, hz = (0.5 * (g0 / (a0 * a0) - 1j / a0 * g) for g in (g1, g2, g3))
+        return onsite, hx, hy, hz
+    if channel_type == 1:
+        p = BI2SE3
+        onsite = (p["C"] + (2.0 * p["D1"] + 4.0 * p["D2"]) / (a0 * a0)) * ident \
+            + (p["M"] - (2.0 * p["B1"] + 4.0 * p["B2"]) / (a0 * a0)) * g0
+        hy = p["A2"] / (2.0 * a0) * 1j * g2 - p["D2"] / (a0 * a0) * ident + p["B2"] / (a0 * a0) * g0
+        hz = p["A1"] / (2.0 * a0) * 1j * g3 - p["D1"] / (a0 * a0) * ident + p["B1"] / (a0 * a0) * g0
+        hx = p["A2"] / (2.0 * a0) * 1j * g1 - p["D2"] / (a0 * a0) * ident + p["B2"] / (a0 * a0) * g0
+        return onsite, hx, hy, hz
+    if channel_type == 2:
+        return 6.0 * t_met * ident, -t_met * ident, -t_met * ident, -t_met * ident
+    if channel_type == 3:
+        return zero, -0.5j * _sy, 0.5j * _sx, zero.copy()
+    return -mu_t * ident, -0.5j * _sy, zero, zero.copy()
+
+
+def channel_model(channel_type, a0=1.0, mu_t=0.0, t_met=1.0, flux=0.0, W=0.0, seed=0, V=None):
+    """negf_build_hamiltonian parameters of channel model ``channel_type`` (channel_blocks);
+    build the handle with norb = CHANNEL_NORB[channel_type]."""
+    onsite, hx, hy, hz = channel_blocks(channel_type, a0, mu_t, t_met)
+    return dict(onsite=onsite, hops=(hx, hy, hz), flux=float(flux), W=float(W), seed=int(seed), V=V)
 
 
 def disorder_potential(npx, npy, npz, W, seed):
@@ -156,11 +215,12 @@ def build_from_model(npx, npy, npz, model):
     """Host twin of negf_build_hamiltonian: (htotd[npx, M, M], hopx[M, M]) with the same
     arithmetic as the device path (the y-hop phase and its product with the block in plain
     float operations, the potential added once to the on-site diagonal), so the two are
-    equal element for element."""
+    equal element for element.  The blocks are norb x norb (norb <= 4)."""
     onsite = np.asarray(model["onsite"], dtype=complex)
     hx, hy, hz = (np.asarray(h, dtype=complex) for h in model["hops"])
+    norb = onsite.shape[0]
     nsite = npy * npz
-    m = NORB * nsite
+    m = norb * nsite
     flux = model["flux"]
     phased = flux != 0.0 and npy > 1 and npz > 1
     hy_z = []
@@ -170,9 +230,9 @@ def build_from_model(npx, npy, npz, model):
             continue
         th = 2.0 * math.pi * z * flux / ((npy - 1) * (npz - 1))
         c, s = math.cos(th), math.sin(th)
-        blk = np.empty((4, 4), dtype=complex)
-        for a in range(4):
-            for b in range(4):
+        blk = np.empty((norb, norb), dtype=complex)
+        for a in range(norb):
+            for b in range(norb):
                 hr, hi = float(hy[a, b].real), float(hy[a, b].imag)
                 blk[a, b] = complex(hr * c - hi * s, hr * s + hi * c)
         hy_z.append(blk)
@@ -180,23 +240,23 @@ def build_from_model(npx, npy, npz, model):
     hopx = np.zeros((m, m), dtype=complex)
     for z in range(npz):
         for y in range(npy):
-            i = (y + z * npy) * NORB
-            s = slice(i, i + NORB)
+            i = (y + z * npy) * norb
+            s = slice(i, i + norb)
             h[s, s] = onsite
             hopx[s, s] = hx
             if y + 1 < npy:
-                t = slice(i + NORB, i + 2 * NORB)
+                t = slice(i + norb, i + 2 * norb)
                 h[s, t] = hy_z[z]
                 h[t, s] = hy_z[z].conj().T
             if z + 1 < npz:
-                t = slice(i + NORB * npy, i + NORB * npy + NORB)
+                t = slice(i + norb * npy, i + norb * npy + norb)
                 h[s, t] = hz
                 h[t, s] = hz.conj().T
     v = anderson_counter(npx, npy, npz, model["W"], model["seed"])
     if model.get("V") is not None:
         v = np.asarray(model["V"], dtype=np.float64) + v      # the device adds V + disorder
     htotd = np.repeat(h[None], npx, axis=0)
-    diag = np.repeat(np.asarray(v).transpose(0, 2, 1).reshape(npx, nsite), NORB, axis=1)
+    diag = np.repeat(np.asarray(v).transpose(0, 2, 1).reshape(npx, nsite), norb, axis=1)
     idx = np.arange(m)
     htotd[:, idx, idx] = (htotd[:, idx, idx].real + diag) + 1j * htotd[:, idx, idx].imag
     return htotd, hopx

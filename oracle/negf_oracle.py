@@ -68,19 +68,94 @@ def reference_gamma_matrices():
     return g0, g1, g2, g3, gMx, gMy, gMz
 
 
-def reference_gds():
-    """gDS, the pairing structure of the superconducting contacts for Nh == 4
-    (Read_In_Allocate.F90:199-202)."""
+def reference_spin_matrices(nh=4):
+    """(gMx, gMy, gMz) for Nh electron orbitals per site: the Nh == 4 matrices of
+    Read_In_Allocate.F90:183-196, the Pauli matrices g1, g2, g3 for Nh == 2 (:205-216), and
+    for any other Nh the zero matrices the arrays are allocated as (:151-159)."""
+    if nh == 4:
+        return reference_gamma_matrices()[4:]
+    if nh == 2:
+        c0, c1, ci = 0j, 1 + 0j, 1j
+        return (np.array([[c0, c1], [c1, c0]]), np.array([[c0, -ci], [ci, c0]]), np.array([[c1, c0], [c0, -c1]]))
+    return tuple(np.zeros((nh, nh), dtype=complex) for _ in range(3))
+
+
+def reference_gds(nh=4):
+    """gDS, the pairing structure of the superconducting contacts: Read_In_Allocate.F90:199-202
+    for Nh == 4, :214-215 for Nh == 2, zero otherwise."""
     c0, c1 = 0j, 1 + 0j
-    return np.array([[c0, c1, c0, c0], [-c1, c0, c0, c0], [c0, c0, c0, c1], [c0, c0, -c1, c0]])
+    if nh == 4:
+        return np.array([[c0, c1, c0, c0], [-c1, c0, c0, c0], [c0, c0, c0, c1], [c0, c0, -c1, c0]])
+    if nh == 2:
+        return np.array([[c0, c1], [-c1, c0]])
+    return np.zeros((nh, nh), dtype=complex)
+
+
+# Bi2Se3 parameters, NEGF_Module.F90:10-17.  They are REAL(8) PARAMETERs initialised from
+# default-kind (single precision) literals, so their values are the nearest floats of the
+# decimals, widened to double.
+MP_A1, MP_A2, MP_C, MP_D1, MP_D2, MP_M, MP_B1, MP_B2 = (
+    float(np.float32(v)) for v in ("2.26", "3.33", "-0.0083", "5.74", "30.4", "0.28", "6.86", "44.5"))
+T_MET = 1.0   # NEGF_Module.F90:7, tMet = 1D0
+
+
+def channel_norb(channel_type):
+    """Orbitals per site of a channel model, Read_In_Allocate.F90:51-65."""
+    return {0: 4, 1: 4, 2: 1, 3: 2, 4: 2}[channel_type]
+
+
+def channel_blocks(channel_type, a0=1.0, mu_t=0.0, t_met=T_MET):
+    """(AA, HopX, HopY, HopZ) site blocks, Nh x Nh, of the channel models of
+    Build_Hamiltonian.F90:13-47: 0 the toy TI, 1 Bi2Se3, 2 the one-band metal, 3 the TI
+    surface state, 4 the 1-D wire with spin-orbit coupling.  Blocks the reference leaves
+    unset stay at their zero initialisation (:8-11).  The Dirac matrices are those of
+    Read_In_Allocate.F90 for the model's Nh (g0 = 0 and g1..g3 the Pauli matrices when
+    Nh == 2, all zero when Nh == 1)."""
+    nh = channel_norb(channel_type)
+    c1, ci = 1 + 0j, 1j
+    ident = np.eye(nh, dtype=complex)
+    if nh == 4:
+        g0, g1, g2, g3 = reference_gamma_matrices()[:4]
+    else:
+        g0 = np.zeros((nh, nh), dtype=complex)
+        g1, g2, g3 = reference_spin_matrices(nh)   # Read_In_Allocate.F90:205-213: g1, g2, g3
+    z = np.zeros((nh, nh), dtype=complex)
+    if channel_type == 0:                                              # :13-18
+        mm = 1.5
+        aa = (mm - 3.0 / (a0 * a0)) * g0 - mu_t * ident
+        hx = 0.5 * (c1 / (a0 * a0) * g0 - ci / a0 * g1)
+        hy = 0.5 * (c1 / (a0 * a0) * g0 - ci / a0 * g2)
+        hz = 0.5 * (c1 / (a0 * a0) * g0 - ci / a0 * g3)
+    elif channel_type == 1:                                            # :19-33
+        aa = (MP_C + (2.0 * MP_D1 + 4.0 * MP_D2) / (a0 * a0)) * ident \
+            + (MP_M - (2.0 * MP_B1 + 4.0 * MP_B2) / (a0 * a0)) * g0
+        hy = MP_A2 / (2.0 * a0) * ci * g2 - MP_D2 / (a0 * a0) * ident + MP_B2 / (a0 * a0) * g0
+        hz = MP_A1 / (2.0 * a0) * ci * g3 - MP_D1 / (a0 * a0) * ident + MP_B1 / (a0 * a0) * g0
+        hx = MP_A2 / (2.0 * a0) * ci * g1 - MP_D2 / (a0 * a0) * ident + MP_B2 / (a0 * a0) * g0
+    elif channel_type == 2:                                            # :34-38
+        aa = np.full((1, 1), 6.0 * t_met, dtype=complex)
+        hx = hy = hz = np.full((1, 1), -t_met, dtype=complex)
+    elif channel_type == 3:                                            # :39-43
+        aa, hz = z, z
+        hy = 0.5 * ci * g1
+        hx = -0.5 * ci * g2
+    elif channel_type == 4:                                            # :44-47
+        aa = (-mu_t) * ident
+        hx = -ci * 0.5 * g2
+        hy = hz = z
+    else:
+        raise ValueError("channelType must be in 0..4")
+    return aa, hx, hy, hz
 
 
 # ---------------------------------------------------------------------------
 # Hamiltonian, model 0 (channelType == 0), Source/Build_Hamiltonian.F90
 # ---------------------------------------------------------------------------
 def build_hamiltonian_reference(npx, npy, npz, a0=1.0, mu_t=0.0, ab_phi=0.0, bcy=0, bcz=0,
-                                disorder=None, onsite_blocks=None, hops=None):
-    """Model-0 slice Hamiltonian, following Build_Hamiltonian.F90:13-18,59-100,154-207.
+                                disorder=None, onsite_blocks=None, hops=None, channel_type=0):
+    """Slice Hamiltonian of channel model ``channel_type`` (``channel_blocks``), following
+    Build_Hamiltonian.F90:13-47,59-100,154-207.  Read_In_Allocate.F90:53-60 forces Npz = 1
+    for model 3 and Npy = Npz = 1 for model 4 (and open boundaries); they are required here.
 
     ``disorder`` is an optional real array (npx, npy, npz) of on-site potentials added by
     Insert_Impurity (Build_Hamiltonian.F90:154-165); the reference only fills slices
@@ -89,19 +164,14 @@ def build_hamiltonian_reference(npx, npy, npz, a0=1.0, mu_t=0.0, ab_phi=0.0, bcy
     default they are the reference's own (MM = 1.5, Build_Hamiltonian.F90:14-18).
     Returns (Htotd[npx, M, M], HopX[M, M]) as complex128, slice index first.
     """
-    norb = 4
-    g0, g1, g2, g3, *_ = reference_gamma_matrices()
-    ident = np.eye(4, dtype=complex)
-    if onsite_blocks is None:
-        mm = 1.5
-        aa = (mm - 3.0 / (a0 * a0)) * g0 - mu_t * ident
-    else:
+    norb = channel_norb(channel_type)
+    if (channel_type == 3 and npz != 1) or (channel_type == 4 and (npy != 1 or npz != 1)):
+        raise ValueError("channel model %d needs Npz = 1 (3) or Npy = Npz = 1 (4)" % channel_type)
+    ident = np.eye(norb, dtype=complex)
+    aa, hx, hy, hz = channel_blocks(channel_type, a0, mu_t)
+    if onsite_blocks is not None:
         aa = np.asarray(onsite_blocks, dtype=complex)
-    if hops is None:
-        hx = 0.5 * (1.0 / (a0 * a0) * g0 - 1j / a0 * g1)
-        hy = 0.5 * (1.0 / (a0 * a0) * g0 - 1j / a0 * g2)
-        hz = 0.5 * (1.0 / (a0 * a0) * g0 - 1j / a0 * g3)
-    else:
+    if hops is not None:
         hx, hy, hz = (np.asarray(h, dtype=complex) for h in hops)
     nn = npy * norb
     m = npz * nn
@@ -344,7 +414,7 @@ def model_contact_self_energy(m, npy, ce, opt: SolveOptions):
         sig[np.arange(k), np.arange(k)] = -1j * rate
         return sig, sig.copy()
     nh, no = opt.nh, opt.norb
-    gds = reference_gds() if opt.gds is None else np.asarray(opt.gds, dtype=complex)
+    gds = reference_gds(opt.nh) if opt.gds is None else np.asarray(opt.gds, dtype=complex)
     ident = np.eye(nh, dtype=complex)
     out = []
     for side in (0, 1):
@@ -459,7 +529,7 @@ def calculate_observables(gnp, grrgt, gam_l, gam_r, htotd, hopx, f1, f2, de, npy
     nsite = npy * npz
     res = {}
     gnd, gpd = gnp["Gnd"], gnp["Gpd"]
-    _, _, _, _, gmx, gmy, gmz = reference_gamma_matrices()
+    gmx, gmy, gmz = reference_spin_matrices(nh)
     if calc_spin:                                           # :10-30
         # site blocks Gnd(idx+ii, idx+jj), ii, jj <= Nh, idx = y*Norb + z*NN, against gM(jj, ii)
         blocks = gnd.reshape(npx, nsite, norb, nsite, norb)

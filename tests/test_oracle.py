@@ -281,3 +281,74 @@ def test_model_contact_self_energies():
     c = O.contact_self_energy(hb, xb, 0.4e-3, O.SolveOptions(norb=8, contact_type=3, chi_lr=0.0, eta=1e-9))
     assert np.array_equal(c["SigmaL"], c["SigmaR"])
     assert abs(c["dosc"][0]) < 1e-3 * mb                     # inside the gap: eta-broadened only
+
+
+# channel models 1-4 (Build_Hamiltonian.F90:19-47) with the sizes Read_In_Allocate.F90:51-60 forces
+CHANNEL_WIRES = {0: (5, 3, 2), 1: (5, 2, 2), 2: (5, 3, 2), 3: (5, 4, 1), 4: (5, 1, 1)}
+
+
+@pytest.mark.parametrize("ct", sorted(CHANNEL_WIRES))
+def test_channel_models_host_twin_equals_oracle_builder(ct):
+    """The package's host twin of the device builder (hamiltonian.channel_model) equals the
+    oracle's Build_Hamiltonian restatement, with disorder and (where the model has a 2-D
+    cross-section) the Aharonov-Bohm phase; every slice is Hermitian."""
+    npx, npy, npz = CHANNEL_WIRES[ct]
+    flux = 0.3 if npy > 1 and npz > 1 else 0.0
+    m = HB.channel_model(ct, mu_t=0.05, flux=flux, W=0.3, seed=7)
+    h, x = HB.build_from_model(npx, npy, npz, m)
+    dis = HB.anderson_counter(npx, npy, npz, 0.3, 7)
+    ho, xo = O.build_hamiltonian_reference(npx, npy, npz, mu_t=0.05, ab_phi=flux, disorder=dis, channel_type=ct)
+    assert h.shape[1] == O.channel_norb(ct) * npy * npz == HB.CHANNEL_NORB[ct] * npy * npz
+    assert np.abs(h - ho).max() <= 1e-15 * max(1.0, np.abs(ho).max())
+    assert np.array_equal(x, xo)
+    for s in ho:
+        assert np.abs(s - s.conj().T).max() <= 1e-15 * np.abs(s).max()
+
+
+def test_channel_models_refuse_sizes_the_reference_forces():
+    with pytest.raises(ValueError):
+        O.build_hamiltonian_reference(4, 3, 2, channel_type=3)
+    with pytest.raises(ValueError):
+        O.build_hamiltonian_reference(4, 2, 1, channel_type=4)
+
+
+def test_one_band_metal_transmission_counts_open_modes():
+    """Clean one-band metal (channelType 2): E = 6t + e_y + e_z - 2t cos kx with the open
+    chains' transverse levels e = -2t cos(pi m / (n + 1)); T equals the number of
+    transverse modes with |E - 6 - e_y - e_z| < 2."""
+    npx, npy, npz = 5, 3, 2
+    h, x = O.build_hamiltonian_reference(npx, npy, npz, channel_type=2)
+    opt = O.SolveOptions(eta=1e-7, sr_tol=1e-12, norb=1)
+    ey = -2.0 * np.cos(np.pi * np.arange(1, npy + 1) / (npy + 1))
+    ez = -2.0 * np.cos(np.pi * np.arange(1, npz + 1) / (npz + 1))
+    for e in (2.0, 3.7, 5.1, 6.3, 9.5):
+        n_open = int(np.sum(np.abs(e - 6.0 - ey[:, None] - ez[None, :]) < 2.0))
+        r = O.energy_sweep(h, x, e, (0.0, 0.0), 1e-3, npy, npz, opt)
+        assert abs(r["T12"] - n_open) < 1e-4, (e, r["T12"], n_open)
+
+
+def test_spin_orbit_wire_and_surface_models_conduct_integer_channels():
+    """The 1-D spin-orbit wire (channelType 4, H(k) = -mu + sin(k) sigma_y) has two
+    channels for |E + mu| < 1 and none outside; the clean TI surface strip (3), the Bi2Se3
+    wire (1) and the toy TI (0) carry an integer number of channels."""
+    h, x = O.build_hamiltonian_reference(5, 1, 1, channel_type=4, mu_t=0.1)
+    opt = O.SolveOptions(eta=1e-7, sr_tol=1e-12, norb=2)
+    for e, want in ((-0.9, 2), (0.3, 2), (0.7, 2), (1.3, 0), (-1.4, 0)):
+        r = O.energy_sweep(h, x, e, (0.0, 0.0), 1e-3, 1, 1, opt)
+        assert abs(r["T12"] - want) < 1e-4, (e, r["T12"])
+    for ct, (npy, npz), es in ((3, (4, 1), (-0.6, 0.8)), (1, (2, 2), (-20.0,)), (0, (3, 2), (0.4,))):
+        h, x = O.build_hamiltonian_reference(5, npy, npz, channel_type=ct)
+        opt = O.SolveOptions(eta=1e-7, sr_tol=1e-12, norb=O.channel_norb(ct))
+        for e in es:
+            t = O.energy_sweep(h, x, e, (0.0, 0.0), 1e-3, npy, npz, opt)["T12"]
+            assert t > 0.5 and abs(t - round(t)) < 1e-4, (ct, e, t)
+
+
+def test_spin_and_pairing_matrices_follow_the_orbital_count():
+    """Read_In_Allocate.F90: Nh = 2 uses the Pauli matrices for gMx, gMy, gMz and
+    [[0, 1], [-1, 0]] for gDS; Nh = 1 leaves them zero."""
+    sx, sy, sz = O.reference_spin_matrices(2)
+    assert np.array_equal(sx @ sy - sy @ sx, 2j * sz)
+    assert all(not g.any() for g in O.reference_spin_matrices(1))
+    assert np.array_equal(O.reference_gds(2), np.array([[0, 1], [-1, 0]], dtype=complex))
+    assert np.array_equal(O.reference_spin_matrices(4)[0], O.reference_gamma_matrices()[4])
