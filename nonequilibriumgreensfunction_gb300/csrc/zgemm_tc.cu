@@ -29,8 +29,9 @@
 // Kernel structure (one 128 x NT output tile per CTA, 6 warps):
 //   warp 0      TMA producer: for each K block of 32, S A-slices (128 x 32) and S B-slices
 //               (NT x 32) into a ring of shared-memory stages (SWIZZLE_64B, K-major).
-//   warp 1      TMEM allocation and the single-thread tcgen05.mma issue loop; commits
-//               release the stage and, at the end, signal the epilogue.
+//   warp 1      TMEM allocation and the single-thread tcgen05.mma issue loop (one MMA per
+//               A slice, spanning the B slices it pairs with); commits release the stage
+//               and, at the end, signal the epilogue.
 //   warps 2-5   epilogue: tcgen05.ld of the S accumulators, FP64 recombination; lanes
 //               2i and 2i+1 hold the real and imaginary parts of C row i and exchange
 //               them with one shuffle, the even lane storing the even columns and the
@@ -437,6 +438,38 @@ struct TcCfg {
   static_assert(KS == 1 || KS == 2, "one or two accumulator sets along K");
 };
 
+// The MMAs of one stage.  Accumulator d (TMEM columns [d NT, (d+1) NT) from acc_base) sums
+// the slice pairs (p, q) with p + q = d.  The stage's B slice tiles lie back to back (slice q
+// at q * B_TILE, NT rows each, one K-major SWIZZLE_64B layout whose 512-byte atoms continue
+// across the tiles), so for one A slice p the B slices q0 .. q0+qn-1 form one (qn NT)-row
+// operand, and one MMA of N = qn NT adds the pairs (p, q0), ..., (p, q0+qn-1) into the
+// accumulators p+q0 .. p+q0+qn-1, which are contiguous in TMEM.  Per K step of 16 that is S
+// MMAs (a few more where S NT > 256, the largest N at M = 128) instead of S (S+1)/2, and each
+// A slice is read from shared memory once instead of S - p times.  Every accumulator still
+// receives its pairs in the same order (p ascending), and its partial sums are the same
+// exact integers.  `overwrite`: the first K block of an accumulator set, whose first MMA per
+// accumulator (p = 0, first K step) replaces what TMEM held.
+template <int S, int NT, int A_TILE, int B_TILE>
+__device__ __forceinline__ void issue_stage_mmas(uint32_t acc_base, uint64_t da0, uint64_t db0, bool overwrite) {
+  constexpr int QMAX = 256 / NT;
+  static_assert(QMAX >= 1, "one B slice per MMA at least");
+#pragma unroll
+  for (int p = 0; p < S; ++p) {
+#pragma unroll
+    for (int q0 = 0; q0 < S - p; q0 += QMAX) {
+      const int qn = (S - p - q0) < QMAX ? (S - p - q0) : QMAX;
+      const uint32_t idesc = make_idesc(TILE_M, qn * NT);
+#pragma unroll
+      for (int kk = 0; kk < BK / 16; ++kk) {
+        const uint64_t da = da0 + (uint64_t)((p * A_TILE + kk * 32) >> 4);
+        const uint64_t db = db0 + (uint64_t)((q0 * B_TILE + kk * 32) >> 4);
+        const uint32_t acc = (!overwrite || p > 0 || kk > 0) ? 1u : 0u;
+        tc_mma(acc_base + (uint32_t)((p + q0) * NT), da, db, idesc, acc);
+      }
+    }
+  }
+}
+
 struct TcArgs {
   int m, n, kp;            // rows of C, complex columns of C, K' = 2K
   int batch;
@@ -561,7 +594,6 @@ __global__ void __launch_bounds__(TC_THREADS, MINB)
   } else if (warp == 1) {
     if (lane == 0) {
       // ---- MMA issue
-      constexpr uint32_t idesc = make_idesc(TILE_M, NT);
       for (int kb = 0; kb < nk; ++kb) {
         const int st = kb % Cfg::STAGES;
         if (!mbar_wait(&full[st], (kb / Cfg::STAGES) & 1)) {
@@ -579,20 +611,7 @@ __global__ void __launch_bounds__(TC_THREADS, MINB)
         const bool second = KS == 2 && kb >= ksplit;
         const uint32_t acc_base = tmem + (second ? (uint32_t)(S * NT) : 0u);
         const bool first_kb = kb == (second ? ksplit : 0);   // the set's first K block overwrites it
-#pragma unroll
-        for (int d = 0; d < S; ++d) {
-#pragma unroll
-          for (int p = 0; p <= d; ++p) {
-            const int q = d - p;
-#pragma unroll
-            for (int kk = 0; kk < BK / 16; ++kk) {
-              const uint64_t da = da0 + (uint64_t)((p * Cfg::A_TILE + kk * 32) >> 4);
-              const uint64_t db = db0 + (uint64_t)((q * Cfg::B_TILE + kk * 32) >> 4);
-              const uint32_t acc = (!first_kb || p > 0 || kk > 0) ? 1u : 0u;
-              tc_mma(acc_base + d * NT, da, db, idesc, acc);
-            }
-          }
-        }
+        issue_stage_mmas<S, NT, Cfg::A_TILE, Cfg::B_TILE>(acc_base, da0, db0, first_kb);
         tc_commit(&empty[st]);
       }
       tc_commit(done);
@@ -788,7 +807,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     }
   } else if (warp == 1) {
     if (lane == 0) {
-      constexpr uint32_t idesc = make_idesc(TILE_M, NT);
       uint32_t kg = 0;
       int it = 0;
       bool stop = false;
@@ -813,20 +831,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           const uint32_t sa = smem_u32(smem + st * Cfg::STAGE);
           const uint32_t sb = sa + S * Cfg::A_TILE;
           const uint64_t da0 = make_desc(sa), db0 = make_desc(sb);
-#pragma unroll
-          for (int d = 0; d < S; ++d) {
-#pragma unroll
-            for (int p = 0; p <= d; ++p) {
-              const int q = d - p;
-#pragma unroll
-              for (int kk = 0; kk < BK / 16; ++kk) {
-                const uint64_t da = da0 + (uint64_t)((p * Cfg::A_TILE + kk * 32) >> 4);
-                const uint64_t db = db0 + (uint64_t)((q * Cfg::B_TILE + kk * 32) >> 4);
-                const uint32_t acc = (kb > 0 || p > 0 || kk > 0) ? 1u : 0u;
-                tc_mma(acc0 + d * NT, da, db, idesc, acc);
-              }
-            }
-          }
+          issue_stage_mmas<S, NT, Cfg::A_TILE, Cfg::B_TILE>(acc0, da0, db0, kb == 0);
           tc_commit(&empty[st]);
         }
         if (!stop) tc_commit(&tfull[buf]);
