@@ -546,7 +546,8 @@ int Engine::invert_impl(double2* A, long long sA, int batch, int* status_dev) {
       NEGF_CUDA_TRY(cudaMemcpyAsync(rk.data(), dRnorm_, sizeof(unsigned long long) * batch, cudaMemcpyDeviceToHost, st_));
     NEGF_TRY(slice_a(A, M_, sA, M_, M_, batch, s_upd_, sa_, st_));
     NEGF_TRY(slice_b(dT_, M_, MM_, M_, M_, batch, s_upd_, sb_, st_));
-    NEGF_TRY(zgemm_tc(sa_, sb_, one, one, A, M_, sA, dTcErr_, st_));              // X += X R
+    // X += X R; dT_ (R, already sliced) lends itself as the autotuner's scratch output
+    NEGF_TRY(zgemm_tc(sa_, sb_, one, one, A, M_, sA, dTcErr_, st_, 0, dT_));
   }
   NEGF_CUDA_TRY(cudaStreamSynchronize(st_));
   // Further steps only for the matrices whose residual norm before the last update was
@@ -576,7 +577,7 @@ int Engine::invert_impl(double2* A, long long sA, int batch, int* status_dev) {
     NEGF_CUDA_TRY(cudaMemcpyAsync(rk.data(), dRnorm_, sizeof(unsigned long long) * na, cudaMemcpyDeviceToHost, st_));
     NEGF_TRY(slice_a(dNsX_, M_, MM_, M_, M_, na, s_upd_, sa_, st_));
     NEGF_TRY(slice_b(dT_, M_, MM_, M_, M_, na, s_upd_, sb_, st_));
-    NEGF_TRY(zgemm_tc(sa_, sb_, one, one, dNsX_, M_, MM_, dTcErr_, st_));          // X += X R
+    NEGF_TRY(zgemm_tc(sa_, sb_, one, one, dNsX_, M_, MM_, dTcErr_, st_, 0, dT_));  // X += X R
     NEGF_TRY(scatter_strided(M_, na, dNsX_, MM_, dNsIdx_, A, sA, st_));
     NEGF_CUDA_TRY(cudaStreamSynchronize(st_));
     std::vector<int> next;

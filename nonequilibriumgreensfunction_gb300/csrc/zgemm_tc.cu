@@ -712,17 +712,26 @@ struct TcPCfg {
   static_assert(NT % 16 == 0 && NT >= 16 && NT <= 256, "UMMA N");
 };
 
-// named barrier 1 over the 128 epilogue threads that also ORs a predicate: every thread
-// gets the same answer, so the four warps always take the same branch out of a loop
+// Epilogue warps of the persistent kernel: two per TMEM lane quarter (a warp reaches the
+// 32 lanes of quarter warp % 4), which split the tile's columns chunk by chunk.  The
+// epilogue's work per output (S accumulator loads, integer recombination, the exact
+// conversion to FP64, the beta term) is long dependent integer code; with one warp per
+// sub-partition nothing hides its latency, and at 3 slices, whose K loop is short, it
+// outlasted the MMAs of the next tile.
+constexpr int TCP_EPI_WARPS = 8;
+constexpr int TCP_THREADS = 64 + 32 * TCP_EPI_WARPS;
+
+// named barrier 1 over the epilogue threads that also ORs a predicate: every thread gets
+// the same answer, so the epilogue warps always take the same branch out of a loop
 __device__ __forceinline__ bool epi_barrier_any(bool v) {
   uint32_t r;
   asm volatile(
       "{\n\t.reg .pred p, q;\n\t"
       "setp.ne.u32 p, %1, 0;\n\t"
-      "bar.red.or.pred q, 1, 128, p;\n\t"
+      "bar.red.or.pred q, 1, %2, p;\n\t"
       "selp.u32 %0, 1, 0, q;\n\t}"
       : "=r"(r)
-      : "r"((uint32_t)v)
+      : "r"((uint32_t)v), "n"(32 * TCP_EPI_WARPS)
       : "memory");
   return r != 0;
 }
@@ -732,7 +741,7 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
 }
 
 template <int S, int NT>
-__global__ void __launch_bounds__(TC_THREADS, 1)
+__global__ void __launch_bounds__(TCP_THREADS, 1)
     zgemm_tc_persistent(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, TcArgs a,
                         int tiles_m, int tiles_n) {
   using Cfg = TcPCfg<S, NT>;
@@ -754,7 +763,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < Cfg::STAGES; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
-    for (int s = 0; s < 2; ++s) { mbar_init(&tfull[s], 1); mbar_init(&tempty[s], 128); }
+    for (int s = 0; s < 2; ++s) { mbar_init(&tfull[s], 1); mbar_init(&tempty[s], 32 * TCP_EPI_WARPS); }
     mbar_init(fin, 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -849,11 +858,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       const int r = (int)(t % tiles_item);
       const int tm = r / tiles_n, tn = r % tiles_n;
       int* cexp = col_exp + buf * NT;
-      for (int c = threadIdx.x - 64; c < NT; c += 128) {
+      for (int c = threadIdx.x - 64; c < NT; c += 32 * TCP_EPI_WARPS) {
         const int col = tn * NT + c;
         cexp[c] = col < a.n ? a.fb[(long long)b * a.n + col] : 0;
       }
-      // the exponents are visible to all four warps, and all agree on stopping
+      // the exponents are visible to all epilogue warps, and all agree on stopping
       if (epi_barrier_any(*((volatile int*)abort_flag) != 0)) break;
       const bool ok = mbar_wait(&tfull[buf], (it >> 1) & 1);
       if (epi_barrier_any(!ok)) {
@@ -868,8 +877,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       double2* Cb = a.C + (long long)b * a.sC;
       const uint32_t acc0 = tmem + (uint32_t)(buf * Cfg::ACC);
       constexpr int CW = 8;   // fp32 columns per chunk
+      constexpr int NGRP = TCP_EPI_WARPS / 4;   // warps per lane quarter
+      const int grp = (warp - 2) >> 2;
 #pragma unroll 1
-      for (int c0 = 0; c0 < NT; c0 += CW) {
+      for (int c0 = grp * CW; c0 < NT; c0 += NGRP * CW) {
         constexpr int DH = S <= 6 ? S : 3;   // S <= 6 fits one int64; S >= 7 splits
         long long hi[CW], lo[CW];
 #pragma unroll
@@ -985,7 +996,7 @@ int launch_persistent(const SlicedOperand& A, const SlicedOperand& B, const TcAr
   const double cflops = 8.0 * args.m * (double)args.n * (args.kp / 2) * args.batch;
   add_tc_complex_flops(cflops);
   timed_begin(st, TK_TC, cflops * (S * (S + 1) / 2), &ev);
-  zgemm_tc_persistent<S, NT><<<grid, TC_THREADS, Cfg::SMEM, st>>>(ma, mb, args, tiles_m, tiles_n);
+  zgemm_tc_persistent<S, NT><<<grid, TCP_THREADS, Cfg::SMEM, st>>>(ma, mb, args, tiles_m, tiles_n);
   NEGF_CUDA_TRY(cudaGetLastError());
   timed_end(st, TK_TC, ev);
   count_launch();
@@ -1077,8 +1088,11 @@ namespace {
 // epilogue, so their results are bitwise identical and the choice never changes a number.
 // The first call of a shape with beta = 0 runs every variant three times (each run
 // overwrites C with the same values), times the last two runs with events on the caller's
-// stream and keeps the fastest; calls with beta != 0 before that use variant 0.  Beyond
-// K' = 800 only the per-tile kernel with two accumulator sets along K exists.
+// stream and keeps the fastest.  A first call with beta != 0 is tuned the same way when the
+// caller lends a scratch output (the timings run with beta = 0 into it, so C keeps its
+// input for the product itself); without one it uses variant 0 and leaves the shape
+// untuned.  Beyond K' = 800 only the per-tile kernel with two accumulator sets along K
+// exists.
 struct TuneKey {
   int S, m, n, kp, batch;
   bool operator<(const TuneKey& o) const {
@@ -1109,7 +1123,8 @@ float time_variant(int v, int S, const SlicedOperand& A, const SlicedOperand& B,
 }  // namespace
 
 // returns the variant to launch, or -2 when tuning already ran the product (C is written)
-int choose_variant(int S, const SlicedOperand& A, const SlicedOperand& B, const TcArgs& args, cudaStream_t st) {
+int choose_variant(int S, const SlicedOperand& A, const SlicedOperand& B, const TcArgs& args, cudaStream_t st,
+                   double2* tune_c) {
   int bb = 1;
   while (bb < args.batch) bb <<= 1;
   const TuneKey key{S, args.m, args.n, args.kp, bb};
@@ -1118,13 +1133,20 @@ int choose_variant(int S, const SlicedOperand& A, const SlicedOperand& B, const 
     auto it = g_tune.find(key);
     if (it != g_tune.end()) return it->second;
   }
-  if (args.beta_kind != 0 || args.kp > 800) return 0;
+  if (args.kp > 800 || (args.beta_kind != 0 && !tune_c)) return 0;
+  TcArgs targs = args;
+  if (args.beta_kind != 0) {   // time into the scratch with beta = 0
+    targs.C = tune_c;
+    targs.sC = (long long)args.ldc * args.n;
+    targs.beta = make_double2(0.0, 0.0);
+    targs.beta_kind = 0;
+  }
   // two timings each, after a first run of each that pays one-time costs
   float best[kVariants];
   for (int v = 0; v < kVariants; ++v) best[v] = 1e30f;
   for (int rep = 0; rep < 3; ++rep)
     for (int v = 0; v < kVariants; ++v) {
-      const float ms = time_variant(v, S, A, B, args, st);
+      const float ms = time_variant(v, S, A, B, targs, st);
       if (ms < 0.0f) return -3;
       if (rep > 0 && ms < best[v]) best[v] = ms;
     }
@@ -1133,11 +1155,11 @@ int choose_variant(int S, const SlicedOperand& A, const SlicedOperand& B, const 
     if (best[v] < best[choice]) choice = v;
   std::lock_guard<std::mutex> g(g_tune_mu);
   g_tune[key] = choice;
-  return -2;
+  return args.beta_kind != 0 ? choice : -2;   // with beta != 0 the product itself is still to run
 }
 
 int zgemm_tc(const SlicedOperand& A, const SlicedOperand& B, double2 alpha, double2 beta, double2* C, int ldc,
-             long long sC, int* err, cudaStream_t st, int slices) {
+             long long sC, int* err, cudaStream_t st, int slices, double2* tune_c) {
   // the leading `slices` digit planes of each operand (its own count by default); the
   // leading planes of a finer slicing are a coarser slicing of the same values
   const int S = slices ? slices : A.slices;
@@ -1162,7 +1184,7 @@ int zgemm_tc(const SlicedOperand& A, const SlicedOperand& B, double2 alpha, doub
     const int v = std::atoi(ev);
     if (ev[0] >= '0' && ev[0] <= '9' && v < kVariants) return launch_variant(v, S, A, B, args, st);
   }
-  const int variant = choose_variant(S, A, B, args, st);
+  const int variant = choose_variant(S, A, B, args, st, tune_c);
   if (variant == -2) return NEGF_OK;        // the tuning runs computed C
   if (variant == -3) return NEGF_ECUDA;
   return launch_variant(variant, S, A, B, args, st);

@@ -37,7 +37,10 @@ int slice_b(const double2* B, int ldb, long long sB, int k, int n, int batch, in
 // C = alpha A B + beta C (C column-major, ldc, batch stride sC); err: optional device flag.
 // slices = 0 uses every plane (A and B must have the same count); slices > 0 uses the
 // leading `slices` planes of each operand, which may have been sliced finer.
+// tune_c: optional scratch of ldc * n * batch complex values.  With it, the first call of a
+// shape with beta != 0 is also tuned: the variants are timed with beta = 0 writing into the
+// scratch (C itself is never touched by the timings), then the chosen one computes C.
 int zgemm_tc(const SlicedOperand& A, const SlicedOperand& B, double2 alpha, double2 beta, double2* C, int ldc,
-             long long sC, int* err, cudaStream_t st, int slices = 0);
+             long long sC, int* err, cudaStream_t st, int slices = 0, double2* tune_c = nullptr);
 
 }  // namespace negf
