@@ -630,14 +630,15 @@ def main():
         issued_tf = (tc_issued / (st["tc_ms"] * 1e-3) / 1e12) if (tc_issued and st["tc_ms"] > 0) else None
         bf16_peak = peaks.get("bf16_tflops")
         # DRAM traffic of one 5-slice RGF product launch (M = 400): an ncu capture of 16
-        # products (dram__bytes_read.sum + dram__bytes_write.sum = 154.4 + 27.7 MB) scaled
-        # to the step's 256 (the operands are per product, so the bytes grow in proportion),
-        # beside the launch's algorithmic bytes: each product's A and B slice planes read
-        # once (800 x 800 and 400 x 800 BF16 values per plane, 5 planes) and C written once
-        traffic = (154.427904e6 + 27.654912e6) * (args.batch / 16)
+        # products by the persistent kernel the autotuner picks at this shape
+        # (dram__bytes_read.sum + dram__bytes_write.sum = 153.8 + 23.8 MB) scaled to the
+        # step's 256 (the operands are per product, so the bytes grow in proportion), beside
+        # the launch's algorithmic bytes: each product's A and B slice planes read once
+        # (800 x 800 and 400 x 800 BF16 values per plane, 5 planes) and C written once
+        traffic = (153.795840e6 + 23.783168e6) * (args.batch / 16)
         algo_bytes = args.batch * (800 * 800 * 5 * 2 + 400 * 800 * 5 * 2 + 400 * 400 * 16)
         roofline = {
-            "bound": "tensor", "kernel": "zgemm_tc_kernel (tcgen05 sliced-BF16 complex GEMM)",
+            "bound": "tensor", "kernel": "zgemm_tc_persistent / zgemm_tc_kernel (tcgen05 sliced-BF16 complex GEMM)",
             "achieved": tc_tf, "peak": bf16_peak, "unit": "TFLOP/s",
             "frac": (tc_tf / bf16_peak) if (tc_tf and bf16_peak) else None, "traffic": traffic,
             "traffic_unit": "bytes per 5-slice product launch of the step's batch",

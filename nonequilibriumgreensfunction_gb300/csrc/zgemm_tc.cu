@@ -26,13 +26,14 @@
 // is set by S: truncation <= 2^-7S of the row/column maximum (S = 4: 4e-9, S = 5: 3e-11,
 // S = 7: 2e-15).
 //
-// Kernel structure (one 128 x NT output tile per CTA, 6 warps):
+// Kernel structure (one 128 x NT output tile per CTA, 10 warps):
 //   warp 0      TMA producer: for each K block of 32, S A-slices (128 x 32) and S B-slices
 //               (NT x 32) into a ring of shared-memory stages (SWIZZLE_64B, K-major).
 //   warp 1      TMEM allocation and the single-thread tcgen05.mma issue loop (one MMA per
 //               A slice, spanning the B slices it pairs with); commits release the stage
 //               and, at the end, signal the epilogue.
-//   warps 2-5   epilogue: tcgen05.ld of the S accumulators, FP64 recombination; lanes
+//   warps 2-9   epilogue, two warps per TMEM lane quarter taking the tile's column chunks
+//               in turn: tcgen05.ld of the S accumulators, FP64 recombination; lanes
 //               2i and 2i+1 hold the real and imaginary parts of C row i and exchange
 //               them with one shuffle, the even lane storing the even columns and the
 //               odd lane the odd ones.
@@ -56,7 +57,13 @@ namespace negf {
 
 namespace {
 
-constexpr int TC_THREADS = 192;
+// Epilogue warps of both kernels: two per TMEM lane quarter (a warp reaches the 32 lanes of
+// quarter warp % 4), which split the tile's columns chunk by chunk.  The epilogue's work per
+// output (S accumulator loads, integer recombination, the exact conversion to FP64, the beta
+// term) is long dependent integer code; with one warp per sub-partition nothing hides its
+// latency, and at 3 slices, whose K loop is short, it outlasted the MMAs of the next tile.
+constexpr int TC_EPI_WARPS = 8;
+constexpr int TC_THREADS = 64 + 32 * TC_EPI_WARPS;   // producer, MMA issuer, epilogue
 #ifndef TC_BK
 #define TC_BK 32
 #endif
@@ -621,11 +628,11 @@ __global__ void __launch_bounds__(TC_THREADS, MINB)
     // output row tm*128 + l.  While the MMAs run, stage the tile's column exponents in
     // shared memory.
     const int quarter = warp & 3;
-    for (int c = threadIdx.x - 64; c < NT; c += 128) {
+    for (int c = threadIdx.x - 64; c < NT; c += 32 * TC_EPI_WARPS) {
       const int col = tn * NT + c;
       col_exp[c] = col < a.n ? a.fb[(long long)b * a.n + col] : 0;
     }
-    asm volatile("bar.sync 1, 128;" ::: "memory");   // the four epilogue warps only
+    asm volatile("bar.sync 1, %0;" ::"n"(32 * TC_EPI_WARPS) : "memory");   // the epilogue warps only
     const bool ok = mbar_wait(done, 0);
     if (!ok && a.err) atomicCAS(a.err, 0, 3);
     tc_fence_after();
@@ -634,9 +641,11 @@ __global__ void __launch_bounds__(TC_THREADS, MINB)
     const bool aborted = !ok || *((volatile int*)abort_flag);
     const int e_row = (row < a.m) ? a.ea[(long long)b * a.m + row] : 0;
     double2* Cb = a.C + (long long)b * a.sC;
-    constexpr int CW = (S >= 7 || MINB == 2 || NT % 16 != 0) ? 8 : 16;   // fp32 columns per chunk
+    constexpr int CW = (S >= 7 || MINB == 2 || KS == 2 || NT % 16 != 0) ? 8 : 16;   // fp32 columns per chunk
+    constexpr int NGRP = TC_EPI_WARPS / 4;   // warps per lane quarter, taking chunks in turn
+    const int grp = (warp - 2) >> 2;
 #pragma unroll 1
-    for (int c0 = 0; c0 < NT; c0 += CW) {
+    for (int c0 = grp * CW; c0 < NT; c0 += NGRP * CW) {
       // exact recombination of the diagonal accumulators (integer-valued FP32) in int64:
       // hi = sum_{d<DH} acc_d 2^(7(DH-1-d)), lo = sum_{d>=DH} acc_d 2^(7(S-1-d))
       constexpr int DH = S <= 6 ? S : 3;   // S <= 6 fits one int64; S >= 7 splits
@@ -691,9 +700,9 @@ __global__ void __launch_bounds__(TC_THREADS, MINB)
 // overlaps the MMAs of the next and the producer keeps STAGES - 1 stages in flight.
 //   warp 0     TMA producer over (tile, K block)
 //   warp 1     TMEM allocation; MMA issue into accumulator set (tile count & 1)
-//   warps 2-5  epilogue of each tile from its accumulator set, then release the set
+//   warps 2-9  epilogue of each tile from its accumulator set, then release the set
 // Barriers: full/empty per stage (as the per-tile kernel), tfull[2] (MMA commit -> epilogue)
-// and tempty[2] (128 epilogue arrivals -> MMA).  Every wait is bounded; a timeout sets the
+// and tempty[2] (one arrival per epilogue thread -> MMA).  Every wait is bounded; a timeout sets the
 // abort flag and the error code, every role leaves its loop, and the MMA warp waits for
 // its issued MMAs to complete before TMEM is freed.
 // ---------------------------------------------------------------------------------
@@ -712,15 +721,6 @@ struct TcPCfg {
   static_assert(NT % 16 == 0 && NT >= 16 && NT <= 256, "UMMA N");
 };
 
-// Epilogue warps of the persistent kernel: two per TMEM lane quarter (a warp reaches the
-// 32 lanes of quarter warp % 4), which split the tile's columns chunk by chunk.  The
-// epilogue's work per output (S accumulator loads, integer recombination, the exact
-// conversion to FP64, the beta term) is long dependent integer code; with one warp per
-// sub-partition nothing hides its latency, and at 3 slices, whose K loop is short, it
-// outlasted the MMAs of the next tile.
-constexpr int TCP_EPI_WARPS = 8;
-constexpr int TCP_THREADS = 64 + 32 * TCP_EPI_WARPS;
-
 // named barrier 1 over the epilogue threads that also ORs a predicate: every thread gets
 // the same answer, so the epilogue warps always take the same branch out of a loop
 __device__ __forceinline__ bool epi_barrier_any(bool v) {
@@ -731,7 +731,7 @@ __device__ __forceinline__ bool epi_barrier_any(bool v) {
       "bar.red.or.pred q, 1, %2, p;\n\t"
       "selp.u32 %0, 1, 0, q;\n\t}"
       : "=r"(r)
-      : "r"((uint32_t)v), "n"(32 * TCP_EPI_WARPS)
+      : "r"((uint32_t)v), "n"(32 * TC_EPI_WARPS)
       : "memory");
   return r != 0;
 }
@@ -741,7 +741,7 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
 }
 
 template <int S, int NT>
-__global__ void __launch_bounds__(TCP_THREADS, 1)
+__global__ void __launch_bounds__(TC_THREADS, 1)
     zgemm_tc_persistent(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, TcArgs a,
                         int tiles_m, int tiles_n) {
   using Cfg = TcPCfg<S, NT>;
@@ -763,7 +763,7 @@ __global__ void __launch_bounds__(TCP_THREADS, 1)
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < Cfg::STAGES; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
-    for (int s = 0; s < 2; ++s) { mbar_init(&tfull[s], 1); mbar_init(&tempty[s], 32 * TCP_EPI_WARPS); }
+    for (int s = 0; s < 2; ++s) { mbar_init(&tfull[s], 1); mbar_init(&tempty[s], 32 * TC_EPI_WARPS); }
     mbar_init(fin, 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -858,7 +858,7 @@ __global__ void __launch_bounds__(TCP_THREADS, 1)
       const int r = (int)(t % tiles_item);
       const int tm = r / tiles_n, tn = r % tiles_n;
       int* cexp = col_exp + buf * NT;
-      for (int c = threadIdx.x - 64; c < NT; c += 32 * TCP_EPI_WARPS) {
+      for (int c = threadIdx.x - 64; c < NT; c += 32 * TC_EPI_WARPS) {
         const int col = tn * NT + c;
         cexp[c] = col < a.n ? a.fb[(long long)b * a.n + col] : 0;
       }
@@ -877,7 +877,7 @@ __global__ void __launch_bounds__(TCP_THREADS, 1)
       double2* Cb = a.C + (long long)b * a.sC;
       const uint32_t acc0 = tmem + (uint32_t)(buf * Cfg::ACC);
       constexpr int CW = 8;   // fp32 columns per chunk
-      constexpr int NGRP = TCP_EPI_WARPS / 4;   // warps per lane quarter
+      constexpr int NGRP = TC_EPI_WARPS / 4;   // warps per lane quarter
       const int grp = (warp - 2) >> 2;
 #pragma unroll 1
       for (int c0 = grp * CW; c0 < NT; c0 += NGRP * CW) {
@@ -996,7 +996,7 @@ int launch_persistent(const SlicedOperand& A, const SlicedOperand& B, const TcAr
   const double cflops = 8.0 * args.m * (double)args.n * (args.kp / 2) * args.batch;
   add_tc_complex_flops(cflops);
   timed_begin(st, TK_TC, cflops * (S * (S + 1) / 2), &ev);
-  zgemm_tc_persistent<S, NT><<<grid, TCP_THREADS, Cfg::SMEM, st>>>(ma, mb, args, tiles_m, tiles_n);
+  zgemm_tc_persistent<S, NT><<<grid, TC_THREADS, Cfg::SMEM, st>>>(ma, mb, args, tiles_m, tiles_n);
   NEGF_CUDA_TRY(cudaGetLastError());
   timed_end(st, TK_TC, ev);
   count_launch();
