@@ -273,6 +273,109 @@ __global__ void __launch_bounds__(256, sizeof(T) == 8 ? 2 : 1) gj_update_kernel(
   }
 }
 
+// The FP32 rank-kb update as a persistent, software-pipelined kernel (two CTAs per SM, each
+// walking output tiles of 80 x 80).  While a CTA computes one tile, cp.async copies the P
+// and R slabs of its next tile into the other half of a double buffer, and the tile's C
+// values load into registers behind the k loop; the one-tile-per-CTA form above ran its
+// load, compute and store phases back to back with two CTAs per SM to overlap them.  Each
+// output element is formed by exactly the operations of gj_update_kernel (the same k order
+// of fused multiply-adds from the same slabs, then A + sum), so results are bitwise equal.
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem, int src_bytes) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"((uint32_t)__cvta_generic_to_shared(smem)),
+               "l"(gmem), "r"(src_bytes)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+constexpr int UPD_SLABS = 32 * UPD_T + 32 * UPD_RS;   // float2 of one buffer: P slab, then R slab
+
+__global__ void __launch_bounds__(256, 2) gj_update_f32_pipelined(float2* A, long long sA, int n, int k0, int kb,
+                                                                  const float2* R, long long sR, int ntm, int ntn,
+                                                                  long long ntiles) {
+  extern __shared__ __align__(16) unsigned char upp_raw[];
+  float2* bufs = reinterpret_cast<float2*>(upp_raw);   // [2][UPD_SLABS]
+  const int t = threadIdx.x;
+  const int tx = t & 15, ty = t >> 4;
+  const long long per_item = (long long)ntm * ntn;
+  // copies of tile q's slabs into buffer Ps (P slab [kb][UPD_T], R slab [kb][UPD_RS]);
+  // entries outside A are zero-filled without a read
+  auto issue = [&](long long q, float2* Ps) {
+    const int b = (int)(q / per_item);
+    const int r = (int)(q % per_item);
+    const int m0 = (r / ntn) * UPD_T, n0 = (r % ntn) * UPD_T;
+    const float2* Ab = A + (long long)b * sA;
+    const float2* Rb = R + (long long)b * sR;
+    float2* Rs = Ps + 32 * UPD_T;
+    for (int e = t; e < kb * UPD_T; e += 256) {
+      const int k = e / UPD_T, i = e % UPD_T;
+      const bool okp = m0 + i < n;
+      cp_async8(&Ps[k * UPD_T + i], okp ? (const void*)&Ab[(long long)(k0 + k) * n + m0 + i] : (const void*)Ab,
+                okp ? 8 : 0);
+      const int j = e / kb, kk = e % kb;
+      const bool okr = n0 + j < n;
+      cp_async8(&Rs[kk * UPD_RS + j], okr ? (const void*)&Rb[(long long)(n0 + j) * kb + kk] : (const void*)Rb,
+                okr ? 8 : 0);
+    }
+    cp_async_commit();
+  };
+  long long q = blockIdx.x;
+  if (q < ntiles) issue(q, bufs);
+  for (int it = 0; q < ntiles; q += gridDim.x, ++it) {
+    const float2* Ps = bufs + (it & 1) * UPD_SLABS;
+    const float2* Rs = Ps + 32 * UPD_T;
+    const int b = (int)(q / per_item);
+    const int r = (int)(q % per_item);
+    const int m0 = (r / ntn) * UPD_T, n0 = (r % ntn) * UPD_T;
+    float2* Ab = A + (long long)b * sA;
+    auto updated = [&](int i, int j) -> float2* {   // nullptr: outside A or in the panel
+      const int row = m0 + tx + 16 * i, col = n0 + ty + 16 * j;
+      if (row >= n || col >= n || (col >= k0 && col < k0 + kb)) return nullptr;
+      return Ab + (long long)col * n + row;
+    };
+    float2 cin[UPD_R][UPD_R];
+#pragma unroll
+    for (int j = 0; j < UPD_R; ++j)
+#pragma unroll
+      for (int i = 0; i < UPD_R; ++i) {
+        const float2* cp = updated(i, j);
+        cin[i][j] = cp ? *cp : make_float2(0.0f, 0.0f);
+      }
+    // the next tile's slabs go into the other buffer, which every thread finished reading
+    // before the barrier that ended the previous iteration
+    if (q + gridDim.x < ntiles) issue(q + gridDim.x, bufs + ((it + 1) & 1) * UPD_SLABS);
+    else cp_async_commit();   // an empty group keeps the count: wait_group 1 below = this tile
+    cp_async_wait<1>();
+    __syncthreads();
+    float2 acc[UPD_R][UPD_R];
+#pragma unroll
+    for (int i = 0; i < UPD_R; ++i)
+#pragma unroll
+      for (int j = 0; j < UPD_R; ++j) acc[i][j] = make_float2(0.0f, 0.0f);
+    for (int k = 0; k < kb; ++k) {
+      float2 av[UPD_R], bv[UPD_R];
+#pragma unroll
+      for (int i = 0; i < UPD_R; ++i) av[i] = Ps[k * UPD_T + tx + 16 * i];
+#pragma unroll
+      for (int j = 0; j < UPD_R; ++j) bv[j] = Rs[k * UPD_RS + ty + 16 * j];
+#pragma unroll
+      for (int i = 0; i < UPD_R; ++i)
+#pragma unroll
+        for (int j = 0; j < UPD_R; ++j) cfma(acc[i][j], av[i], bv[j]);
+    }
+#pragma unroll
+    for (int j = 0; j < UPD_R; ++j)
+#pragma unroll
+      for (int i = 0; i < UPD_R; ++i) {
+        float2* cp = updated(i, j);
+        if (cp) *cp = cadd(acc[i][j], cin[i][j]);
+      }
+    __syncthreads();   // this buffer is free for the tile after next
+  }
+  cp_async_wait<0>();
+}
+
 // One thread per row: column interchanges in reverse pivot order.
 template <typename T>
 __global__ void gj_colswap_kernel(T* A, long long sA, int n, const int* ipiv) {
@@ -500,6 +603,10 @@ int gj_invert(T* A, long long sA, int n, int batch, InvWork& w, cudaStream_t st)
   NEGF_CUDA_TRY(cudaFuncSetAttribute(gj_panel_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPanelSmemMax));
   const size_t upd_smem = sizeof(T) * 32 * (UPD_T + UPD_RS);
   NEGF_CUDA_TRY(cudaFuncSetAttribute(gj_update_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)upd_smem));
+  const size_t upp_smem = sizeof(float2) * 2 * (size_t)UPD_SLABS;
+  if constexpr (sizeof(T) == 8)
+    NEGF_CUDA_TRY(cudaFuncSetAttribute(gj_update_f32_pipelined, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)upp_smem));
   if (nb > 32 || batch > 65535) return NEGF_EINVAL;
   NEGF_CUDA_TRY(cudaMemsetAsync(w.info, 0, sizeof(int) * batch, st));
   T* rbuf = reinterpret_cast<T*>(w.rbuf);
@@ -519,8 +626,17 @@ int gj_invert(T* A, long long sA, int n, int batch, InvWork& w, cudaStream_t st)
     {
       cudaEvent_t eu;
       timed_begin(st, sizeof(T) == 8 ? TK_F32 : TK_GEMM, 8.0 * n * (double)(n - kb) * kb * batch, &eu);
-      dim3 gu((n + UPD_T - 1) / UPD_T, (n + UPD_T - 1) / UPD_T, batch);
-      gj_update_kernel<T><<<gu, 256, upd_smem, st>>>(A, sA, n, k0, kb, rbuf, sR);
+      const int nt = (n + UPD_T - 1) / UPD_T;
+      if constexpr (sizeof(T) == 8) {
+        const long long ntiles = (long long)nt * nt * batch;
+        const int grid = (int)std::min<long long>(ntiles, 2LL * sm_count_cached());
+        gj_update_f32_pipelined<<<grid, 256, upp_smem, st>>>(reinterpret_cast<float2*>(A), sA, n, k0, kb,
+                                                             reinterpret_cast<const float2*>(rbuf), sR, nt, nt,
+                                                             ntiles);
+      } else {
+        dim3 gu(nt, nt, batch);
+        gj_update_kernel<T><<<gu, 256, upd_smem, st>>>(A, sA, n, k0, kb, rbuf, sR);
+      }
       NEGF_CUDA_TRY(cudaGetLastError());
       timed_end(st, sizeof(T) == 8 ? TK_F32 : TK_GEMM, eu);
       count_launch();
