@@ -58,19 +58,28 @@ __device__ __forceinline__ void panel_factor(T* Ps, int n, int k0, int kb, int* 
     }
     if (lane == 0) { red_v[warp] = bv; red_i[warp] = bi; }
     __syncthreads();
-    if (t == 0) {
-      R v = red_v[0];
-      int i = red_i[0];
-      for (int w = 1; w < nwarps; ++w) argmax_combine(v, i, red_v[w], red_i[w]);
-      if (i >= n) i = r;
-      *s_piv = i;
-      ip[r] = i;
-      T pv = col[i];
-      if (pv.x == 0 && pv.y == 0) {
-        if (*info_b == 0) *info_b = r + 1;
-        *s_d = CplxTraits<T>::make(0, 0);
-      } else {
-        *s_d = crcp(pv);
+    // second level by warp 0 with shuffles (the maximum under "larger value, then lower
+    // index" does not depend on the order of the comparisons)
+    if (warp == 0) {
+      R v = lane < nwarps ? red_v[lane] : (R)-1;
+      int i = lane < nwarps ? red_i[lane] : n;
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        R ov = __shfl_down_sync(0xffffffffu, v, off);
+        int oi = __shfl_down_sync(0xffffffffu, i, off);
+        argmax_combine(v, i, ov, oi);
+      }
+      if (lane == 0) {
+        if (i >= n) i = r;
+        *s_piv = i;
+        ip[r] = i;
+        T pv = col[i];
+        if (pv.x == 0 && pv.y == 0) {
+          if (*info_b == 0) *info_b = r + 1;
+          *s_d = CplxTraits<T>::make(0, 0);
+        } else {
+          *s_d = crcp(pv);
+        }
       }
     }
     __syncthreads();
@@ -87,11 +96,33 @@ __device__ __forceinline__ void panel_factor(T* Ps, int n, int k0, int kb, int* 
     }
     __syncthreads();
     if (singular) continue;
-    // ---- eliminate column c from every other row; row i is owned by one thread
+    // ---- eliminate column c from every other row; row i is owned by one thread, which
+    // loads EU columns of its row and of the pivot row before any arithmetic or store (the
+    // row's elements are independent, so this only removes the wait on each load)
+    constexpr int EU = 8;
     for (int i = t; i < n; i += nth) {
       if (i == r) continue;
       const T f = col[i];
-      for (int j = 0; j < kb; ++j) {
+      int j0 = 0;
+      for (; j0 + EU <= kb; j0 += EU) {
+        T rv[EU], v[EU];
+#pragma unroll
+        for (int q = 0; q < EU; ++q) {
+          const T* cj = Ps + (long long)(j0 + q) * n;
+          rv[q] = cj[r];
+          v[q] = cj[i];
+        }
+#pragma unroll
+        for (int q = 0; q < EU; ++q) {
+          if (j0 + q == c) continue;
+          v[q].x = fma((R)-f.x, rv[q].x, v[q].x);
+          v[q].x = fma(f.y, rv[q].y, v[q].x);
+          v[q].y = fma((R)-f.x, rv[q].y, v[q].y);
+          v[q].y = fma((R)-f.y, rv[q].x, v[q].y);
+          Ps[(long long)(j0 + q) * n + i] = v[q];
+        }
+      }
+      for (int j = j0; j < kb; ++j) {
         if (j == c) continue;
         T* cj = Ps + (long long)j * n;
         const T rv = cj[r];
