@@ -76,7 +76,7 @@ def max_over_ranks(value, dist, device):
     return float(t.item())
 
 
-def survey_flops_per_solve(m, npx, n_sr, n_leads=2):
+def scope_flops_per_solve(m, npx, n_sr, n_leads=2):
     """The work model of the hot-path scope table (real flops per energy point):
     F = 96 M^3 Npx + n_leads (72 n_SR + 56) M^3 + 16 M^3 -- per slice 12 complex M^3
     products or inverses of 8 M^3 each (both sweeps, both column propagations, the two
@@ -657,7 +657,7 @@ def main():
         k: st[k] * 1e-3 / args.steps for k in ("phase_sr_ms", "phase_rgf_ms", "phase_inv_ms", "phase_dens_ms",
                                                "tc_ms", "gemm_ms", "panel_ms", "f32_gemm_ms", "slice_ms")}
     flops_solve = algorithmic_flops_per_solve(m, NPX, sr_iters)
-    flops_survey = survey_flops_per_solve(m, NPX, sr_iters)
+    flops_scope = scope_flops_per_solve(m, NPX, sr_iters)
     serving = None
     if args.serving_seconds > 0 and world == 1:
         if solver is not None:
@@ -681,8 +681,8 @@ def main():
         "algorithmic_flops_per_solve": flops_solve,
         "algorithmic_model": "48 M^3 Npx + (88 n_SR + 24) M^3 / seeds + 32 M^3 (the work this solver "
                              "does: site-local HopX, decimation shared by the seeds of an energy)",
-        "solve_tflops_survey_model": flops_survey * value / 1e12 / world,
-        "survey_flops_per_solve": flops_survey,
+        "solve_tflops_scope_model": flops_scope * value / 1e12 / world,
+        "scope_flops_per_solve": flops_scope,
         "sr_iters": sr_iters,
         "cpu_baseline": cpu,
         "fp64_form": fp64,
