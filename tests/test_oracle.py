@@ -352,3 +352,21 @@ def test_spin_and_pairing_matrices_follow_the_orbital_count():
     assert all(not g.any() for g in O.reference_spin_matrices(1))
     assert np.array_equal(O.reference_gds(2), np.array([[0, 1], [-1, 0]], dtype=complex))
     assert np.array_equal(O.reference_spin_matrices(4)[0], O.reference_gamma_matrices()[4])
+
+
+def test_surface_model_josephson_current_is_odd_in_the_phase():
+    """Superconducting contacts on the two-orbital TI surface (channelType 3, BdG with
+    Nh = 2: gDS = [[0, 1], [-1, 0]], Read_In_Allocate.F90:214-215): the spectral supercurrent
+    of Calculate_Observables.F90:60-81 vanishes at chi = 0 and pi and is odd in chi."""
+    h, x = O.build_hamiltonian_reference(6, 3, 1, channel_type=3)
+    hb, xb = O.bdg_hamiltonian(h, x, 3, 1, nh=2)
+
+    def t12(chi, e):
+        opt = O.SolveOptions(eta=1e-5, sr_tol=1e-10, norb=4, contact_type=3, chi_lr=chi)
+        return O.energy_sweep(hb, xb, e, (0.0, 0.0), 1e-4, 3, 1, opt)["T12"]
+
+    for e in (-5e-4, 7e-4):
+        plus, minus = t12(0.3, e), t12(-0.3, e)
+        assert abs(plus) > 1e-5
+        assert abs(plus + minus) <= 1e-9 * abs(plus)
+        assert abs(t12(0.0, e)) <= 1e-12 and abs(t12(np.pi, e)) <= 1e-12
