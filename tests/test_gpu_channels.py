@@ -155,3 +155,25 @@ def test_builder_refuses_blocks_outside_norb(need_gpu):
         with pytest.raises(capi.NegfError):
             s.build_hamiltonian(m4)
         s.build_hamiltonian(m)
+
+
+def test_superconducting_contacts_on_the_surface_model(need_gpu):
+    """The TI surface strip (channelType 3, two orbitals) between superconducting contacts:
+    a BdG Hamiltonian of norb = 4 with the Nh = 2 pairing matrix
+    (Read_In_Allocate.F90:214-215).  Supercurrent transmission, electron-only densities and
+    spin against the oracle, per energy, to 1e-9 (in-gap quantities against their scale)."""
+    import importlib.util
+    import os
+    spec = importlib.util.spec_from_file_location("contacts", os.path.join(os.path.dirname(__file__),
+                                                                           "test_gpu_contacts.py"))
+    tc = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(tc)
+    npx, npy, npz = 5, 3, 1
+    h2, x2 = HB.build_from_model(npx, npy, npz, HB.channel_model(3, W=0.2, seed=12))
+    h, x = HB.bdg(h2, x2, npy, npz, nh=2)
+    opt = O.SolveOptions(eta=1e-4, norb=4, contact_type=3, chi_lr=0.8, calc_spin=True)
+    kw = dict(norb=4, eta=1e-4, contact_type=3, chi_lr=0.8, delta_sc=(1e-3, 1e-3), calc_spin=True)
+    with Solver(npx, npy, npz, **kw) as s:
+        s.set_hamiltonian(h, x)
+        tc._check_per_energy(s, h, x, np.linspace(-1.1e-3, 1.1e-3, 5), opt, (0.0, 0.0), 2.2e-3 / 4, npy, npz,
+                             currents=False)
