@@ -179,3 +179,29 @@ def test_device_bytes_estimate_needs_no_device():
     assert est(npy=15, npz=14)[0] == capi.NEGF_EINVAL         # M = 840 > 800 in the mixed form
     assert est(npy=15, npz=14, precision=capi.NEGF_PREC_FP64)[0] == capi.NEGF_OK
     assert est(batch=0)[0] == capi.NEGF_EINVAL
+
+
+def test_wire_model_struct_pads_smaller_site_blocks():
+    """negf_wire_model holds 4 x 4 blocks; a channel model of norb < 4 goes into their leading
+    norb x norb corner (row-major [row][col][re, im]) with zeros elsewhere, which the device
+    builder requires."""
+    import numpy as np
+    from nonequilibriumgreensfunction_gb300 import capi
+    from nonequilibriumgreensfunction_gb300 import hamiltonian as HB
+    for ct in (2, 3, 4):
+        model = HB.channel_model(ct, mu_t=0.2, W=0.1, seed=3)
+        n = HB.CHANNEL_NORB[ct]
+        m, keep = capi.wire_model_struct(model, (4, 1, 1))
+        onsite = np.array(m.onsite[:]).reshape(4, 4, 2)
+        hops = np.array(m.hop[:]).reshape(3, 4, 4, 2)
+        want = np.asarray(model["onsite"])
+        assert np.array_equal(onsite[:n, :n, 0], want.real) and np.array_equal(onsite[:n, :n, 1], want.imag)
+        for j in range(3):
+            hj = np.asarray(model["hops"][j])
+            assert np.array_equal(hops[j, :n, :n, 0], hj.real) and np.array_equal(hops[j, :n, :n, 1], hj.imag)
+        mask = np.ones((4, 4), dtype=bool)
+        mask[:n, :n] = False
+        assert not onsite[mask].any() and not hops[:, mask].any()
+        assert m.W == 0.1 and m.seed == 3 and keep is None
+    with pytest.raises(ValueError):
+        capi.wire_model_struct(dict(onsite=np.eye(5), hops=(np.eye(5),) * 3, flux=0.0, W=0.0, seed=0), (4, 1, 1))
