@@ -14,9 +14,11 @@ reference calls through MKL), the reference's per-energy path:
     Source/Recursive_Greens.F90:2-107       get_retarded_greens()
     Source/Calculate_Gnp.F90:1-136          calculate_gnp()
     Source/Calculate_Observables.F90:2-169  calculate_observables()
-    Source/Build_Hamiltonian.F90:1-207      build_hamiltonian_reference() (model 0 only)
+    Source/Build_Hamiltonian.F90:1-207      build_hamiltonian_reference() (channel models 0-4)
+    Source/Build_Hamiltonian.F90:13-47      channel_blocks(); Read_In_Allocate.F90:51-65 channel_norb()
+    Source/NEGF_Module.F90:7,10-17          Bi2Se3 parameters and tMet
     Source/Build_Hamiltonian.F90:52-56,162-163,199-200   bdg_hamiltonian()
-    Source/Read_In_Allocate.F90:161-197     gamma matrices
+    Source/Read_In_Allocate.F90:151-216     gamma, spin and pairing matrices for Nh = 4, 2, 1
 
 The algorithm follows the reference step by step: the backward GRd/GRu/GRl recursion
 is kept, Gn/Gp are formed as full blocks, and the same zgemm products are taken in
@@ -28,9 +30,10 @@ Parity status: UNPINNED against the reference executable.  The reference is Fort
 + MKL + MPI; no Fortran compiler exists in the build container or on the GPU host, and
 the reference ships no tests, golden vectors or fixtures.  The oracle is pinned instead
 by (i) a dense inversion of the full (Npx*M)^2 matrix, (ii) physics invariants (integer
-transmission of a clean wire, L<->R reciprocity, the A = Gn + Gp sum rule, the surface
-Dyson equation of the lead self-energy) and (iii) committed golden vectors it generated
-(tests/golden/make_golden.py).
+transmission of a clean wire, the exact open-mode count of the one-band metal and the two
+channels of the 1-D spin-orbit wire, L<->R reciprocity, the A = Gn + Gp sum rule, the
+surface Dyson equation of the lead self-energy, a Josephson current odd in the phase) and
+(iii) committed golden vectors it generated (tests/golden/make_golden.py).
 
 Reference quirks are exposed as parameters of ``SolveOptions``; the defaults are the
 reference's own values (eta = 1e-4, Sancho-Rubio tolerance 1e-8, T=0 step occupations).
